@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark of the preconditioned Krylov path on one GB300.
+
+Workload (the reference's measured configuration that fits one GPU): 3D 7-point
+upwind convection-diffusion on a 128^3 grid (N = 2,097,152, nnz = 14,581,760),
+unit diffusion, velocity (1,1,1), cell Peclet 0.5; b = A x_true with
+x_true ~ U(-1,1) (seed 0); ABMC ordering with block size 16 ("connect",
+A + A^T graph); ILU(0); right-preconditioned GMRES(30) in FP64 to a 1e-8
+relative residual (x0 = 0).
+
+A step is one complete solve. ``value`` is the mean solve time with A, the
+factors, b and the Krylov workspace resident in HBM (CUDA events on the
+library's stream); ``e2e`` is the same solve through the drop-in C ABI call with
+host arrays (upload, factor re-layout, solve and copy-back of x inside the timed
+region). Inputs are larger than L2 (A + L + U + V is about 0.9 GB), so no flush
+is needed between steps.
+
+    python bench.py [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solve ms to 1e-8 rel. residual (ABMC-ILU(0)-GMRES(30), FP64)"
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="grid points per dimension")
+    ap.add_argument("--m", type=int, default=30)
+    ap.add_argument("--eps", type=float, default=1e-8)
+    ap.add_argument("--orth", default="cgs2", choices=["cgs2", "cgs", "mgs"])
+    ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload_name(n):
+    return f"convdiff3d {n}^3, Pe 0.5, ABMC bsize 16 (connect), ILU(0), GMRES(30), eps 1e-8, x0=0"
+
+
+def problem(n):
+    from senk_gb300 import problems as P
+    A = P.convdiff3d(n, 0.5)
+    xt = P.uniform_solution(A.n, 0)
+    return A, xt
+
+
+def setup_gpu(A, xt):
+    """Product host setup (include/senk_*.hpp through the C ABI)."""
+    from senk_gb300 import setup as S
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    Lf, Uf, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
+    b = Ar.matvec(xt[LP])
+    return Ar, Lf, Uf, nc, sc, b
+
+
+def setup_oracle(port, A, xt):
+    nc, sc, LP, RP = port.abmc_permutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = port.reordering(A, LP, RP)
+    Lf, Uf, _ = port.split(port.ilu0(Ar), "L-DU", True)
+    b = Ar.matvec(xt[LP])
+    return Ar, Lf, Uf, nc, sc, b
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.proc = None
+        self.lines = []
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_for(kernel):
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_solve(port, Ar, Lf, Uf, nc, sc, b, eps, m, threads):
+    import oracle
+    port.set_threads(threads)
+    t0 = time.perf_counter()
+    x, it, res, conv = port.solve("gmres", Ar, b, L=Lf, U=Uf, pc=oracle.PC_ILU_ABMC, cptr=sc, cnum=nc, bsize=16,
+                                  outer=10000 // m, m=m, eps=eps, nrm_b=float(np.linalg.norm(b)))
+    ms = (time.perf_counter() - t0) * 1e3
+    port.set_threads(1)
+    return ms, it, x
+
+
+def run_reference(args, rank):
+    """The reference's CPU algorithm (the C restatement in oracle/, OpenMP over all
+    host cores) on the same workload."""
+    if rank != 0:
+        return
+    import oracle
+    port = oracle.port()
+    threads = os.cpu_count() or 1
+    A, xt = problem(args.n)
+    Ar, Lf, Uf, nc, sc, b = setup_oracle(port, A, xt)
+    for _ in range(args.warmup):
+        cpu_solve(port, Ar, Lf, Uf, nc, sc, b, args.eps, args.m, threads)
+    times, its = [], []
+    for _ in range(args.steps):
+        ms, it, x = cpu_solve(port, Ar, Lf, Uf, nc, sc, b, args.eps, args.m, threads)
+        times.append(ms)
+        its.append(it)
+    v = sum(times) / len(times)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_name(args.n), "N": A.n, "nnz": A.nnz, "colours": nc,
+                       "iterations": its[-1]},
+            "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
+                             "sample": "full solves of the workload (oracle C restatement of the reference, "
+                                       "OpenMP, reference compiled headers are not available on this host)"},
+            "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world):
+    from senk_gb300 import lib as L
+    from senk_gb300 import solver as SV
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    L.check("set_device", L.lib().senk_set_device(local))
+    A, xt = problem(args.n)
+    Ar, Lf, Uf, nc, sc, b = setup_gpu(A, xt)
+    nb = float(np.linalg.norm(b))
+    orth = {"cgs2": L.ORTH_CGS2, "cgs": L.ORTH_CGS, "mgs": L.ORTH_MGS}[args.orth]
+    spmv = {"auto": L.SPMV_AUTO, "csr": L.SPMV_CSR, "sell": L.SPMV_SELL}[args.spmv]
+    outer = 10000 // args.m
+    sysm = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=args.m, orth=orth, spmv=spmv)
+    sysm.set_rhs(b)
+    for _ in range(args.warmup):
+        sysm.zero_x()
+        sysm.gmres(nb, outer, args.m, args.eps)
+    barrier(world)
+    results = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            sysm.zero_x()
+            results.append(sysm.gmres(nb, outer, args.m, args.eps))
+    barrier(world)
+    dev_ms = sum(r.solve_ms for r in results) / len(results)
+    dev_ms = allmax(world, dev_ms)
+    x = sysm.get_x()
+    true_res = float(np.linalg.norm(b - Ar.matvec(x)) / nb)
+    r = results[-1]
+    hbm, peak_kind = peaks()
+    # kernel-level figures, CUDA events on the system's stream
+    pre_ms, pre_bytes = sysm.time_op(L.OP_PRECOND, 20)
+    l_ms, l_bytes = sysm.time_op(L.OP_SWEEP_L, 20)
+    u_ms, u_bytes = sysm.time_op(L.OP_SWEEP_U, 20)
+    sp_ms, sp_bytes = sysm.time_op(L.OP_SPMV, 20)
+    dot_ms, dot_bytes = sysm.time_op(L.OP_DOT, 20)
+    gbs = lambda by, ms: by / (ms * 1e-3) / 1e9
+    sysm.close()
+    e2e = None
+    if not args.no_e2e:
+        e2e_ms, rr = [], None
+        for i in range(max(1, min(args.steps, 3))):
+            xh = np.zeros(Ar.n)
+            t0 = time.perf_counter()
+            rr = SV.AbmcIluGmresm(Ar.val, Ar.cind, Ar.rptr, Lf.val, Lf.cind, Lf.rptr, Uf.val, Uf.cind, Uf.rptr, sc,
+                                  nc, 16, b, xh, nb, outer, args.m, Ar.n, args.eps, orth=orth, spmv=spmv)
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e = {"value": allmax(world, sum(e2e_ms) / len(e2e_ms)), "unit": "ms",
+               "h2d_bytes_per_step": int(rr.h2d_bytes), "d2h_bytes_per_step": int(rr.d2h_bytes),
+               "steps": len(e2e_ms), "iterations": rr.iters,
+               "note": "drop-in C ABI call senk_abmc_ilu_gmres_d with host arrays; wall clock"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        port = oracle.port()
+        threads = os.cpu_count() or 1
+        cms, cit, _ = cpu_solve(port, Ar, Lf, Uf, nc, sc, b, args.eps, args.m, threads)
+        cpu = {"value": cms, "unit": "ms", "cores": threads, "kind": "port",
+               "sample": f"one full solve of the workload ({cit} iterations), oracle C restatement of the "
+                         "reference with OpenMP"}
+    if rank != 0:
+        return
+    pre_gbs = gbs(pre_bytes, pre_ms)
+    line = {
+        "metric": METRIC, "value": dev_ms, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args.n), "N": Ar.n, "nnz": Ar.nnz, "colours": nc,
+                   "orth": args.orth, "spmv": args.spmv, "iterations": r.iters, "cycles": r.cycles,
+                   "implicit_residual": r.res, "true_residual": true_res,
+                   "l2": "inputs larger than L2 (A, L, U and the 31 basis vectors, about 0.9 GB)",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": e2e,
+        "gpu_launches": int(sum(x.launches for x in results)),
+        "roofline": {"kernel": "ILU(0) application: ABMC L and U sweeps, all colours", "bound": "hbm",
+                     "achieved": pre_gbs, "peak": hbm, "unit": "GB/s", "frac": pre_gbs / hbm,
+                     "peak_source": peak_kind, "traffic": traffic_for("ilu_apply"),
+                     "bytes_per_launch": pre_bytes, "ms_per_launch": pre_ms},
+        "kernels": {"spmv_gbs": gbs(sp_bytes, sp_ms), "spmv_ms": sp_ms,
+                    "sptrsv_l_gbs": gbs(l_bytes, l_ms), "sptrsv_u_gbs": gbs(u_bytes, u_ms),
+                    "ilu_apply_gbs": pre_gbs, "ilu_apply_ms": pre_ms, "dot_gbs": gbs(dot_bytes, dot_ms)},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+_pg = None
+
+
+def init_dist():
+    global _pg
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    rank = int(os.environ.get("RANK", 0))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        _pg = dist
+    return rank, world
+
+
+def barrier(world):
+    if world > 1 and _pg is not None:
+        _pg.barrier()
+
+
+def allmax(world, v):
+    if world > 1 and _pg is not None:
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        _pg.all_reduce(t, op=_pg.ReduceOp.MAX)
+        return float(t.item())
+    return v
+
+
+def main():
+    args = parse()
+    rank, world = init_dist()
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,254 @@
+/*
+ * senk_gpu.h — C ABI of libsenk_gpu.so, the GB300 (sm_103a) implementation of
+ * SenK's preconditioned Krylov path.
+ *
+ * Plain C types only: host or device pointers, sizes, and opaque handles. Every
+ * function returns a status code (SENK_OK == 0); senk_last_error() gives a
+ * message for the last failure on the calling thread. Each declaration names the
+ * reference interface it replaces (sapporosaburo/SenK, include/*.hpp file:line).
+ *
+ * Layout conventions are the reference's: CSR with int32 indices, sorted columns
+ * (val[nnz], cind[nnz], rptr[N+1]); split ILU factors as made by
+ * senk::matrix::Split(..., "L-DU", invDiag=true) (L strictly lower; each U row
+ * starts with the inverted diagonal); BCSR blocks column-major.
+ */
+#ifndef SENK_GPU_H
+#define SENK_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------- status codes */
+#define SENK_OK 0
+#define SENK_ERR_ARG 1
+#define SENK_ERR_CUDA 2
+#define SENK_ERR_ALLOC 3
+#define SENK_ERR_BREAKDOWN 4
+#define SENK_ERR_ZERO_PIVOT 5
+
+/* Message of the last failure on this thread ("" if none). */
+const char *senk_last_error(void);
+/* Library version (major*10000 + minor*100 + patch). */
+int senk_version(void);
+/* Number of visible CUDA devices (0 on a host without a GPU; never fails). */
+int senk_device_count(void);
+/* Make `device` current for the calling thread's later calls. */
+int senk_set_device(int device);
+
+/* ------------------------------------------------------- solver reporting */
+/* The reference reports only on stdout (include/senk_gmres.hpp:72-73,86-87;
+ * senk_bicgstab.hpp:63-66,77-78; senk_gcr.hpp:48,115). The same numbers are
+ * returned here; with opt->verbose the same lines are also printed. */
+typedef struct {
+    int iters;        /* iteration count exactly as the reference prints it */
+    int converged;    /* 1 when the stopping test was met */
+    double res;       /* relative residual as the reference prints it */
+    double solve_ms;  /* device time of the iteration, uploads excluded */
+    int breakdown;    /* 1 if a Krylov scalar was zero or not finite */
+    int cycles;       /* restart cycles (GMRES/GCR) or iterations (BiCGStab) run */
+    long long h2d_bytes; /* host -> device bytes this call copied */
+    long long d2h_bytes; /* device -> host bytes this call copied */
+    long long launches;  /* kernels launched by the solve (graph nodes x cycles) */
+} senk_result;
+
+/* Orthogonalisation of the Arnoldi step (new: the reference always uses MGS,
+ * include/senk_gmres.hpp:224-227). */
+#define SENK_ORTH_CGS2 0 /* classical Gram-Schmidt + one re-orthogonalisation */
+#define SENK_ORTH_CGS 1  /* one classical pass: one fused multi-dot + one update */
+#define SENK_ORTH_MGS 2  /* modified Gram-Schmidt, the reference's order */
+
+#define SENK_SPMV_AUTO 0
+#define SENK_SPMV_CSR 1   /* CSR, lanes per row from the mean row length */
+#define SENK_SPMV_SELL 2  /* SELL-32 built on upload */
+
+typedef struct {
+    int orth;         /* SENK_ORTH_* */
+    int spmv;         /* SENK_SPMV_* */
+    int verbose;      /* print the reference's stdout lines */
+} senk_options;
+
+/* Preconditioners and the schedules of their triangular sweeps. */
+#define SENK_PC_NONE 0
+#define SENK_PC_ILU 1       /* natural order: sweeps run level set by level set */
+#define SENK_PC_ILU_AMC 2   /* AMC order: cptr counts rows, cnum colours */
+#define SENK_PC_ILU_ABMC 3  /* ABMC order: cptr counts blocks of bsize rows */
+
+/* ======================================================= drop-in solvers ==
+ * Host arrays in, x updated in place; one call uploads, solves on the GPU and
+ * copies x back, like one call of the reference template. opt may be NULL. */
+
+/* senk::solver::Gmresm<double> (include/senk_gmres.hpp:33-37) */
+int senk_gmres_d(const double *val, const int *cind, const int *rptr,
+                 const double *b, double *x, double nrm_b,
+                 int outer, int m, int N, double epsilon,
+                 const senk_options *opt, senk_result *res);
+
+/* senk::solver::IluGmresm<T> (include/senk_gmres.hpp:197-203) */
+int senk_ilu_gmres_d(const double *val, const int *cind, const int *rptr,
+                     const double *lval, const int *lcind, const int *lrptr,
+                     const double *uval, const int *ucind, const int *urptr,
+                     const double *b, double *x, double nrm_b,
+                     int outer, int m, int N, double epsilon,
+                     const senk_options *opt, senk_result *res);
+int senk_ilu_gmres_s(const float *val, const int *cind, const int *rptr,
+                     const float *lval, const int *lcind, const int *lrptr,
+                     const float *uval, const int *ucind, const int *urptr,
+                     const float *b, float *x, float nrm_b,
+                     int outer, int m, int N, float epsilon,
+                     const senk_options *opt, senk_result *res);
+
+/* senk::solver::AmcIluGmresm<double> (include/senk_gmres.hpp:293-300) */
+int senk_amc_ilu_gmres_d(const double *val, const int *cind, const int *rptr,
+                         const double *lval, const int *lcind, const int *lrptr,
+                         const double *uval, const int *ucind, const int *urptr,
+                         const int *cptr, int cnum,
+                         const double *b, double *x, double nrm_b,
+                         int outer, int m, int N, double epsilon,
+                         const senk_options *opt, senk_result *res);
+
+/* senk::solver::AbmcIluGmresm<T> (include/senk_gmres.hpp:391-398) */
+int senk_abmc_ilu_gmres_d(const double *val, const int *cind, const int *rptr,
+                          const double *lval, const int *lcind, const int *lrptr,
+                          const double *uval, const int *ucind, const int *urptr,
+                          const int *cptr, int cnum, int bsize,
+                          const double *b, double *x, double nrm_b,
+                          int outer, int m, int N, double epsilon,
+                          const senk_options *opt, senk_result *res);
+int senk_abmc_ilu_gmres_s(const float *val, const int *cind, const int *rptr,
+                          const float *lval, const int *lcind, const int *lrptr,
+                          const float *uval, const int *ucind, const int *urptr,
+                          const int *cptr, int cnum, int bsize,
+                          const float *b, float *x, float nrm_b,
+                          int outer, int m, int N, float epsilon,
+                          const senk_options *opt, senk_result *res);
+
+/* ================================================ device-resident systems ==
+ * Upload once, solve many times (the timed path of the benchmark). */
+typedef struct senk_system senk_system;
+
+#define SENK_F64 0
+#define SENK_F32 1
+
+typedef struct {
+    int N;
+    int dtype;                 /* SENK_F64 or SENK_F32: type of every value array */
+    const void *val; const int *cind; const int *rptr;   /* A (CSR, host) */
+    int precond;               /* SENK_PC_* */
+    const void *lval; const int *lcind; const int *lrptr; /* split L (host) */
+    const void *uval; const int *ucind; const int *urptr; /* split U (host) */
+    const int *cptr; int cnum; int bsize;                 /* colour schedule */
+    int m_max;                 /* largest restart length to be used (<= 64) */
+} senk_system_desc;
+
+int senk_system_create(senk_system **out, const senk_system_desc *desc, const senk_options *opt);
+int senk_system_destroy(senk_system *sys);
+/* The CUDA stream (cudaStream_t) every operation of this system runs on. */
+void *senk_system_stream(senk_system *sys);
+/* Copy b and the initial x from host memory (x may be NULL for x0 = 0). */
+int senk_system_set_rhs(senk_system *sys, const void *b, const void *x0);
+/* Read the current x back to host memory. */
+int senk_system_get_x(senk_system *sys, void *x);
+/* x = 0 on the device (enqueued on the system's stream). */
+int senk_system_zero_x(senk_system *sys);
+/* Device pointers of b and x (type of desc->dtype), for callers that fill them. */
+void *senk_system_b(senk_system *sys);
+void *senk_system_x(senk_system *sys);
+/* Restarted GMRES(m) on the resident system (right-preconditioned when the system
+ * has a preconditioner): include/senk_gmres.hpp:33-95 / 197-270 / 293-367 /
+ * 391-465. */
+int senk_system_gmres(senk_system *sys, double nrm_b, int outer, int m, double epsilon,
+                      senk_result *res);
+
+/* Times `reps` back-to-back runs of one operation of the system's solve path on
+ * its stream with CUDA events (after one untimed run). Reports the mean time of
+ * one run and its algorithmic bytes (matrix values and indices once, each vector
+ * read or written once). */
+#define SENK_OP_SPMV 0      /* y = A x with the solve's SpMV format */
+#define SENK_OP_PRECOND 1   /* t = U^-1 L^-1 v, all colours of both sweeps */
+#define SENK_OP_SWEEP_L 2   /* the L sweep alone */
+#define SENK_OP_SWEEP_U 3   /* the U sweep alone (in place) */
+#define SENK_OP_DOT 4       /* one FP64 dot product of two vectors */
+int senk_system_time_op(senk_system *sys, int op, int reps, double *ms_per_rep, long long *bytes_per_rep);
+
+/* ================================================ device kernels (one op) ==
+ * Device pointers; stream is a cudaStream_t (NULL = legacy default stream). */
+
+/* senk::sparse::SpmvCsr<T> (include/senk_sparse.hpp:25-35): y = A x */
+int senk_dev_spmv_csr_d(const double *val, const int *cind, const int *rptr,
+                        const double *x, double *y, int N, int nnz, void *stream);
+int senk_dev_spmv_csr_s(const float *val, const int *cind, const int *rptr,
+                        const float *x, float *y, int N, int nnz, void *stream);
+/* senk::sparse::SpmvCsr<T> with diag (include/senk_sparse.hpp:47-57) */
+int senk_dev_spmv_csr_diag_d(const double *val, const int *cind, const int *rptr,
+                             const double *diag, const double *x, double *y, int N, void *stream);
+/* senk::sparse::SpmvBcsr<T,bnl,bnw> (include/senk_sparse.hpp:70-91); supported
+ * block shapes: 1x1, 2x2, 3x3, 4x4, 8x1, 4x1, 2x1 */
+int senk_dev_spmv_bcsr_d(const double *bval, const int *bcind, const int *brptr,
+                         const double *x, double *y, int N, int bnl, int bnw, void *stream);
+/* senk::sparse::SpmvSell<T> (include/senk_sparse.hpp:103-121) on the layout of
+ * senk::matrix::Csr2Sell (include/senk_matrix.hpp:90-142) */
+int senk_dev_spmv_sell_d(const double *val, const int *cind, const int *wid, int len,
+                         const double *x, double *y, int N, void *stream);
+
+/* senk::blas1::Dot / Nrm2 (include/senk_blas1.hpp:92-112); result to host */
+int senk_dev_dot_d(const double *x, const double *y, int N, double *result, void *stream);
+int senk_dev_nrm2_d(const double *x, int N, double *result, void *stream);
+/* senk::blas1::Axpy / Axpby / Axpyz / Scal / Copy (include/senk_blas1.hpp:26-83) */
+int senk_dev_axpy_d(double a, const double *x, double *y, int N, void *stream);
+int senk_dev_axpby_d(double a, const double *x, double b, double *y, int N, void *stream);
+int senk_dev_axpyz_d(double a, const double *x, const double *y, double *z, int N, void *stream);
+int senk_dev_scal_d(double a, double *x, int N, void *stream);
+int senk_dev_copy_d(const double *x, double *y, int N, void *stream);
+
+/* ILU sweep plan: the split factors re-laid out for colour-by-colour sweeps.
+ * Replaces the reference's sweeps SptrsvCsr_l/_u: sequential
+ * (include/senk_sparse.hpp:132-167, run by level sets), AMC (:180-236) and
+ * ABMC (:250-315). Factor arrays are host memory, dtype SENK_F64/SENK_F32. */
+typedef struct senk_ilu_plan senk_ilu_plan;
+int senk_ilu_plan_create(senk_ilu_plan **out, int dtype, int N,
+                         const void *lval, const int *lcind, const int *lrptr,
+                         const void *uval, const int *ucind, const int *urptr,
+                         int precond, const int *cptr, int cnum, int bsize);
+/* y = U^-1 L^-1 x (device vectors of the plan's dtype); x == y allowed. */
+int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *stream);
+/* One triangular sweep: y = L^-1 x (upper=0) or y = U^-1 x (upper=1). */
+int senk_ilu_plan_sweep(senk_ilu_plan *plan, int upper, const void *x, void *y, void *stream);
+int senk_ilu_plan_destroy(senk_ilu_plan *plan);
+
+/* ===================================================== host setup (CPU) ==
+ * The reference's setup functions, bit-exact, for callers without C++ headers.
+ * Outputs are malloc'd; release them with senk_free. */
+void senk_free(void *p);
+/* senk::matrix::Ilu0<double> (include/senk_matrix.hpp:418-448), in place */
+int senk_setup_ilu0(double *val, const int *cind, const int *rptr, int N);
+/* senk::matrix::Split<double> (include/senk_matrix.hpp:257-333) */
+int senk_setup_split(const double *val, const int *cind, const int *rptr,
+                     double **lval, int **lcind, int **lrptr,
+                     double **uval, int **ucind, int **urptr,
+                     double **diag, int N, const char *key, int invDiag);
+/* senk::graph::GetABMCPermutation (include/senk_graph.hpp:291-334) */
+int senk_setup_abmc_permutation(const int *cind, const int *rptr, int *num_color,
+                                int **size_color, int **LP, int **RP,
+                                int N, int bsize, int isSym, const char *bmethod);
+/* senk::graph::GetAMCPermutation (include/senk_graph.hpp:250-277) */
+int senk_setup_amc_permutation(const int *cind, const int *rptr, int *num_color,
+                               int **size_color, int **LP, int **RP, int N, int isSym);
+/* senk::matrix::Reordering<double>(val, cind, rptr, LP, RP, N)
+ * (include/senk_matrix.hpp:703-730), in place */
+int senk_setup_reordering(double *val, int *cind, int *rptr, const int *LP, const int *RP, int N);
+/* senk::matrix::Csr2Bcsr<double> (include/senk_matrix.hpp:144-211) */
+int senk_setup_csr2bcsr(const double *val, const int *cind, const int *rptr,
+                        double **bval, int **bcind, int **brptr, int N, int bnl, int bnw);
+/* senk::matrix::AllocBlockZero<double> (include/senk_matrix.hpp:652-666) */
+int senk_setup_alloc_block_zero(double **val, int **cind, int **rptr, int N, int bnl, int bnw);
+/* senk::matrix::Ilup<double> / AllocLevelZero<double>
+ * (include/senk_matrix.hpp:450-549 / 551-650) */
+int senk_setup_ilup(double **val, int **cind, int **rptr, int N, int p);
+int senk_setup_alloc_level_zero(double **val, int **cind, int **rptr, int N, int p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SENK_GPU_H */

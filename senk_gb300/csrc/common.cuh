@@ -1,0 +1,113 @@
+// Shared device/host helpers for the sm_103a SenK kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+namespace senkgpu {
+
+// ------------------------------------------------------------------ errors
+// Status codes returned by every extern "C" entry point (0 = success).
+enum Status : int {
+    kOk = 0,
+    kErrArg = 1,         // invalid argument (sizes, unsupported block shape, null pointer)
+    kErrCuda = 2,        // a CUDA runtime call failed
+    kErrAlloc = 3,       // device or host allocation failed
+    kErrBreakdown = 4,   // a Krylov scalar became zero/NaN (division by zero in the reference)
+    kErrZeroPivot = 5,   // ILU(0) met a zero pivot (the reference exits)
+    kErrNotConverged = 6 // iteration limit reached (informational; x is still updated)
+};
+
+void set_last_error(const std::string &msg);
+
+struct CudaError {
+    cudaError_t code;
+    const char *what;
+    const char *file;
+    int line;
+};
+
+#define SENK_CUDA(call)                                                               \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) throw ::senkgpu::CudaError{e_, #call, __FILE__, __LINE__}; \
+    } while (0)
+
+#define SENK_LAUNCH_CHECK() SENK_CUDA(cudaGetLastError())
+
+// ---------------------------------------------------------------- geometry
+constexpr int kNumSMs = 152;    // GB300: 2 dies x 76 SMs
+constexpr int kThreads = 256;   // default CTA size of the streaming kernels
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Grid size for a grid-stride streaming kernel: enough CTAs for every SM to hold
+// `per_sm` resident CTAs, but never more than the work needs.
+inline int stream_grid(long long n_items, int items_per_cta, int per_sm = 4)
+{
+    long long need = (n_items + items_per_cta - 1) / items_per_cta;
+    long long cap = (long long)kNumSMs * per_sm;
+    if (need < 1) need = 1;
+    return (int)(need < cap ? need : cap);
+}
+
+// ------------------------------------------------------------ load helpers
+// Streamed matrix data: read once per sweep, should not evict the vectors that
+// the gathers reuse from L2.
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+
+template <typename T>
+__device__ __forceinline__ T ld_keep(const T *p) { return __ldg(p); }
+
+// ------------------------------------------------------- warp reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the CTA; result valid in thread 0. `sh` holds one value per warp.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *sh)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = warp_sum(v);
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    T r = 0;
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        r = lane < nw ? sh[lane] : T(0);
+        r = warp_sum(r);
+    }
+    __syncthreads();
+    return r;
+}
+
+// "Last CTA finishes" protocol for grid-wide reductions without a second launch.
+// Every CTA writes its partials, fences, and bumps a ticket; the CTA that draws
+// the last ticket sees all partials and finalizes (then resets the ticket so the
+// same counter serves the next launch, including inside a replayed CUDA graph).
+__device__ __forceinline__ bool last_cta_arrives(unsigned int *ticket, unsigned int total)
+{
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(ticket, 1u);
+        is_last = (t == total - 1);
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        if (threadIdx.x == 0) *ticket = 0;
+    }
+    return is_last;
+}
+
+}  // namespace senkgpu

@@ -1,0 +1,221 @@
+// Host-side device objects of libsenk_gpu: buffers, the ILU sweep plan, the SpMV
+// operator and the resident system used by the Krylov engines.
+#pragma once
+
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/senk_gpu.h"
+#include "kernels.cuh"
+
+namespace senkgpu {
+
+struct ArgError : std::runtime_error {
+    explicit ArgError(const std::string &m) : std::runtime_error(m) {}
+};
+
+#define SENK_REQUIRE(cond, msg) \
+    do { if (!(cond)) throw ::senkgpu::ArgError(msg); } while (0)
+
+// Runs an entry point body, mapping exceptions to status codes + last error.
+template <typename F>
+int guarded(const char *fn, F &&body)
+{
+    try {
+        return body();
+    } catch (const CudaError &e) {
+        set_last_error(std::string(fn) + ": " + e.what + " failed: " + cudaGetErrorString(e.code) +
+                       " (" + e.file + ":" + std::to_string(e.line) + ")");
+        cudaGetLastError();  // clear a sticky-free error so the next call starts clean
+        return e.code == cudaErrorMemoryAllocation ? kErrAlloc : kErrCuda;
+    } catch (const ArgError &e) {
+        set_last_error(std::string(fn) + ": " + e.what());
+        return kErrArg;
+    } catch (const std::bad_alloc &) {
+        set_last_error(std::string(fn) + ": host allocation failed");
+        return kErrAlloc;
+    } catch (const std::exception &e) {
+        set_last_error(std::string(fn) + ": " + e.what());
+        return kErrArg;
+    }
+}
+
+// Owning device allocation.
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t count) { alloc(count); }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept
+    {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        if (count) SENK_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void upload(const T *h, size_t count, cudaStream_t s)
+    {
+        if (count) SENK_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T> &h, cudaStream_t s)
+    {
+        if (h.size() > n) alloc(h.size());
+        upload(h.data(), h.size(), s);
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// Partials + ticket for the last-CTA-finishes reductions. One per stream: the
+// reduction kernels of a stream run one after another and share it.
+struct ReduceScratch {
+    static constexpr int kMaxCols = 64;
+    static constexpr int kMaxCtas = 4 * kNumSMs;
+    DevBuf<double> part;
+    DevBuf<unsigned> ticket;
+    void ensure(cudaStream_t s)
+    {
+        if (!part.p) {
+            part.alloc((size_t)kMaxCols * kMaxCtas);
+            ticket.alloc(1);
+            SENK_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
+        }
+    }
+};
+
+// ----------------------------------------------------------------- SpMV op
+
+// A on the device. CSR always (for the residual); optionally a SELL-32 copy.
+template <typename T>
+struct SpmvOp {
+    int n = 0, nnz = 0;
+    int lanes = 8;              // lanes per row of the CSR kernel
+    DevBuf<T> val;
+    DevBuf<int> cind, rptr;
+    bool use_sell = false;
+    DevBuf<T> sval;
+    DevBuf<int> scol, soff;
+
+    void upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s);
+    // y = A x (MODE 0) or y = b - A x (MODE 1)
+    void apply(const T *x, T *y, cudaStream_t s, const int *gate) const;
+    // y = b - A x, ||y|| -> *norm_out, 1/||y|| -> *inv_out
+    void residual(const T *x, const T *b, T *y, ReduceScratch &red, double *norm_out, double *inv_out,
+                  cudaStream_t s) const;
+};
+
+// Lanes per row of the CSR kernel: the smallest power of two covering the mean
+// row length, between 2 and 32.
+int csr_lanes(long long nnz, int n);
+
+void launch_spmv_csr_d(const double *v, const int *c, const int *r, const double *x, const double *b,
+                       double *y, int n, int lanes, int mode, cudaStream_t s, const int *gate);
+void launch_spmv_csr_s(const float *v, const int *c, const int *r, const float *x, const float *b,
+                       float *y, int n, int lanes, int mode, cudaStream_t s, const int *gate);
+
+// ----------------------------------------------------------- ILU sweeps
+
+// One triangular factor in the chain-sliced layout.
+template <typename VT>
+struct SweepFactor {
+    bool upper = false;
+    bool mapped = false;           // schedule positions map to rows through rowmap
+    int bs = 1;                    // rows per chain
+    DevBuf<VT> val;
+    DevBuf<int> col;
+    DevBuf<VT> dinv;               // U: inverted diagonal per schedule position
+    DevBuf<int> rowmap;
+    DevBuf<SliceDesc> slices;
+    std::vector<int> group_slices; // slice range of each group, in processing order
+    long long elems = 0;           // padded slots
+    long long nnz = 0;             // stored off-diagonal entries (+N for U's diagonal)
+};
+
+// A split ILU factorisation with its sweep schedule.
+template <typename VT>
+struct IluPlan {
+    int n = 0;
+    int precond = SENK_PC_NONE;
+    SweepFactor<VT> L, U;
+
+    void build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
+               const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s);
+    template <typename XT>
+    void sweep(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate) const;
+    template <typename XT>
+    void apply(const XT *x, XT *y, cudaStream_t s, const int *gate) const
+    {
+        sweep(L, x, y, s, gate);
+        sweep(U, (const XT *)y, y, s, gate);
+    }
+    // Algorithmic bytes of one application (values + indices once, x read once,
+    // y written once per sweep and re-read by the U sweep), for roofline figures.
+    long long apply_bytes() const;
+};
+
+// --------------------------------------------------------- Krylov system
+
+template <typename T>
+struct System {
+    int n = 0;
+    cudaStream_t stream = nullptr;
+    senk_options opt{};
+    SpmvOp<T> A;
+    std::unique_ptr<IluPlan<T>> pc;
+    DevBuf<T> b, x, t;
+    // GMRES workspace
+    int m_alloc = 0;
+    DevBuf<T> V;
+    DevBuf<double> H, cs, sn, e, y, coef;
+    DevBuf<KrylovState> st;
+    ReduceScratch red;
+    KrylovState *st_host = nullptr;  // pinned mirror
+    // captured restart cycle
+    cudaGraphExec_t cycle = nullptr;
+    int cycle_m = -1, cycle_orth = -1;
+    long long cycle_nodes = 0;       // kernel nodes of the captured cycle
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    System() = default;
+    System(const System &) = delete;
+    ~System();
+    void create(const senk_system_desc &d, const senk_options *o);
+    void ensure_gmres(int m);
+    void enqueue_gmres_cycle(int m);
+    int gmres(double nrm_b, int outer, int m, double eps, senk_result *res);
+    void time_op(int op, int reps, double *ms, long long *bytes);
+    long long h2d_bytes = 0;         // bytes uploaded by create()
+};
+
+}  // namespace senkgpu
+
+// The opaque handles of the C ABI.
+struct senk_system {
+    int dtype = SENK_F64;
+    std::unique_ptr<senkgpu::System<double>> d;
+    std::unique_ptr<senkgpu::System<float>> f;
+};
+
+struct senk_ilu_plan {
+    int dtype = SENK_F64;
+    std::unique_ptr<senkgpu::IluPlan<double>> d;
+    std::unique_ptr<senkgpu::IluPlan<float>> f;
+};

@@ -1,0 +1,502 @@
+// Krylov engines on a device-resident system. One restart cycle of GMRES(m) is
+// captured once as a CUDA graph; every inner-iteration kernel is gated by the
+// device `done` flag so the iteration count is exact without a host round trip
+// per iteration. The host synchronises once per cycle.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+#include "device.hpp"
+
+namespace senkgpu {
+
+namespace {
+
+constexpr int kRedCtas = 2 * kNumSMs;  // CTAs of the multi-dot / update kernels
+
+template <typename T, int OP>
+void ew(const T *x, T *y, T *z, long long n, T a, T b, const double *a_dev, double a_mul, cudaStream_t s,
+        const int *gate)
+{
+    k_elementwise<T, OP><<<stream_grid(n, kThreads, 8), kThreads, 0, s>>>(a, a_dev, a_mul, b, x, y, z, n, gate);
+}
+
+}  // namespace
+
+template <typename T>
+System<T>::~System()
+{
+    if (cycle) cudaGraphExecDestroy(cycle);
+    if (st_host) cudaFreeHost(st_host);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+template <typename T>
+void System<T>::create(const senk_system_desc &d, const senk_options *o)
+{
+    SENK_REQUIRE(d.N > 0, "N must be positive");
+    n = d.N;
+    if (o) opt = *o;
+    SENK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    SENK_CUDA(cudaEventCreate(&ev0));
+    SENK_CUDA(cudaEventCreate(&ev1));
+    SENK_CUDA(cudaMallocHost((void **)&st_host, sizeof(KrylovState)));
+    A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream);
+    if (d.precond != SENK_PC_NONE) {
+        pc = std::make_unique<IluPlan<T>>();
+        pc->build(n, (const T *)d.lval, d.lcind, d.lrptr, (const T *)d.uval, d.ucind, d.urptr, d.precond, d.cptr,
+                  d.cnum, d.bsize, stream);
+    }
+    b.alloc(n);
+    x.alloc(n);
+    t.alloc(n);
+    SENK_CUDA(cudaMemsetAsync(b.p, 0, b.bytes(), stream));
+    SENK_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), stream));
+    st.alloc(1);
+    red.ensure(stream);
+    if (d.m_max > 0) ensure_gmres(d.m_max);
+    SENK_CUDA(cudaStreamSynchronize(stream));
+    h2d_bytes = (long long)(A.val.bytes() + A.cind.bytes() + A.rptr.bytes() + A.sval.bytes() + A.scol.bytes() +
+                            A.soff.bytes());
+    if (pc) {
+        for (const SweepFactor<T> *F : {&pc->L, &pc->U})
+            h2d_bytes += (long long)(F->val.bytes() + F->col.bytes() + F->dinv.bytes() + F->rowmap.bytes() +
+                                     F->slices.bytes());
+    }
+}
+
+template <typename T>
+void System<T>::ensure_gmres(int m)
+{
+    SENK_REQUIRE(m >= 1 && m <= 63, "restart length m must be in [1, 63]");
+    if (m <= m_alloc) return;
+    V.alloc((size_t)(m + 1) * n);
+    H.alloc((size_t)(m + 1) * m);
+    cs.alloc(m);
+    sn.alloc(m);
+    e.alloc(m + 1);
+    y.alloc(m);
+    coef.alloc(64);
+    m_alloc = m;
+    if (cycle) {
+        cudaGraphExecDestroy(cycle);
+        cycle = nullptr;
+        cycle_m = -1;
+    }
+}
+
+// Arnoldi step j: w = V_{j+1} against V_0..V_j, H column j, Givens, test.
+template <typename T>
+static void enqueue_orth(System<T> &S, int j, int m, int orth, const int *gate)
+{
+    const long long ld = S.n;
+    T *w = S.V.p + (long long)(j + 1) * ld;
+    double *hcol = S.H.p + (long long)j * (m + 1);
+    GmresEpi g{S.H.p, S.cs.p, S.sn.p, S.e.p, j, m};
+    GmresEpi none{};
+    const int nv = j + 1;
+    const dim3 gdot(kRedCtas, (nv + 7) / 8);
+    cudaStream_t s = S.stream;
+    if (orth == SENK_ORTH_MGS) {
+        for (int k = 0; k <= j; k++) {
+            const T *vk = S.V.p + (long long)k * ld;
+            k_multidot<T, false><<<dim3(kRedCtas, 1), kThreads, 0, s>>>(vk, ld, 1, w, ld, S.red.part.p,
+                                                                         S.red.ticket.p, S.coef.p, hcol + k, gate);
+            if (k == j)
+                k_update<T, kEpiGmres><<<kRedCtas, kThreads, 0, s>>>(vk, ld, 1, S.coef.p, w, ld, S.red.part.p,
+                                                                     S.red.ticket.p, nullptr, S.st.p, g, gate);
+            else
+                k_update<T, kEpiNone><<<kRedCtas, kThreads, 0, s>>>(vk, ld, 1, S.coef.p, w, ld, S.red.part.p,
+                                                                    S.red.ticket.p, nullptr, S.st.p, none, gate);
+        }
+        return;
+    }
+    k_multidot<T, false><<<gdot, kThreads, 0, s>>>(S.V.p, ld, nv, w, ld, S.red.part.p, S.red.ticket.p, S.coef.p,
+                                                   hcol, gate);
+    if (orth == SENK_ORTH_CGS) {
+        k_update<T, kEpiGmres><<<kRedCtas, kThreads, 0, s>>>(S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
+                                                             S.red.ticket.p, nullptr, S.st.p, g, gate);
+        return;
+    }
+    // CGS2: second pass corrects the coefficients (H += correction).
+    k_update<T, kEpiNone><<<kRedCtas, kThreads, 0, s>>>(S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
+                                                        S.red.ticket.p, nullptr, S.st.p, none, gate);
+    k_multidot<T, true><<<gdot, kThreads, 0, s>>>(S.V.p, ld, nv, w, ld, S.red.part.p, S.red.ticket.p, S.coef.p,
+                                                  hcol, gate);
+    k_update<T, kEpiGmres><<<kRedCtas, kThreads, 0, s>>>(S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
+                                                         S.red.ticket.p, nullptr, S.st.p, g, gate);
+}
+
+// One restart cycle (include/senk_gmres.hpp:214-257, and :47-84 without a
+// preconditioner), every kernel on S.stream.
+template <typename T>
+void System<T>::enqueue_gmres_cycle(int m)
+{
+    const int *gate = &st.p->done;
+    const long long ld = n;
+    // r0 = b - A x, e0 = ||r0||, V0 = r0 / e0
+    A.residual(x.p, b.p, V.p, red, e.p, &st.p->scale, stream);
+    ew<T, 3>(nullptr, V.p, nullptr, n, T(0), T(0), &st.p->scale, 1.0, stream, nullptr);
+    for (int j = 0; j < m; j++) {
+        T *vj = V.p + (long long)j * ld;
+        T *w = V.p + (long long)(j + 1) * ld;
+        if (pc) {
+            pc->apply(vj, t.p, stream, gate);
+            A.apply(t.p, w, stream, gate);
+        } else {
+            A.apply(vj, w, stream, gate);
+        }
+        enqueue_orth(*this, j, m, opt.orth, gate);
+        ew<T, 3>(nullptr, w, nullptr, n, T(0), T(0), &st.p->scale, 1.0, stream, gate);
+    }
+    k_gmres_trsv<<<1, 32, 0, stream>>>(st.p, H.p, e.p, y.p, m);
+    const int grid = stream_grid(n, kThreads, 8);
+    if (pc) {
+        k_gmres_combine<T, true><<<grid, kThreads, 0, stream>>>(V.p, ld, y.p, st.p, x.p, n, m);
+        pc->apply(V.p, t.p, stream, nullptr);
+        ew<T, 0>(t.p, x.p, nullptr, n, T(1), T(0), nullptr, 1.0, stream, nullptr);
+    } else {
+        k_gmres_combine<T, false><<<grid, kThreads, 0, stream>>>(V.p, ld, y.p, st.p, x.p, n, m);
+    }
+    SENK_LAUNCH_CHECK();
+}
+
+template <typename T>
+int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *res)
+{
+    SENK_REQUIRE(outer >= 0, "outer must be non-negative");
+    ensure_gmres(m);
+    const int orth = opt.orth;
+    SENK_REQUIRE(orth == SENK_ORTH_CGS2 || orth == SENK_ORTH_CGS || orth == SENK_ORTH_MGS, "unknown orthogonalisation");
+    if (!cycle || cycle_m != m || cycle_orth != orth) {
+        if (cycle) cudaGraphExecDestroy(cycle);
+        cycle = nullptr;
+        cudaGraph_t g;
+        SENK_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue_gmres_cycle(m);
+        } catch (...) {
+            cudaStreamEndCapture(stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        SENK_CUDA(cudaStreamEndCapture(stream, &g));
+        size_t nodes = 0;
+        SENK_CUDA(cudaGraphGetNodes(g, nullptr, &nodes));
+        cycle_nodes = (long long)nodes;
+        cudaError_t ie = cudaGraphInstantiate(&cycle, g, 0);
+        cudaGraphDestroy(g);
+        SENK_CUDA(ie);
+        cycle_m = m;
+        cycle_orth = orth;
+    }
+    KrylovState init{};
+    init.nrm_b = nrm_b;
+    init.eps = eps;
+    *st_host = init;
+    SENK_CUDA(cudaMemcpyAsync(st.p, st_host, sizeof(KrylovState), cudaMemcpyHostToDevice, stream));
+    SENK_CUDA(cudaEventRecord(ev0, stream));
+    int cycles = 0, iters = outer * m, conv = 0;
+    double resid = -1;
+    for (int i = 0; i < outer; i++) {
+        SENK_CUDA(cudaGraphLaunch(cycle, stream));
+        SENK_CUDA(cudaMemcpyAsync(st_host, st.p, sizeof(KrylovState), cudaMemcpyDeviceToHost, stream));
+        SENK_CUDA(cudaStreamSynchronize(stream));
+        cycles++;
+        if (st_host->done) {
+            conv = 1;
+            iters = i * m + st_host->jconv;
+            resid = st_host->res;
+            break;
+        }
+    }
+    SENK_CUDA(cudaEventRecord(ev1, stream));
+    SENK_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0;
+    SENK_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    if (opt.verbose) {
+        if (conv) {
+            printf("I iter %d\n", iters);
+            printf("# res %e\n", resid);
+        } else {
+            printf("# iter %d\n", outer * m);
+            printf("# res : Check by using senk::test\n");
+        }
+        fflush(stdout);
+    }
+    if (res) {
+        res->iters = iters;
+        res->converged = conv;
+        res->res = resid;
+        res->solve_ms = ms;
+        res->breakdown = st_host->breakdown;
+        res->cycles = cycles;
+        res->launches = cycle_nodes * cycles;
+    }
+    return kOk;
+}
+
+template <typename T>
+void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
+{
+    ensure_gmres(std::max(m_alloc, 1));
+    T *v0 = V.p, *v1 = V.p + n;
+    const long long vb = sizeof(T);
+    long long bytes = 0;
+    auto run = [&]() {
+        switch (op) {
+        case SENK_OP_SPMV: A.apply(v0, v1, stream, nullptr); break;
+        case SENK_OP_PRECOND: SENK_REQUIRE(pc, "system has no preconditioner"); pc->apply(v0, t.p, stream, nullptr); break;
+        case SENK_OP_SWEEP_L: SENK_REQUIRE(pc, "system has no preconditioner"); pc->sweep(pc->L, v0, t.p, stream, nullptr); break;
+        case SENK_OP_SWEEP_U: SENK_REQUIRE(pc, "system has no preconditioner"); pc->sweep(pc->U, (const T *)t.p, t.p, stream, nullptr); break;
+        case SENK_OP_DOT:
+            k_multidot<T, false><<<dim3(kRedCtas, 1), kThreads, 0, stream>>>(v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
+            break;
+        default: throw ArgError("unknown op");
+        }
+    };
+    switch (op) {
+    case SENK_OP_SPMV: bytes = (long long)A.nnz * (vb + 4) + 4LL * (n + 1) + 2LL * n * vb; break;
+    case SENK_OP_PRECOND: bytes = pc->apply_bytes(); break;
+    case SENK_OP_SWEEP_L: bytes = pc->L.nnz * (vb + 4) + 2LL * n * vb; break;
+    case SENK_OP_SWEEP_U: bytes = (pc->U.nnz - n) * (vb + 4) + 3LL * n * vb; break;
+    case SENK_OP_DOT: bytes = 2LL * n * vb; break;
+    }
+    // deterministic finite inputs
+    ew<T, 4>(x.p, v0, nullptr, n, T(0), T(0), nullptr, 1.0, stream, nullptr);
+    SENK_CUDA(cudaMemsetAsync(v1, 0, vb * n, stream));
+    run();
+    SENK_CUDA(cudaEventRecord(ev0, stream));
+    for (int i = 0; i < reps; i++) run();
+    SENK_CUDA(cudaEventRecord(ev1, stream));
+    SENK_CUDA(cudaEventSynchronize(ev1));
+    SENK_LAUNCH_CHECK();
+    float ms = 0;
+    SENK_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    *ms_out = ms / reps;
+    *bytes_out = bytes;
+}
+
+template struct System<double>;
+template struct System<float>;
+
+namespace {
+
+template <typename T>
+int dropin_gmres(const char *fn, const T *val, const int *cind, const int *rptr, const T *lval, const int *lcind,
+                 const int *lrptr, const T *uval, const int *ucind, const int *urptr, int precond, const int *cptr,
+                 int cnum, int bsize, const T *b, T *x, double nrm_b, int outer, int m, int N, double eps,
+                 const senk_options *opt, senk_result *res)
+{
+    return guarded(fn, [&] {
+        SENK_REQUIRE(val && cind && rptr && b && x, "null argument");
+        senk_system_desc d{};
+        d.N = N;
+        d.dtype = sizeof(T) == 8 ? SENK_F64 : SENK_F32;
+        d.val = val;
+        d.cind = cind;
+        d.rptr = rptr;
+        d.precond = precond;
+        d.lval = lval; d.lcind = lcind; d.lrptr = lrptr;
+        d.uval = uval; d.ucind = ucind; d.urptr = urptr;
+        d.cptr = cptr; d.cnum = cnum; d.bsize = bsize;
+        d.m_max = m;
+        senk_options o{};
+        if (opt) o = *opt;
+        System<T> S;
+        S.create(d, &o);
+        S.b.upload(b, N, S.stream);
+        S.x.upload(x, N, S.stream);
+        senk_result r{};
+        S.gmres(nrm_b, outer, m, eps, &r);
+        SENK_CUDA(cudaMemcpyAsync(x, S.x.p, sizeof(T) * N, cudaMemcpyDeviceToHost, S.stream));
+        SENK_CUDA(cudaStreamSynchronize(S.stream));
+        r.h2d_bytes = S.h2d_bytes + 2LL * sizeof(T) * N;
+        r.d2h_bytes = (long long)sizeof(T) * N;
+        if (res) *res = r;
+        return r.breakdown ? (int)kErrBreakdown : (int)kOk;
+    });
+}
+
+}  // namespace
+
+}  // namespace senkgpu
+
+using namespace senkgpu;
+
+extern "C" {
+
+int senk_system_create(senk_system **out, const senk_system_desc *desc, const senk_options *opt)
+{
+    return guarded("senk_system_create", [&] {
+        SENK_REQUIRE(out && desc, "null argument");
+        auto h = std::make_unique<senk_system>();
+        h->dtype = desc->dtype;
+        if (desc->dtype == SENK_F64) {
+            h->d = std::make_unique<System<double>>();
+            h->d->create(*desc, opt);
+        } else if (desc->dtype == SENK_F32) {
+            h->f = std::make_unique<System<float>>();
+            h->f->create(*desc, opt);
+        } else {
+            throw ArgError("dtype must be SENK_F64 or SENK_F32");
+        }
+        *out = h.release();
+        return (int)kOk;
+    });
+}
+
+int senk_system_destroy(senk_system *sys)
+{
+    return guarded("senk_system_destroy", [&] {
+        delete sys;
+        return (int)kOk;
+    });
+}
+
+void *senk_system_stream(senk_system *sys)
+{
+    if (!sys) return nullptr;
+    return sys->d ? (void *)sys->d->stream : (void *)sys->f->stream;
+}
+
+void *senk_system_b(senk_system *sys)
+{
+    if (!sys) return nullptr;
+    return sys->d ? (void *)sys->d->b.p : (void *)sys->f->b.p;
+}
+
+void *senk_system_x(senk_system *sys)
+{
+    if (!sys) return nullptr;
+    return sys->d ? (void *)sys->d->x.p : (void *)sys->f->x.p;
+}
+
+int senk_system_set_rhs(senk_system *sys, const void *b, const void *x0)
+{
+    return guarded("senk_system_set_rhs", [&] {
+        SENK_REQUIRE(sys && b, "null argument");
+        if (sys->d) {
+            auto &S = *sys->d;
+            S.b.upload((const double *)b, S.n, S.stream);
+            if (x0) S.x.upload((const double *)x0, S.n, S.stream);
+            else SENK_CUDA(cudaMemsetAsync(S.x.p, 0, S.x.bytes(), S.stream));
+            SENK_CUDA(cudaStreamSynchronize(S.stream));
+        } else {
+            auto &S = *sys->f;
+            S.b.upload((const float *)b, S.n, S.stream);
+            if (x0) S.x.upload((const float *)x0, S.n, S.stream);
+            else SENK_CUDA(cudaMemsetAsync(S.x.p, 0, S.x.bytes(), S.stream));
+            SENK_CUDA(cudaStreamSynchronize(S.stream));
+        }
+        return (int)kOk;
+    });
+}
+
+int senk_system_zero_x(senk_system *sys)
+{
+    return guarded("senk_system_zero_x", [&] {
+        SENK_REQUIRE(sys, "null system");
+        if (sys->d) SENK_CUDA(cudaMemsetAsync(sys->d->x.p, 0, sys->d->x.bytes(), sys->d->stream));
+        else SENK_CUDA(cudaMemsetAsync(sys->f->x.p, 0, sys->f->x.bytes(), sys->f->stream));
+        return (int)kOk;
+    });
+}
+
+int senk_system_get_x(senk_system *sys, void *x)
+{
+    return guarded("senk_system_get_x", [&] {
+        SENK_REQUIRE(sys && x, "null argument");
+        if (sys->d) {
+            SENK_CUDA(cudaMemcpyAsync(x, sys->d->x.p, sys->d->x.bytes(), cudaMemcpyDeviceToHost, sys->d->stream));
+            SENK_CUDA(cudaStreamSynchronize(sys->d->stream));
+        } else {
+            SENK_CUDA(cudaMemcpyAsync(x, sys->f->x.p, sys->f->x.bytes(), cudaMemcpyDeviceToHost, sys->f->stream));
+            SENK_CUDA(cudaStreamSynchronize(sys->f->stream));
+        }
+        return (int)kOk;
+    });
+}
+
+int senk_system_time_op(senk_system *sys, int op, int reps, double *ms_per_rep, long long *bytes_per_rep)
+{
+    return guarded("senk_system_time_op", [&] {
+        SENK_REQUIRE(sys && reps > 0, "bad argument");
+        double ms = 0;
+        long long bytes = 0;
+        if (sys->d) sys->d->time_op(op, reps, &ms, &bytes);
+        else sys->f->time_op(op, reps, &ms, &bytes);
+        if (ms_per_rep) *ms_per_rep = ms;
+        if (bytes_per_rep) *bytes_per_rep = bytes;
+        return (int)kOk;
+    });
+}
+
+int senk_system_gmres(senk_system *sys, double nrm_b, int outer, int m, double epsilon, senk_result *res)
+{
+    return guarded("senk_system_gmres", [&] {
+        SENK_REQUIRE(sys, "null system");
+        senk_result r{};
+        if (sys->d) sys->d->gmres(nrm_b, outer, m, epsilon, &r);
+        else sys->f->gmres(nrm_b, outer, m, epsilon, &r);
+        if (res) *res = r;
+        return r.breakdown ? (int)kErrBreakdown : (int)kOk;
+    });
+}
+
+int senk_gmres_d(const double *val, const int *cind, const int *rptr, const double *b, double *x, double nrm_b,
+                 int outer, int m, int N, double epsilon, const senk_options *opt, senk_result *res)
+{
+    return dropin_gmres<double>("senk_gmres_d", val, cind, rptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                nullptr, SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+int senk_ilu_gmres_d(const double *val, const int *cind, const int *rptr, const double *lval, const int *lcind,
+                     const int *lrptr, const double *uval, const int *ucind, const int *urptr, const double *b,
+                     double *x, double nrm_b, int outer, int m, int N, double epsilon, const senk_options *opt,
+                     senk_result *res)
+{
+    return dropin_gmres<double>("senk_ilu_gmres_d", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                                SENK_PC_ILU, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+int senk_ilu_gmres_s(const float *val, const int *cind, const int *rptr, const float *lval, const int *lcind,
+                     const int *lrptr, const float *uval, const int *ucind, const int *urptr, const float *b,
+                     float *x, float nrm_b, int outer, int m, int N, float epsilon, const senk_options *opt,
+                     senk_result *res)
+{
+    return dropin_gmres<float>("senk_ilu_gmres_s", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                               SENK_PC_ILU, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+int senk_amc_ilu_gmres_d(const double *val, const int *cind, const int *rptr, const double *lval, const int *lcind,
+                         const int *lrptr, const double *uval, const int *ucind, const int *urptr, const int *cptr,
+                         int cnum, const double *b, double *x, double nrm_b, int outer, int m, int N,
+                         double epsilon, const senk_options *opt, senk_result *res)
+{
+    return dropin_gmres<double>("senk_amc_ilu_gmres_d", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                                SENK_PC_ILU_AMC, cptr, cnum, 1, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+int senk_abmc_ilu_gmres_d(const double *val, const int *cind, const int *rptr, const double *lval,
+                          const int *lcind, const int *lrptr, const double *uval, const int *ucind,
+                          const int *urptr, const int *cptr, int cnum, int bsize, const double *b, double *x,
+                          double nrm_b, int outer, int m, int N, double epsilon, const senk_options *opt,
+                          senk_result *res)
+{
+    return dropin_gmres<double>("senk_abmc_ilu_gmres_d", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                                SENK_PC_ILU_ABMC, cptr, cnum, bsize, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+int senk_abmc_ilu_gmres_s(const float *val, const int *cind, const int *rptr, const float *lval, const int *lcind,
+                          const int *lrptr, const float *uval, const int *ucind, const int *urptr, const int *cptr,
+                          int cnum, int bsize, const float *b, float *x, float nrm_b, int outer, int m, int N,
+                          float epsilon, const senk_options *opt, senk_result *res)
+{
+    return dropin_gmres<float>("senk_abmc_ilu_gmres_s", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                               SENK_PC_ILU_ABMC, cptr, cnum, bsize, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+}  // extern "C"

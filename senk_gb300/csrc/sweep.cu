@@ -1,0 +1,337 @@
+// ILU sweep plans: the split factors re-laid out for colour-by-colour triangular
+// sweeps on the GPU (replaces include/senk_sparse.hpp:132-315, SptrsvCsr_l/_u in
+// their sequential, AMC and ABMC forms).
+//
+// Layout ("chain-sliced"): the schedule is a list of groups (colours, or level
+// sets for the natural order) in processing order; the positions of a group are
+// cut into slices of 32, each solved by one warp. A chain is `bs` consecutive
+// positions (one ABMC block) solved in order; bs divides 32, so slices hold
+// whole chains. Per row, entries referencing other chains come first (they are
+// final before the group starts) and entries inside the chain follow, as
+// chain-local column numbers; within each part the order is the reference's
+// subtraction order (ascending columns for L, descending for U). Slot k of a
+// slice is a 32-wide column, so loads of one slot across the warp coalesce.
+#include <algorithm>
+#include <climits>
+
+#include "device.hpp"
+
+namespace senkgpu {
+
+namespace {
+
+struct Group {
+    int p0, p1;  // schedule positions [p0, p1)
+};
+
+template <typename VT>
+void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
+                  const std::vector<Group> &groups, const std::vector<int> *rowmap, int bs,
+                  const std::vector<int> *group_of_row, cudaStream_t s)
+{
+    F.upper = upper;
+    F.mapped = rowmap != nullptr;
+    F.bs = bs;
+    const bool chains = !F.mapped && bs > 1;
+    std::vector<int> next(N), nint(N);
+    int bad = -1;
+#pragma omp parallel for schedule(static)
+    for (int p = 0; p < N; p++) {
+        const int row = rowmap ? (*rowmap)[p] : p;
+        int b = rptr[row], e = rptr[row + 1];
+        bool ok = true;
+        if (upper) {
+            ok = e > b && cind[b] == row;  // U row must start with its diagonal
+            b++;
+        }
+        const int cs = row - row % bs, ce = cs + bs;
+        int ni = 0;
+        for (int j = b; j < e && ok; j++) {
+            const int c = cind[j];
+            if (c < 0 || c >= N || (upper ? c <= row : c >= row)) { ok = false; break; }
+            if (chains && c >= cs && c < ce) ni++;
+            else if (group_of_row && (*group_of_row)[c] >= (*group_of_row)[row])
+                ok = false;  // a column outside the chain must belong to a group solved earlier
+        }
+        if (!ok) {
+#pragma omp atomic write
+            bad = row;
+        }
+        next[p] = (e - b) - ni;
+        nint[p] = ni;
+    }
+    SENK_REQUIRE(bad < 0, std::string(upper ? "U" : "L") + " factor row " + std::to_string(bad) +
+                              " does not fit the schedule (diagonal first in U, strictly triangular, "
+                              "columns of other chains in earlier colours)");
+    std::vector<SliceDesc> sl;
+    F.group_slices.assign(1, 0);
+    for (const Group &g : groups) {
+        for (int p = g.p0; p < g.p1; p += 32) {
+            SliceDesc d{};
+            d.pos0 = p;
+            d.nrows = (short)std::min(32, g.p1 - p);
+            sl.push_back(d);
+        }
+        F.group_slices.push_back((int)sl.size());
+    }
+    const int ns = (int)sl.size();
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < ns; i++) {
+        int we = 0, wi = 0;
+        for (int l = 0; l < sl[i].nrows; l++) {
+            we = std::max(we, next[sl[i].pos0 + l]);
+            wi = std::max(wi, nint[sl[i].pos0 + l]);
+        }
+        sl[i].we = (short)we;
+        sl[i].wi = (short)wi;
+    }
+    long long off = 0;
+    for (int i = 0; i < ns; i++) {
+        sl[i].off = (int)off;
+        off += (long long)(sl[i].we + sl[i].wi) * 32;
+        SENK_REQUIRE(off < INT_MAX, "factor too large for 32-bit slot offsets");
+    }
+    F.elems = off;
+    std::vector<VT> hv((size_t)std::max<long long>(off, 1), VT(0));
+    std::vector<int> hc((size_t)std::max<long long>(off, 1), -1);
+    std::vector<VT> hd(upper ? N : 0);
+    long long stored = 0;
+#pragma omp parallel for schedule(static) reduction(+ : stored)
+    for (int i = 0; i < ns; i++) {
+        const SliceDesc d = sl[i];
+        for (int l = 0; l < d.nrows; l++) {
+            const int p = d.pos0 + l;
+            const int row = rowmap ? (*rowmap)[p] : p;
+            const int cs = row - row % bs, ce = cs + bs;
+            int ke = 0, ki = 0;
+            auto put = [&](int j) {
+                const int c = cind[j];
+                if (chains && c >= cs && c < ce) {
+                    const long long at = d.off + (long long)(d.we + ki) * 32 + l;
+                    hv[at] = val[j];
+                    hc[at] = c - cs;
+                    ki++;
+                } else {
+                    const long long at = d.off + (long long)ke * 32 + l;
+                    hv[at] = val[j];
+                    hc[at] = c;
+                    ke++;
+                }
+                stored++;
+            };
+            if (upper) {
+                hd[p] = val[rptr[row]];
+                for (int j = rptr[row + 1] - 1; j >= rptr[row] + 1; j--) put(j);
+            } else {
+                for (int j = rptr[row]; j < rptr[row + 1]; j++) put(j);
+            }
+        }
+    }
+    F.nnz = stored + (upper ? N : 0);
+    F.val.alloc(hv.size());
+    F.val.upload(hv.data(), hv.size(), s);
+    F.col.alloc(hc.size());
+    F.col.upload(hc.data(), hc.size(), s);
+    if (upper) {
+        F.dinv.alloc(N);
+        F.dinv.upload(hd.data(), N, s);
+    }
+    if (rowmap) {
+        F.rowmap.alloc(N);
+        F.rowmap.upload(rowmap->data(), N, s);
+    }
+    F.slices.alloc(std::max(ns, 1));
+    F.slices.upload(sl.data(), ns, s);
+    // Host vectors are released on return: finish the copies first.
+    SENK_CUDA(cudaStreamSynchronize(s));
+}
+
+// Level sets of a triangular factor for the natural order: level(i) = 1 + max
+// level of the rows it reads. Rows of one level are independent, and each row's
+// arithmetic is the sequential sweep's, so the result equals the sequential one.
+void level_schedule(int N, const int *cind, const int *rptr, bool upper, std::vector<int> &rowmap,
+                    std::vector<Group> &groups)
+{
+    std::vector<int> lev(N, 0);
+    int maxlev = 0;
+    if (!upper) {
+        for (int i = 0; i < N; i++) {
+            int l = 0;
+            for (int j = rptr[i]; j < rptr[i + 1]; j++) l = std::max(l, lev[cind[j]] + 1);
+            lev[i] = l;
+            maxlev = std::max(maxlev, l);
+        }
+    } else {
+        for (int i = N - 1; i >= 0; i--) {
+            int l = 0;
+            for (int j = rptr[i] + 1; j < rptr[i + 1]; j++) l = std::max(l, lev[cind[j]] + 1);
+            lev[i] = l;
+            maxlev = std::max(maxlev, l);
+        }
+    }
+    std::vector<int> cnt(maxlev + 2, 0);
+    for (int i = 0; i < N; i++) cnt[lev[i] + 1]++;
+    for (int l = 0; l <= maxlev; l++) cnt[l + 1] += cnt[l];
+    rowmap.assign(N, 0);
+    std::vector<int> at(cnt.begin(), cnt.end() - 1);
+    for (int i = 0; i < N; i++) rowmap[at[lev[i]]++] = i;
+    groups.clear();
+    for (int l = 0; l <= maxlev; l++) groups.push_back({cnt[l], cnt[l + 1]});
+}
+
+template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
+void launch_group(const SweepFactor<VT> &F, int sb, int se, const XT *x, XT *y, cudaStream_t s, const int *gate)
+{
+    const int warps_per_cta = kThreads / 32;
+    const int grid = ceil_div(se - sb, warps_per_cta);
+    k_sweep<VT, XT, BS, UPPER, MAPPED><<<grid, kThreads, 0, s>>>(F.slices.p, sb, se, F.val.p, F.col.p, F.dinv.p,
+                                                                  F.rowmap.p, x, y, gate);
+}
+
+template <typename VT, typename XT, bool UPPER>
+void sweep_groups(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate)
+{
+    const int ng = (int)F.group_slices.size() - 1;
+    for (int g = 0; g < ng; g++) {
+        const int sb = F.group_slices[g], se = F.group_slices[g + 1];
+        if (se == sb) continue;
+        if (F.mapped) {
+            launch_group<VT, XT, 1, UPPER, true>(F, sb, se, x, y, s, gate);
+            continue;
+        }
+        switch (F.bs) {
+        case 1: launch_group<VT, XT, 1, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        case 2: launch_group<VT, XT, 2, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        case 4: launch_group<VT, XT, 4, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        case 8: launch_group<VT, XT, 8, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        case 16: launch_group<VT, XT, 16, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        case 32: launch_group<VT, XT, 32, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        default: throw ArgError("unsupported chain length");
+        }
+    }
+    SENK_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+template <typename VT>
+void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval,
+                        const int *ucind, const int *urptr, int pckind, const int *cptr, int cnum, int bsize,
+                        cudaStream_t s)
+{
+    SENK_REQUIRE(N > 0, "N must be positive");
+    SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
+    n = N;
+    precond = pckind;
+    if (pckind == SENK_PC_ILU) {
+        std::vector<int> rm;
+        std::vector<Group> gr;
+        level_schedule(N, lcind, lrptr, false, rm, gr);
+        build_factor(L, false, N, lval, lcind, lrptr, gr, &rm, 1, nullptr, s);
+        level_schedule(N, ucind, urptr, true, rm, gr);
+        build_factor(U, true, N, uval, ucind, urptr, gr, &rm, 1, nullptr, s);
+        return;
+    }
+    SENK_REQUIRE(pckind == SENK_PC_ILU_AMC || pckind == SENK_PC_ILU_ABMC, "unknown preconditioner kind");
+    const int bs = pckind == SENK_PC_ILU_AMC ? 1 : bsize;
+    SENK_REQUIRE(bs == 1 || bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32,
+                 "ABMC block size must be 1, 2, 4, 8, 16 or 32 on the GPU path (got " + std::to_string(bs) + ")");
+    SENK_REQUIRE(cptr && cnum > 0, "colour pointer missing");
+    SENK_REQUIRE(cptr[0] == 0 && (long long)cptr[cnum] * bs == N, "colour pointer does not cover N rows");
+    std::vector<Group> fwd, bwd;
+    std::vector<int> colour_of(N);
+    for (int k = 0; k < cnum; k++) {
+        SENK_REQUIRE(cptr[k + 1] >= cptr[k], "colour pointer not monotone");
+        fwd.push_back({cptr[k] * bs, cptr[k + 1] * bs});
+        for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
+    }
+    for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
+    build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
+    // For U, "earlier" means a later colour: flip the colour numbers.
+    for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
+    build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
+}
+
+template <typename VT>
+template <typename XT>
+void IluPlan<VT>::sweep(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate) const
+{
+    if (F.upper) sweep_groups<VT, XT, true>(F, x, y, s, gate);
+    else sweep_groups<VT, XT, false>(F, x, y, s, gate);
+}
+
+template <typename VT>
+long long IluPlan<VT>::apply_bytes() const
+{
+    const long long vb = sizeof(VT);
+    // stored entries: value + column; U diagonal: value only; x read, t written,
+    // t read and written again by the in-place U sweep.
+    return (L.nnz + (U.nnz - n)) * (vb + 4) + (long long)n * vb + 4LL * n * vb;
+}
+
+template struct IluPlan<double>;
+template struct IluPlan<float>;
+template void IluPlan<double>::sweep<double>(const SweepFactor<double> &, const double *, double *, cudaStream_t, const int *) const;
+template void IluPlan<float>::sweep<float>(const SweepFactor<float> &, const float *, float *, cudaStream_t, const int *) const;
+
+}  // namespace senkgpu
+
+using namespace senkgpu;
+
+extern "C" {
+
+int senk_ilu_plan_create(senk_ilu_plan **out, int dtype, int N, const void *lval, const int *lcind,
+                         const int *lrptr, const void *uval, const int *ucind, const int *urptr, int precond,
+                         const int *cptr, int cnum, int bsize)
+{
+    return guarded("senk_ilu_plan_create", [&] {
+        SENK_REQUIRE(out != nullptr, "out is null");
+        auto h = std::make_unique<senk_ilu_plan>();
+        h->dtype = dtype;
+        if (dtype == SENK_F64) {
+            h->d = std::make_unique<IluPlan<double>>();
+            h->d->build(N, (const double *)lval, lcind, lrptr, (const double *)uval, ucind, urptr, precond, cptr,
+                        cnum, bsize, nullptr);
+        } else if (dtype == SENK_F32) {
+            h->f = std::make_unique<IluPlan<float>>();
+            h->f->build(N, (const float *)lval, lcind, lrptr, (const float *)uval, ucind, urptr, precond, cptr,
+                        cnum, bsize, nullptr);
+        } else {
+            throw ArgError("dtype must be SENK_F64 or SENK_F32");
+        }
+        *out = h.release();
+        return (int)kOk;
+    });
+}
+
+int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *stream)
+{
+    return guarded("senk_ilu_plan_apply", [&] {
+        SENK_REQUIRE(plan && x && y, "null argument");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (plan->d) plan->d->apply((const double *)x, (double *)y, s, nullptr);
+        else plan->f->apply((const float *)x, (float *)y, s, nullptr);
+        return (int)kOk;
+    });
+}
+
+int senk_ilu_plan_sweep(senk_ilu_plan *plan, int upper, const void *x, void *y, void *stream)
+{
+    return guarded("senk_ilu_plan_sweep", [&] {
+        SENK_REQUIRE(plan && x && y, "null argument");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (plan->d) plan->d->sweep(upper ? plan->d->U : plan->d->L, (const double *)x, (double *)y, s, nullptr);
+        else plan->f->sweep(upper ? plan->f->U : plan->f->L, (const float *)x, (float *)y, s, nullptr);
+        return (int)kOk;
+    });
+}
+
+int senk_ilu_plan_destroy(senk_ilu_plan *plan)
+{
+    return guarded("senk_ilu_plan_destroy", [&] {
+        delete plan;
+        return (int)kOk;
+    });
+}
+
+}  // extern "C"

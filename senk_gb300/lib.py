@@ -1,0 +1,142 @@
+"""ctypes binding of libsenk_gpu.so (the C ABI declared in include/senk_gpu.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback for
+any operation of the solver path.  Build it with ``python -m senk_gb300.build``
+(or ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_BREAKDOWN, ERR_ZERO_PIVOT = range(6)
+ORTH_CGS2, ORTH_CGS, ORTH_MGS = 0, 1, 2
+SPMV_AUTO, SPMV_CSR, SPMV_SELL = 0, 1, 2
+PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC = 0, 1, 2, 3
+OP_SPMV, OP_PRECOND, OP_SWEEP_L, OP_SWEEP_U, OP_DOT = 0, 1, 2, 3, 4
+F64, F32 = 0, 1
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_Fl = C.c_float
+
+
+class SenkError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+class Result(C.Structure):
+    _fields_ = [("iters", _I), ("converged", _I), ("res", _D), ("solve_ms", _D), ("breakdown", _I),
+                ("cycles", _I), ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong),
+                ("launches", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Options(C.Structure):
+    _fields_ = [("orth", _I), ("spmv", _I), ("verbose", _I)]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("N", _I), ("dtype", _I), ("val", _P), ("cind", _P), ("rptr", _P), ("precond", _I),
+                ("lval", _P), ("lcind", _P), ("lrptr", _P), ("uval", _P), ("ucind", _P), ("urptr", _P),
+                ("cptr", _P), ("cnum", _I), ("bsize", _I), ("m_max", _I)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: build it with `python -m senk_gb300.build`; "
+                          "the solver path has no CPU fallback")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    def d(name, args, res=_I):
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+
+    d("senk_last_error", [], C.c_char_p)
+    d("senk_version", [])
+    d("senk_device_count", [])
+    d("senk_set_device", [_I])
+    d("senk_free", [_P], None)
+    Rp, Op = C.POINTER(Result), C.POINTER(Options)
+    d("senk_gmres_d", [_P, _P, _P, _P, _P, _D, _I, _I, _I, _D, Op, Rp])
+    d("senk_ilu_gmres_d", [_P] * 11 + [_D, _I, _I, _I, _D, Op, Rp])
+    d("senk_ilu_gmres_s", [_P] * 11 + [_Fl, _I, _I, _I, _Fl, Op, Rp])
+    d("senk_amc_ilu_gmres_d", [_P] * 10 + [_I, _P, _P, _D, _I, _I, _I, _D, Op, Rp])
+    d("senk_abmc_ilu_gmres_d", [_P] * 10 + [_I, _I, _P, _P, _D, _I, _I, _I, _D, Op, Rp])
+    d("senk_abmc_ilu_gmres_s", [_P] * 10 + [_I, _I, _P, _P, _Fl, _I, _I, _I, _Fl, Op, Rp])
+    d("senk_system_create", [C.POINTER(_P), C.POINTER(SystemDesc), Op])
+    d("senk_system_destroy", [_P])
+    d("senk_system_stream", [_P], _P)
+    d("senk_system_b", [_P], _P)
+    d("senk_system_x", [_P], _P)
+    d("senk_system_set_rhs", [_P, _P, _P])
+    d("senk_system_get_x", [_P, _P])
+    d("senk_system_zero_x", [_P])
+    d("senk_system_gmres", [_P, _D, _I, _I, _D, Rp])
+    d("senk_system_time_op", [_P, _I, _I, C.POINTER(_D), C.POINTER(C.c_longlong)])
+    d("senk_dev_spmv_csr_d", [_P, _P, _P, _P, _P, _I, _I, _P])
+    d("senk_dev_spmv_csr_s", [_P, _P, _P, _P, _P, _I, _I, _P])
+    d("senk_dev_spmv_csr_diag_d", [_P, _P, _P, _P, _P, _P, _I, _P])
+    d("senk_dev_spmv_bcsr_d", [_P, _P, _P, _P, _P, _I, _I, _I, _P])
+    d("senk_dev_spmv_sell_d", [_P, _P, _P, _I, _P, _P, _I, _P])
+    d("senk_dev_dot_d", [_P, _P, _I, C.POINTER(_D), _P])
+    d("senk_dev_nrm2_d", [_P, _I, C.POINTER(_D), _P])
+    d("senk_dev_axpy_d", [_D, _P, _P, _I, _P])
+    d("senk_dev_axpby_d", [_D, _P, _D, _P, _I, _P])
+    d("senk_dev_axpyz_d", [_D, _P, _P, _P, _I, _P])
+    d("senk_dev_scal_d", [_D, _P, _I, _P])
+    d("senk_dev_copy_d", [_P, _P, _I, _P])
+    d("senk_ilu_plan_create", [C.POINTER(_P), _I, _I, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I])
+    d("senk_ilu_plan_apply", [_P, _P, _P, _P])
+    d("senk_ilu_plan_sweep", [_P, _I, _P, _P, _P])
+    d("senk_ilu_plan_destroy", [_P])
+    PP = C.POINTER(_P)
+    d("senk_setup_ilu0", [_P, _P, _P, _I])
+    d("senk_setup_split", [_P, _P, _P, PP, PP, PP, PP, PP, PP, PP, _I, C.c_char_p, _I])
+    d("senk_setup_abmc_permutation", [_P, _P, C.POINTER(_I), PP, PP, PP, _I, _I, _I, C.c_char_p])
+    d("senk_setup_amc_permutation", [_P, _P, C.POINTER(_I), PP, PP, PP, _I, _I])
+    d("senk_setup_reordering", [_P, _P, _P, _P, _P, _I])
+    d("senk_setup_csr2bcsr", [_P, _P, _P, PP, PP, PP, _I, _I, _I])
+    d("senk_setup_alloc_block_zero", [PP, PP, PP, _I, _I, _I])
+    d("senk_setup_ilup", [PP, PP, PP, _I, _I])
+    d("senk_setup_alloc_level_zero", [PP, PP, PP, _I, _I])
+
+
+def check(fn: str, code: int) -> int:
+    """Raise SenkError for a non-zero status (breakdown is reported, not raised)."""
+    if code not in (OK, ERR_BREAKDOWN):
+        raise SenkError(fn, code, lib().senk_last_error().decode())
+    return code
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def exported_symbols(header: str) -> list:
+    """Names of the functions declared in a C header of include/ (for tests)."""
+    import re
+    text = open(header).read()
+    return sorted(set(re.findall(r"\b(senk_[a-z0-9_]+)\s*\(", text)))

@@ -1,0 +1,157 @@
+"""Solvers through the C ABI, mirroring senk::solver (include/senk_gmres.hpp,
+include/senk_gcr.hpp, include/senk_bicgstab.hpp).
+
+The drop-in functions take the reference's arguments in the reference's order
+(host numpy arrays; ``x`` is updated in place) and return the ``Result`` that the
+reference only prints.  ``System`` is the device-resident form used for repeated
+solves (upload once, solve many times).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .lib import (F32, F64, PC_ILU, PC_ILU_ABMC, PC_ILU_AMC, PC_NONE, Options, Result, SystemDesc, check, lib,
+                  ptr)
+from .problems import Csr
+
+
+def _opts(orth=0, spmv=0, verbose=False):
+    return Options(orth, spmv, int(verbose))
+
+
+def _T(x):
+    return np.float32 if x.dtype == np.float32 else np.float64
+
+
+def _arr(a, dtype):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a
+
+
+def Gmresm(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, **opt) -> Result:
+    """senk::solver::Gmresm<double> (include/senk_gmres.hpp:33-95)."""
+    r = Result()
+    check("senk_gmres_d", lib().senk_gmres_d(ptr(_arr(val, np.float64)), ptr(_arr(cind, np.int32)),
+                                             ptr(_arr(rptr, np.int32)), ptr(_arr(b, np.float64)), ptr(x),
+                                             nrm_b, outer, m, N, epsilon, C.byref(_opts(**opt)), C.byref(r)))
+    return r
+
+
+def IluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, outer, m, N, epsilon,
+              **opt) -> Result:
+    """senk::solver::IluGmresm<T> (include/senk_gmres.hpp:197-270); T from x."""
+    T = _T(x)
+    fn = "senk_ilu_gmres_s" if T == np.float32 else "senk_ilu_gmres_d"
+    r = Result()
+    keep = [_arr(val, T), _arr(cind, np.int32), _arr(rptr, np.int32), _arr(lval, T), _arr(lcind, np.int32),
+            _arr(lrptr, np.int32), _arr(uval, T), _arr(ucind, np.int32), _arr(urptr, np.int32), _arr(b, T)]
+    check(fn, getattr(lib(), fn)(*[ptr(a) for a in keep], ptr(x), nrm_b, outer, m, N, epsilon,
+                                 C.byref(_opts(**opt)), C.byref(r)))
+    return r
+
+
+def AmcIluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, b, x, nrm_b, outer, m, N,
+                 epsilon, **opt) -> Result:
+    """senk::solver::AmcIluGmresm<double> (include/senk_gmres.hpp:293-367)."""
+    r = Result()
+    keep = [_arr(val, np.float64), _arr(cind, np.int32), _arr(rptr, np.int32), _arr(lval, np.float64),
+            _arr(lcind, np.int32), _arr(lrptr, np.int32), _arr(uval, np.float64), _arr(ucind, np.int32),
+            _arr(urptr, np.int32), _arr(cptr, np.int32)]
+    check("senk_amc_ilu_gmres_d",
+          lib().senk_amc_ilu_gmres_d(*[ptr(a) for a in keep], cnum, ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer,
+                                     m, N, epsilon, C.byref(_opts(**opt)), C.byref(r)))
+    return r
+
+
+def AbmcIluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, bsize, b, x, nrm_b, outer,
+                  m, N, epsilon, **opt) -> Result:
+    """senk::solver::AbmcIluGmresm<T> (include/senk_gmres.hpp:391-465); T from x."""
+    T = _T(x)
+    fn = "senk_abmc_ilu_gmres_s" if T == np.float32 else "senk_abmc_ilu_gmres_d"
+    r = Result()
+    keep = [_arr(val, T), _arr(cind, np.int32), _arr(rptr, np.int32), _arr(lval, T), _arr(lcind, np.int32),
+            _arr(lrptr, np.int32), _arr(uval, T), _arr(ucind, np.int32), _arr(urptr, np.int32),
+            _arr(cptr, np.int32)]
+    check(fn, getattr(lib(), fn)(*[ptr(a) for a in keep], cnum, bsize, ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N,
+                                 epsilon, C.byref(_opts(**opt)), C.byref(r)))
+    return r
+
+
+class System:
+    """A device-resident system: A (+ split ILU factors and their schedule) uploaded
+    once; b and x live on the device between solves."""
+
+    def __init__(self, A: Csr, L: Csr = None, U: Csr = None, precond: int = PC_NONE, cptr=None, cnum: int = 0,
+                 bsize: int = 1, dtype=np.float64, m_max: int = 30, **opt):
+        self.dtype = np.dtype(dtype)
+        T = self.dtype
+        self.n = A.n
+        self._keep = [_arr(A.val, T), _arr(A.cind, np.int32), _arr(A.rptr, np.int32)]
+        d = SystemDesc()
+        d.N, d.dtype = A.n, (F32 if T == np.float32 else F64)
+        d.val, d.cind, d.rptr = [ptr(a) for a in self._keep]
+        d.precond = precond
+        if precond != PC_NONE:
+            fac = [_arr(L.val, T), _arr(L.cind, np.int32), _arr(L.rptr, np.int32), _arr(U.val, T),
+                   _arr(U.cind, np.int32), _arr(U.rptr, np.int32)]
+            self._keep += fac
+            d.lval, d.lcind, d.lrptr, d.uval, d.ucind, d.urptr = [ptr(a) for a in fac]
+            if cptr is not None:
+                cp = _arr(cptr, np.int32)
+                self._keep.append(cp)
+                d.cptr = ptr(cp)
+            d.cnum, d.bsize = cnum, bsize
+        d.m_max = m_max
+        self._h = C.c_void_p()
+        check("senk_system_create", lib().senk_system_create(C.byref(self._h), C.byref(d), C.byref(_opts(**opt))))
+        self._keep = None
+
+    @property
+    def stream(self) -> int:
+        return lib().senk_system_stream(self._h)
+
+    @property
+    def b_ptr(self) -> int:
+        return lib().senk_system_b(self._h)
+
+    @property
+    def x_ptr(self) -> int:
+        return lib().senk_system_x(self._h)
+
+    def set_rhs(self, b, x0=None):
+        b = _arr(b, self.dtype)
+        x0 = None if x0 is None else _arr(x0, self.dtype)
+        check("senk_system_set_rhs", lib().senk_system_set_rhs(self._h, ptr(b), ptr(x0)))
+
+    def zero_x(self):
+        check("senk_system_zero_x", lib().senk_system_zero_x(self._h))
+
+    def get_x(self):
+        x = np.empty(self.n, self.dtype)
+        check("senk_system_get_x", lib().senk_system_get_x(self._h, ptr(x)))
+        return x
+
+    def time_op(self, op: int, reps: int):
+        """(ms per run, algorithmic bytes per run) of one op of the solve path,
+        timed with CUDA events on the system's stream."""
+        ms, by = C.c_double(0), C.c_longlong(0)
+        check("senk_system_time_op", lib().senk_system_time_op(self._h, op, reps, C.byref(ms), C.byref(by)))
+        return ms.value, by.value
+
+    def gmres(self, nrm_b, outer, m, epsilon) -> Result:
+        r = Result()
+        check("senk_system_gmres", lib().senk_system_gmres(self._h, nrm_b, outer, m, epsilon, C.byref(r)))
+        return r
+
+    def close(self):
+        if self._h:
+            lib().senk_system_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
