@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-kernels", action="store_true", help="skip the per-kernel timings (profiling runs)")
     return ap.parse_args()
 
 
@@ -226,11 +227,13 @@ def run_gpu(args, rank, world):
     r = results[-1]
     hbm, peak_kind = peaks()
     # kernel-level figures, CUDA events on the system's stream
-    pre_ms, pre_bytes = sysm.time_op(L.OP_PRECOND, 20)
-    l_ms, l_bytes = sysm.time_op(L.OP_SWEEP_L, 20)
-    u_ms, u_bytes = sysm.time_op(L.OP_SWEEP_U, 20)
-    sp_ms, sp_bytes = sysm.time_op(L.OP_SPMV, 20)
-    dot_ms, dot_bytes = sysm.time_op(L.OP_DOT, 20)
+    reps = 0 if args.no_kernels else 20
+    timed = lambda op: sysm.time_op(op, reps) if reps else (float("nan"), 0)
+    pre_ms, pre_bytes = timed(L.OP_PRECOND)
+    l_ms, l_bytes = timed(L.OP_SWEEP_L)
+    u_ms, u_bytes = timed(L.OP_SWEEP_U)
+    sp_ms, sp_bytes = timed(L.OP_SPMV)
+    dot_ms, dot_bytes = timed(L.OP_DOT)
     gbs = lambda by, ms: by / (ms * 1e-3) / 1e9
     sysm.close()
     e2e = None
