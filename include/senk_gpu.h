@@ -194,6 +194,21 @@ int senk_dev_spmv_sell_d(const double *val, const int *cind, const int *wid, int
 /* senk::blas1::Dot / Nrm2 (include/senk_blas1.hpp:92-112); result to host */
 int senk_dev_dot_d(const double *x, const double *y, int N, double *result, void *stream);
 int senk_dev_nrm2_d(const double *x, int N, double *result, void *stream);
+/* Column dot products out[k] = V_k . w for k < nv (V_k = V + k*ldv; all device
+ * pointers, out holds nv doubles), computed without allocating device memory.
+ * No counterpart in the reference. It is for callers that cannot allocate at the
+ * point of the call: applications that hand all GPU memory to their own pool at
+ * start-up and forbid later cudaMalloc, and latency-critical loops where
+ * cudaMalloc/cudaFree could synchronise the device. Same kernel and results as
+ * senk_dev_dot_d per column, but its reduction scratch is a fixed 39,168-byte
+ * array inside the library's device image, held by every GPU that loads the
+ * library until the process exits. Limits: 1 <= nv <= 16 (other values return
+ * SENK_ERR_ARG). The first call on each device looks up that array's device
+ * address; make it before any stream capture. All calls share the one array
+ * (each call clears what must start at zero), so calls that overlap on the GPU,
+ * e.g. on two streams at once, race and give wrong results. */
+int senk_dev_multidot_d_noalloc(const double *V, long long ldv, int nv, const double *w, int N,
+                                double *out, void *stream);
 /* senk::blas1::Axpy / Axpby / Axpyz / Scal / Copy (include/senk_blas1.hpp:26-83) */
 int senk_dev_axpy_d(double a, const double *x, double *y, int N, void *stream);
 int senk_dev_axpby_d(double a, const double *x, double b, double *y, int N, void *stream);
