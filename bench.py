@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=128, help="grid points per dimension")
     ap.add_argument("--m", type=int, default=30)
     ap.add_argument("--eps", type=float, default=1e-8)
-    ap.add_argument("--orth", default="cgs2", choices=["cgs2", "cgs", "mgs"])
+    ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2", "mgs"])
     ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -54,11 +54,11 @@ typedef struct {
 
 /* Orthogonalisation of the Arnoldi step (new: the reference always uses MGS,
  * include/senk_gmres.hpp:224-227). */
-#define SENK_ORTH_CGS2 0 /* classical Gram-Schmidt + one re-orthogonalisation */
-#define SENK_ORTH_CGS 1  /* one classical pass: one fused multi-dot + one update */
+#define SENK_ORTH_CGS 0  /* one classical pass: one fused multi-dot + one update (default) */
+#define SENK_ORTH_CGS2 1 /* classical Gram-Schmidt + one re-orthogonalisation */
 #define SENK_ORTH_MGS 2  /* modified Gram-Schmidt, the reference's order */
 
-#define SENK_SPMV_AUTO 0
+#define SENK_SPMV_AUTO 0  /* SELL-32 for the solver's inner SpMV */
 #define SENK_SPMV_CSR 1   /* CSR, lanes per row from the mean row length */
 #define SENK_SPMV_SELL 2  /* SELL-32 built on upload */
 

@@ -143,8 +143,10 @@ struct SweepFactor {
     DevBuf<int> col;
     DevBuf<VT> dinv;               // U: inverted diagonal per schedule position
     DevBuf<int> rowmap;
-    DevBuf<SliceDesc> slices;
-    std::vector<int> group_slices; // slice range of each group, in processing order
+    DevBuf<GroupDesc> groups;
+    DevBuf<unsigned char> widths;  // per group: we[bs], wi[bs]
+    std::vector<int> colour_groups; // group range of each colour, in processing order
+    std::vector<size_t> colour_smem; // bytes to stage the largest group of each colour
     long long elems = 0;           // padded slots
     long long nnz = 0;             // stored off-diagonal entries (+N for U's diagonal)
 };
@@ -155,6 +157,7 @@ struct IluPlan {
     int n = 0;
     int precond = SENK_PC_NONE;
     SweepFactor<VT> L, U;
+    DevBuf<int> status;  // set to 1 by a sweep whose TMA wait ran out
 
     void build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
                const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s);
@@ -169,6 +172,8 @@ struct IluPlan {
     // Algorithmic bytes of one application (values + indices once, x read once,
     // y written once per sweep and re-read by the U sweep), for roofline figures.
     long long apply_bytes() const;
+    // Throws if a sweep reported a failed wait (synchronises the stream).
+    void check_status(cudaStream_t s) const;
 };
 
 // --------------------------------------------------------- Krylov system

@@ -378,88 +378,146 @@ k_gmres_combine(XT *__restrict__ V, long long ldv, const double *__restrict__ y,
 
 // --------------------------------------------------------------- ILU sweep
 
-// One slice of the chain-sliced factor layout: up to 32 consecutive schedule
-// positions of one colour (whole chains of bsize rows). Entries of slot k of the
-// slice's row `lane` sit at off + k*32 + lane; slots [0, we) hold entries whose
-// column lies outside the row's chain, slots [we, we+wi) hold in-chain entries
-// as chain-local column indices. Unused slots have column -1.
-struct SliceDesc {
-    int pos0;       // first schedule position
-    int off;        // element offset of slot 0 (multiple of 32)
-    short nrows;    // rows in this slice (<= 32)
-    short we;       // external slots
-    short wi;       // in-chain slots
-    short pad;
+// One group of the chain-major factor layout: up to 32 chains of one colour (a
+// chain = bsize consecutive schedule positions solved in order, one ABMC block),
+// one chain per lane. Row l of a group has we[l] external slots followed, after
+// all rows' external slots, by wi[l] in-chain slots; slot k of row l of the
+// chain in `lane` sits at off + (slot_index)*32 + lane, so a warp's loads of one
+// slot coalesce. In-chain slots hold chain-local row numbers; unused slots hold
+// column -1. The widths (uint8 we[BS], wi[BS]) are at widths + widx.
+struct GroupDesc {
+    int pos0;       // schedule position of chain 0, row 0
+    int off;        // element offset of the group's first slot
+    int nchains;    // chains in this group (<= 32)
+    int widx;       // byte offset of this group's widths
 };
-static_assert(sizeof(SliceDesc) == 16, "SliceDesc is one 16-byte load");
+static_assert(sizeof(GroupDesc) == 16, "GroupDesc is one 16-byte load");
+
+constexpr unsigned kWaitLimit = 1u << 24;  // polls of a TMA wait before it is declared failed
 
 // Sweep of one colour: L (forward, unit diagonal) or U (backward, inverted
-// diagonal in dinv). Each warp solves one slice; the rows of a chain are
-// finished in order by broadcasting each finished value to the chain's lanes.
-// Per row the subtraction order is the reference's: external entries (columns
-// of other, already solved colours) first, then in-chain entries, each in the
-// reference's column order (ascending for L, descending for U).
-template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
-__global__ void __launch_bounds__(kThreads)
-k_sweep(const SliceDesc *__restrict__ slices, int s_begin, int s_end,
+// diagonal in dinv). One CTA of BS warps solves one group of up to 32 chains:
+//  * phase 1 (all warps): warp l takes row l of every chain (lane = chain) and
+//    subtracts that row's external entries (columns of other colours, already
+//    final); the warp reads slot k of row l as one 32-wide row of the staged
+//    block, so shared-memory reads are conflict-free and every lane of an FP64
+//    instruction is useful;
+//  * phase 2 (warp 0, one lane per chain): the chain's rows in solve order with
+//    their in-chain entries, all operands on chip;
+//  * all warps store the finished rows.
+// Per row the subtraction order is the reference's: external entries, then
+// in-chain ones, each in the reference's column order.
+//
+// STAGED: the group's factor block (values and columns, contiguous in the
+// layout) is copied to shared memory by two TMA bulk copies issued before the
+// kernel waits for the previous colour (programmatic dependent launch), so the
+// loads of colour k+1 overlap the tail of colour k. A TMA wait that does not end
+// within kWaitLimit polls sets *status; the CTA then waits once more (bounded)
+// for its copies and leaves.
+template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED, bool STAGED>
+__global__ void __launch_bounds__(BS * 32)
+k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *__restrict__ widths,
         const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
-        const int *__restrict__ rowmap, const XT *x, XT *y, const int *gate)
+        const int *__restrict__ rowmap, const XT *x, XT *y, const int *gate, int *status)
 {
-    if (gated(gate)) return;
-    const int s = s_begin + (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (s >= s_end) return;  // warp-uniform
-    const int lane = threadIdx.x & 31;
-    const SliceDesc d = slices[s];
-    const int pos = d.pos0 + lane;
-    const bool live = lane < d.nrows;
-    const int row = live ? (MAPPED ? __ldg(rowmap + pos) : pos) : 0;
-    XT t = live ? x[row] : XT(0);
-    // Phase 1: entries outside the chain (other colours, already final).
-    const int *cb = col + d.off + lane;
-    const VT *vb = val + d.off + lane;
-    int k = 0;
-    for (; k + 2 <= d.we; k += 2) {
-        const int c0 = ld_stream(cb + k * 32), c1 = ld_stream(cb + (k + 1) * 32);
-        const VT v0 = ld_stream(vb + k * 32), v1 = ld_stream(vb + (k + 1) * 32);
-        const XT y0 = c0 >= 0 ? y[c0] : XT(0);
-        const XT y1 = c1 >= 0 ? y[c1] : XT(0);
-        if (c0 >= 0) t -= (XT)v0 * y0;
-        if (c1 >= 0) t -= (XT)v1 * y1;
-    }
-    if (k < d.we) {
-        const int c0 = ld_stream(cb + k * 32);
-        const VT v0 = ld_stream(vb + k * 32);
-        if (c0 >= 0) t -= (XT)v0 * y[c0];
-    }
-    if (BS > 1) {
-        // Phase 2: in-chain entries, column by column in solve order.
-        const int r = lane % BS, base = lane - r;
-        const int kend = d.we + d.wi;
-        int kk = d.we;
-        int ic0 = -1, ic1 = -1, ic2 = -1, ic3 = -1;
-        VT iv0 = 0, iv1 = 0, iv2 = 0, iv3 = 0;
-        if (kk < kend) { ic0 = ld_stream(cb + kk * 32); iv0 = ld_stream(vb + kk * 32); }
-        if (kk + 1 < kend) { ic1 = ld_stream(cb + (kk + 1) * 32); iv1 = ld_stream(vb + (kk + 1) * 32); }
-        if (kk + 2 < kend) { ic2 = ld_stream(cb + (kk + 2) * 32); iv2 = ld_stream(vb + (kk + 2) * 32); }
-        if (kk + 3 < kend) { ic3 = ld_stream(cb + (kk + 3) * 32); iv3 = ld_stream(vb + (kk + 3) * 32); }
-        kk += 4;
+    extern __shared__ __align__(128) unsigned char dsm[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ XT tsh[BS][32];    // row l of chain q
+    __shared__ XT dsh[UPPER ? BS : 1][32];
+    __shared__ int wsh[2 * BS];   // we[BS], wi[BS]
+    const int g = g_begin + blockIdx.x;
+    const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
+    const GroupDesc d = groups[g];
+    if (threadIdx.x < 2 * BS) wsh[threadIdx.x] = widths[d.widx + threadIdx.x];
+    __syncthreads();
+    int eo = 0, etot = 0;
 #pragma unroll
-        for (int step = 0; step < BS; step++) {
-            const int sc = UPPER ? BS - 1 - step : step;
-            if (UPPER && r == sc && live) t *= (XT)__ldg(dinv + pos);
-            const XT yv = __shfl_sync(0xffffffffu, t, base + sc);
-            if (ic0 == sc) {
-                t -= (XT)iv0 * yv;
-                ic0 = ic1; iv0 = iv1; ic1 = ic2; iv1 = iv2; ic2 = ic3; iv2 = iv3;
-                if (kk < kend) { ic3 = ld_stream(cb + kk * 32); iv3 = ld_stream(vb + kk * 32); }
-                else ic3 = -1;
-                kk++;
+    for (int r = 0; r < BS; r++) {
+        if (r < l) eo += wsh[r];
+        etot += wsh[r];
+    }
+    int itot = 0;
+#pragma unroll
+    for (int r = 0; r < BS; r++) itot += wsh[BS + r];
+    const int slots = etot + itot;
+    const unsigned vbytes = (unsigned)slots * 32u * sizeof(VT), cbytes = (unsigned)slots * 32u * 4u;
+    const VT *vb;
+    const int *cb;
+    if (STAGED) {
+        VT *sv = reinterpret_cast<VT *>(dsm);
+        int *sc = reinterpret_cast<int *>(dsm + vbytes);
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            if (slots > 0) {
+                mbar_expect_tx(&bar, vbytes + cbytes);
+                bulk_g2s(sv, val + d.off, vbytes, &bar);
+                bulk_g2s(sc, col + d.off, cbytes, &bar);
             }
         }
-    } else if (UPPER) {
-        if (live) t *= (XT)__ldg(dinv + pos);
+        __syncthreads();
+        vb = sv;
+        cb = sc;
+    } else {
+        vb = val + d.off;
+        cb = col + d.off;
     }
-    if (live) y[row] = t;
+    pdl_launch_dependents();
+    pdl_wait();  // the previous colour (or the producer of x) has finished
+    const bool skip = gated(gate);
+    bool ok = true;
+    if (STAGED && slots > 0) ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (__syncthreads_or(!ok)) {  // leave together: no thread may wait at a later barrier alone
+        if (threadIdx.x == 0) atomicExch(status, 1);
+        if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
+        return;
+    }
+    if (skip) return;
+    const bool live = q < d.nchains;
+    const int pos = d.pos0 + q * BS + l;
+    const int row = live ? (MAPPED ? __ldg(rowmap + pos) : pos) : 0;
+    XT t = live ? x[row] : XT(0);
+    // Phase 1: row l's external entries.
+    const int we = wsh[l];
+    for (int k = 0; k < we; k++) {
+        const int at = (eo + k) * 32 + q;
+        const int c = STAGED ? cb[at] : ld_stream(cb + at);
+        const VT v = STAGED ? vb[at] : ld_stream(vb + at);
+        if (c >= 0) t -= (XT)v * y[c];
+    }
+    if (BS == 1) {
+        if (UPPER && live) t *= (XT)__ldg(dinv + pos);
+        if (live) y[row] = t;
+        return;
+    }
+    tsh[l][q] = t;
+    if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
+    __syncthreads();
+    // Phase 2: one lane per chain, rows in solve order.
+    if (l == 0) {
+        int io = etot;
+        int ioff[BS];
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+            ioff[r] = io;
+            io += wsh[BS + r];
+        }
+#pragma unroll
+        for (int s = 0; s < BS; s++) {
+            const int r = UPPER ? BS - 1 - s : s;
+            XT tt = tsh[r][q];
+            const int wi = wsh[BS + r];
+            for (int k = 0; k < wi; k++) {
+                const int at = (ioff[r] + k) * 32 + q;
+                const int c = cb[at];
+                const VT v = vb[at];
+                if (c >= 0) tt -= (XT)v * tsh[c][q];
+            }
+            if (UPPER) tt *= dsh[r][q];
+            tsh[r][q] = tt;
+        }
+    }
+    __syncthreads();
+    if (live) y[row] = tsh[l][q];
 }
 
 }  // namespace senkgpu

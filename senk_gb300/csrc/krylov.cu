@@ -63,7 +63,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o)
     if (pc) {
         for (const SweepFactor<T> *F : {&pc->L, &pc->U})
             h2d_bytes += (long long)(F->val.bytes() + F->col.bytes() + F->dinv.bytes() + F->rowmap.bytes() +
-                                     F->slices.bytes());
+                                     F->groups.bytes() + F->widths.bytes());
     }
 }
 
@@ -216,6 +216,7 @@ int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *re
     SENK_CUDA(cudaEventSynchronize(ev1));
     float ms = 0;
     SENK_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    if (pc) pc->check_status(stream);
     if (opt.verbose) {
         if (conv) {
             printf("I iter %d\n", iters);

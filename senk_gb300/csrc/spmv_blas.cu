@@ -64,7 +64,10 @@ void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format
     val.upload(v, nnz, s);
     cind.upload(c, nnz, s);
     rptr.upload(r, N + 1, s);
-    use_sell = format == SENK_SPMV_SELL;
+    // The inner SpMV defaults to SELL-32: one thread per row keeps every lane of
+    // every FP64 instruction useful (GB300's FP64 pipe, not HBM, limits the
+    // CSR-vector kernel).
+    use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_AUTO;
     if (use_sell) {
         // SELL-32 (no row sorting): slice i = rows [32i, 32i+32), width = longest row.
         const int ns = (N + 31) / 32;

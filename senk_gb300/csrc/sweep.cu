@@ -2,15 +2,15 @@
 // sweeps on the GPU (replaces include/senk_sparse.hpp:132-315, SptrsvCsr_l/_u in
 // their sequential, AMC and ABMC forms).
 //
-// Layout ("chain-sliced"): the schedule is a list of groups (colours, or level
-// sets for the natural order) in processing order; the positions of a group are
-// cut into slices of 32, each solved by one warp. A chain is `bs` consecutive
-// positions (one ABMC block) solved in order; bs divides 32, so slices hold
-// whole chains. Per row, entries referencing other chains come first (they are
-// final before the group starts) and entries inside the chain follow, as
-// chain-local column numbers; within each part the order is the reference's
-// subtraction order (ascending columns for L, descending for U). Slot k of a
-// slice is a 32-wide column, so loads of one slot across the warp coalesce.
+// Layout ("chain-major"): the schedule is a list of colours (or level sets for
+// the natural order) in processing order. A chain is `bs` consecutive schedule
+// positions (one ABMC block) solved in order; 32 chains of a colour form a
+// group, solved by one CTA of bs warps. Per row, entries referencing other
+// chains are stored first (they are final before the colour starts, so the
+// thread gathers all of them at once) and entries inside the chain after all of
+// them, as chain-local row numbers; each part keeps the reference's subtraction
+// order (ascending columns for L, descending for U). Slot k of a row is a
+// 32-wide column across the group's chains, so a warp's loads coalesce.
 #include <algorithm>
 #include <climits>
 
@@ -53,7 +53,7 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
             else if (group_of_row && (*group_of_row)[c] >= (*group_of_row)[row])
                 ok = false;  // a column outside the chain must belong to a group solved earlier
         }
-        if (!ok) {
+        if (!ok || e - b - ni > 255 || ni > 255) {
 #pragma omp atomic write
             bad = row;
         }
@@ -62,68 +62,89 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     }
     SENK_REQUIRE(bad < 0, std::string(upper ? "U" : "L") + " factor row " + std::to_string(bad) +
                               " does not fit the schedule (diagonal first in U, strictly triangular, "
-                              "columns of other chains in earlier colours)");
-    std::vector<SliceDesc> sl;
-    F.group_slices.assign(1, 0);
+                              "columns of other chains in earlier colours, at most 255 entries)");
+    // Groups of up to 32 chains inside each colour, in processing order.
+    std::vector<GroupDesc> gd;
+    F.colour_groups.assign(1, 0);
     for (const Group &g : groups) {
-        for (int p = g.p0; p < g.p1; p += 32) {
-            SliceDesc d{};
-            d.pos0 = p;
-            d.nrows = (short)std::min(32, g.p1 - p);
-            sl.push_back(d);
+        const int nch = (g.p1 - g.p0) / bs;
+        for (int q = 0; q < nch; q += 32) {
+            GroupDesc d{};
+            d.pos0 = g.p0 + q * bs;
+            d.nchains = std::min(32, nch - q);
+            d.widx = (int)gd.size() * 2 * bs;
+            gd.push_back(d);
         }
-        F.group_slices.push_back((int)sl.size());
+        F.colour_groups.push_back((int)gd.size());
     }
-    const int ns = (int)sl.size();
+    const int ng = (int)gd.size();
+    std::vector<unsigned char> wd((size_t)std::max(ng, 1) * 2 * bs, 0);
+    std::vector<long long> slots(ng, 0);
 #pragma omp parallel for schedule(static)
-    for (int i = 0; i < ns; i++) {
-        int we = 0, wi = 0;
-        for (int l = 0; l < sl[i].nrows; l++) {
-            we = std::max(we, next[sl[i].pos0 + l]);
-            wi = std::max(wi, nint[sl[i].pos0 + l]);
+    for (int i = 0; i < ng; i++) {
+        long long tot = 0;
+        for (int l = 0; l < bs; l++) {
+            int we = 0, wi = 0;
+            for (int q = 0; q < gd[i].nchains; q++) {
+                const int p = gd[i].pos0 + q * bs + l;
+                we = std::max(we, next[p]);
+                wi = std::max(wi, nint[p]);
+            }
+            wd[(size_t)gd[i].widx + l] = (unsigned char)we;
+            wd[(size_t)gd[i].widx + bs + l] = (unsigned char)wi;
+            tot += we + wi;
         }
-        sl[i].we = (short)we;
-        sl[i].wi = (short)wi;
+        slots[i] = tot;
     }
     long long off = 0;
-    for (int i = 0; i < ns; i++) {
-        sl[i].off = (int)off;
-        off += (long long)(sl[i].we + sl[i].wi) * 32;
+    for (int i = 0; i < ng; i++) {
+        gd[i].off = (int)off;
+        off += slots[i] * 32;
         SENK_REQUIRE(off < INT_MAX, "factor too large for 32-bit slot offsets");
     }
+    // Shared memory a colour's CTAs need to stage their group's block.
+    F.colour_smem.assign(F.colour_groups.size() - 1, 0);
+    for (size_t c = 0; c + 1 < F.colour_groups.size(); c++)
+        for (int i = F.colour_groups[c]; i < F.colour_groups[c + 1]; i++)
+            F.colour_smem[c] = std::max(F.colour_smem[c], (size_t)slots[i] * 32 * (sizeof(VT) + sizeof(int)));
     F.elems = off;
     std::vector<VT> hv((size_t)std::max<long long>(off, 1), VT(0));
     std::vector<int> hc((size_t)std::max<long long>(off, 1), -1);
     std::vector<VT> hd(upper ? N : 0);
     long long stored = 0;
 #pragma omp parallel for schedule(static) reduction(+ : stored)
-    for (int i = 0; i < ns; i++) {
-        const SliceDesc d = sl[i];
-        for (int l = 0; l < d.nrows; l++) {
-            const int p = d.pos0 + l;
-            const int row = rowmap ? (*rowmap)[p] : p;
-            const int cs = row - row % bs, ce = cs + bs;
-            int ke = 0, ki = 0;
-            auto put = [&](int j) {
-                const int c = cind[j];
-                if (chains && c >= cs && c < ce) {
-                    const long long at = d.off + (long long)(d.we + ki) * 32 + l;
+    for (int i = 0; i < ng; i++) {
+        const GroupDesc d = gd[i];
+        const unsigned char *w = wd.data() + d.widx;
+        int eoff[32], ioff[32];
+        int acc = 0;
+        for (int l = 0; l < bs; l++) { eoff[l] = acc; acc += w[l]; }
+        for (int l = 0; l < bs; l++) { ioff[l] = acc; acc += w[bs + l]; }
+        for (int q = 0; q < d.nchains; q++) {
+            for (int l = 0; l < bs; l++) {
+                const int p = d.pos0 + q * bs + l;
+                const int row = rowmap ? (*rowmap)[p] : p;
+                const int cs = row - row % bs, ce = cs + bs;
+                int ke = 0, ki = 0;
+                auto put = [&](int j) {
+                    const int c = cind[j];
+                    long long at;
+                    if (chains && c >= cs && c < ce) {
+                        at = d.off + (long long)(ioff[l] + ki++) * 32 + q;
+                        hc[at] = c - cs;
+                    } else {
+                        at = d.off + (long long)(eoff[l] + ke++) * 32 + q;
+                        hc[at] = c;
+                    }
                     hv[at] = val[j];
-                    hc[at] = c - cs;
-                    ki++;
+                    stored++;
+                };
+                if (upper) {
+                    hd[p] = val[rptr[row]];
+                    for (int j = rptr[row + 1] - 1; j >= rptr[row] + 1; j--) put(j);
                 } else {
-                    const long long at = d.off + (long long)ke * 32 + l;
-                    hv[at] = val[j];
-                    hc[at] = c;
-                    ke++;
+                    for (int j = rptr[row]; j < rptr[row + 1]; j++) put(j);
                 }
-                stored++;
-            };
-            if (upper) {
-                hd[p] = val[rptr[row]];
-                for (int j = rptr[row + 1] - 1; j >= rptr[row] + 1; j--) put(j);
-            } else {
-                for (int j = rptr[row]; j < rptr[row + 1]; j++) put(j);
             }
         }
     }
@@ -140,8 +161,10 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
         F.rowmap.alloc(N);
         F.rowmap.upload(rowmap->data(), N, s);
     }
-    F.slices.alloc(std::max(ns, 1));
-    F.slices.upload(sl.data(), ns, s);
+    F.groups.alloc(std::max(ng, 1));
+    F.groups.upload(gd.data(), ng, s);
+    F.widths.alloc(wd.size());
+    F.widths.upload(wd.data(), wd.size(), s);
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
 }
@@ -179,37 +202,79 @@ void level_schedule(int N, const int *cind, const int *rptr, bool upper, std::ve
     for (int l = 0; l <= maxlev; l++) groups.push_back({cnt[l], cnt[l + 1]});
 }
 
-template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
-void launch_group(const SweepFactor<VT> &F, int sb, int se, const XT *x, XT *y, cudaStream_t s, const int *gate)
+// Largest block staged through shared memory; bigger groups read the factor
+// from global memory instead.
+constexpr size_t kMaxStagedBytes = 160 * 1024;
+
+template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED, bool STAGED>
+void launch_group(const SweepFactor<VT> &F, int *status, int gb, int ge, size_t smem, const XT *x, XT *y,
+                  cudaStream_t s, const int *gate)
 {
-    const int warps_per_cta = kThreads / 32;
-    const int grid = ceil_div(se - sb, warps_per_cta);
-    k_sweep<VT, XT, BS, UPPER, MAPPED><<<grid, kThreads, 0, s>>>(F.slices.p, sb, se, F.val.p, F.col.p, F.dinv.p,
-                                                                  F.rowmap.p, x, y, gate);
+    auto kern = k_sweep<VT, XT, BS, UPPER, MAPPED, STAGED>;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(ge - gb);
+    cfg.blockDim = dim3(BS * 32);
+    cfg.dynamicSmemBytes = STAGED ? smem : 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SENK_CUDA(cudaLaunchKernelEx(&cfg, kern, (const GroupDesc *)F.groups.p, gb, (const unsigned char *)F.widths.p,
+                                 (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p,
+                                 (const int *)F.rowmap.p, x, y, gate, status));
+}
+
+template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
+void launch_colour(const SweepFactor<VT> &F, int *status, int c, const XT *x, XT *y, cudaStream_t s,
+                   const int *gate)
+{
+    const int gb = F.colour_groups[c], ge = F.colour_groups[c + 1];
+    if (ge == gb) return;
+    const size_t smem = F.colour_smem[c];
+    if (smem <= kMaxStagedBytes) launch_group<VT, XT, BS, UPPER, MAPPED, true>(F, status, gb, ge, smem, x, y, s, gate);
+    else launch_group<VT, XT, BS, UPPER, MAPPED, false>(F, status, gb, ge, smem, x, y, s, gate);
+}
+
+template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
+void allow_smem()
+{
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep<VT, XT, BS, UPPER, MAPPED, true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStagedBytes));
 }
 
 template <typename VT, typename XT, bool UPPER>
-void sweep_groups(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate)
+void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
-    const int ng = (int)F.group_slices.size() - 1;
-    for (int g = 0; g < ng; g++) {
-        const int sb = F.group_slices[g], se = F.group_slices[g + 1];
-        if (se == sb) continue;
+    const int nc = (int)F.colour_groups.size() - 1;
+    for (int c = 0; c < nc; c++) {
         if (F.mapped) {
-            launch_group<VT, XT, 1, UPPER, true>(F, sb, se, x, y, s, gate);
+            launch_colour<VT, XT, 1, UPPER, true>(F, status, c, x, y, s, gate);
             continue;
         }
         switch (F.bs) {
-        case 1: launch_group<VT, XT, 1, UPPER, false>(F, sb, se, x, y, s, gate); break;
-        case 2: launch_group<VT, XT, 2, UPPER, false>(F, sb, se, x, y, s, gate); break;
-        case 4: launch_group<VT, XT, 4, UPPER, false>(F, sb, se, x, y, s, gate); break;
-        case 8: launch_group<VT, XT, 8, UPPER, false>(F, sb, se, x, y, s, gate); break;
-        case 16: launch_group<VT, XT, 16, UPPER, false>(F, sb, se, x, y, s, gate); break;
-        case 32: launch_group<VT, XT, 32, UPPER, false>(F, sb, se, x, y, s, gate); break;
+        case 1: launch_colour<VT, XT, 1, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 2: launch_colour<VT, XT, 2, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 4: launch_colour<VT, XT, 4, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 8: launch_colour<VT, XT, 8, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 16: launch_colour<VT, XT, 16, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 32: launch_colour<VT, XT, 32, UPPER, false>(F, status, c, x, y, s, gate); break;
         default: throw ArgError("unsupported chain length");
         }
     }
-    SENK_LAUNCH_CHECK();
+}
+
+template <typename VT, typename XT>
+void allow_all_smem()
+{
+    allow_smem<VT, XT, 1, false, true>(); allow_smem<VT, XT, 1, true, true>();
+    allow_smem<VT, XT, 1, false, false>(); allow_smem<VT, XT, 1, true, false>();
+    allow_smem<VT, XT, 2, false, false>(); allow_smem<VT, XT, 2, true, false>();
+    allow_smem<VT, XT, 4, false, false>(); allow_smem<VT, XT, 4, true, false>();
+    allow_smem<VT, XT, 8, false, false>(); allow_smem<VT, XT, 8, true, false>();
+    allow_smem<VT, XT, 16, false, false>(); allow_smem<VT, XT, 16, true, false>();
+    allow_smem<VT, XT, 32, false, false>(); allow_smem<VT, XT, 32, true, false>();
 }
 
 }  // namespace
@@ -223,6 +288,9 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
     SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
     n = N;
     precond = pckind;
+    status.alloc(1);
+    SENK_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+    allow_all_smem<VT, VT>();
     if (pckind == SENK_PC_ILU) {
         std::vector<int> rm;
         std::vector<Group> gr;
@@ -256,8 +324,8 @@ template <typename VT>
 template <typename XT>
 void IluPlan<VT>::sweep(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate) const
 {
-    if (F.upper) sweep_groups<VT, XT, true>(F, x, y, s, gate);
-    else sweep_groups<VT, XT, false>(F, x, y, s, gate);
+    if (F.upper) sweep_groups<VT, XT, true>(F, status.p, x, y, s, gate);
+    else sweep_groups<VT, XT, false>(F, status.p, x, y, s, gate);
 }
 
 template <typename VT>
@@ -267,6 +335,15 @@ long long IluPlan<VT>::apply_bytes() const
     // stored entries: value + column; U diagonal: value only; x read, t written,
     // t read and written again by the in-place U sweep.
     return (L.nnz + (U.nnz - n)) * (vb + 4) + (long long)n * vb + 4LL * n * vb;
+}
+
+template <typename VT>
+void IluPlan<VT>::check_status(cudaStream_t s) const
+{
+    int h = 0;
+    SENK_CUDA(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SENK_CUDA(cudaStreamSynchronize(s));
+    if (h) throw CudaError{cudaErrorLaunchTimeout, "ILU sweep: a TMA wait did not complete", __FILE__, __LINE__};
 }
 
 template struct IluPlan<double>;
@@ -311,6 +388,7 @@ int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *strea
         cudaStream_t s = (cudaStream_t)stream;
         if (plan->d) plan->d->apply((const double *)x, (double *)y, s, nullptr);
         else plan->f->apply((const float *)x, (float *)y, s, nullptr);
+        SENK_LAUNCH_CHECK();
         return (int)kOk;
     });
 }
