@@ -117,6 +117,61 @@ k_spmv_sell32(const MT *__restrict__ val, const int *__restrict__ col, const int
     if (row < n && row >= 0) y[row] = MODE == 1 ? (XT)((A)b[row] - sum) : (XT)sum;
 }
 
+// r = b - A x on the SELL-32 copy, with ||r||^2 reduced to the last CTA, which
+// stores ||r|| in *norm_out and 1/||r|| in *inv_out.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_residual_sell32(const T *__restrict__ val, const int *__restrict__ col, const int *__restrict__ off,
+                  const T *__restrict__ x, const T *__restrict__ b, T *__restrict__ r, int n, double *part,
+                  unsigned *ticket, double *norm_out, double *inv_out)
+{
+    using A = typename Acc<T>::type;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double nacc = 0;
+    if (p < n) {
+        const int s = (int)(p >> 5), lane = (int)(p & 31);
+        const int o = __ldg(off + s), w = (__ldg(off + s + 1) - o) >> 5;
+        A sum = 0;
+        for (int k = 0; k < w; k++) {
+            const int i0 = o + k * 32 + lane;
+            sum += (A)ld_stream(val + i0) * (A)__ldg(x + ld_stream(col + i0));
+        }
+        const T v = (T)((A)b[p] - sum);
+        r[p] = v;
+        nacc = (double)v * (double)v;
+    }
+    __shared__ double sh[32];
+    const double t = block_sum(nacc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    if (last_cta_arrives(ticket, gridDim.x)) {
+        double s = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += part[i];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) {
+            const double nr = sqrt(s);
+            *norm_out = nr;
+            if (inv_out) *inv_out = 1.0 / nr;
+        }
+    }
+}
+
+// Iterative refinement glue: r32 = (float)(r * (*inv)); x += (*norm) * d32.
+static __global__ void __launch_bounds__(kThreads)
+k_ir_demote(const double *__restrict__ r, const double *inv, float *__restrict__ r32, long long n)
+{
+    const double s = *inv;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        r32[i] = (float)(r[i] * s);
+}
+
+static __global__ void __launch_bounds__(kThreads)
+k_ir_correct(double *__restrict__ x, const double *norm, const float *__restrict__ d32, long long n)
+{
+    const double s = *norm;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] += s * (double)d32[i];
+}
+
 // CSR SpMV with a separately stored diagonal (reference SpmvCsr with diag).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -217,20 +272,41 @@ k_multidot(const XT *__restrict__ V, long long ldv, int nv, const XT *__restrict
     constexpr int CH = 8;
     const int c0 = blockIdx.y * CH;
     const int nc = min(CH, nv - c0);
-    double acc[CH];
+    // Per-thread partial sums in the vector type (FP32 vectors stay on the FP32
+    // pipe), combined across threads and CTAs in FP64; four independent
+    // elements per step keep enough loads in flight.
+    using A = typename Acc<XT>::type;
+    A acc[CH];
 #pragma unroll
     for (int q = 0; q < CH; q++) acc[q] = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double wi = (double)w[i];
+    const long long S = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * S < n; i += 4 * S) {
+        const A w0 = (A)w[i], w1 = (A)w[i + S], w2 = (A)w[i + 2 * S], w3 = (A)w[i + 3 * S];
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            if (q < nc) {
+                const XT *vq = V + (long long)(c0 + q) * ldv + i;
+                const A a0 = (A)ld_stream(vq), a1 = (A)ld_stream(vq + S), a2 = (A)ld_stream(vq + 2 * S),
+                        a3 = (A)ld_stream(vq + 3 * S);
+                acc[q] += a0 * w0;
+                acc[q] += a1 * w1;
+                acc[q] += a2 * w2;
+                acc[q] += a3 * w3;
+            }
+        }
+    }
+    for (; i < n; i += S) {
+        const A wi = (A)w[i];
 #pragma unroll
         for (int q = 0; q < CH; q++)
-            if (q < nc) acc[q] += (double)ld_stream(V + (long long)(c0 + q) * ldv + i) * wi;
+            if (q < nc) acc[q] += (A)ld_stream(V + (long long)(c0 + q) * ldv + i) * wi;
     }
     __shared__ double sh[CH][kThreads / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < CH; q++) {
-        double v = warp_sum(acc[q]);
+        double v = warp_sum((double)acc[q]);
         if (lane == 0) sh[q][wid] = v;
     }
     __syncthreads();
@@ -307,19 +383,45 @@ k_update(const XT *__restrict__ V, long long ldv, int nv, const double *__restri
          KrylovState *st, GmresEpi g, const int *gate)
 {
     if (gated(gate)) return;
-    __shared__ double sc[64];
-    if (threadIdx.x < nv) sc[threadIdx.x] = coef[threadIdx.x];
+    using A = typename Acc<XT>::type;  // FP32 vectors are updated on the FP32 pipe
+    __shared__ A sc[64];
+    if (threadIdx.x < nv) sc[threadIdx.x] = (A)coef[threadIdx.x];
     __syncthreads();
-    double nacc = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double v = (double)w[i];
-        for (int k = 0; k < nv; k++) v -= sc[k] * (double)ld_stream(V + (long long)k * ldv + i);
+    A nacc = 0;
+    const long long S = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * S < n; i += 4 * S) {  // four independent elements per step
+        A v0 = (A)w[i], v1 = (A)w[i + S], v2 = (A)w[i + 2 * S], v3 = (A)w[i + 3 * S];
+#pragma unroll 2
+        for (int k = 0; k < nv; k++) {
+            const XT *vk = V + (long long)k * ldv + i;
+            const A c = sc[k];
+            const A a0 = (A)ld_stream(vk), a1 = (A)ld_stream(vk + S), a2 = (A)ld_stream(vk + 2 * S),
+                    a3 = (A)ld_stream(vk + 3 * S);
+            v0 -= c * a0;
+            v1 -= c * a1;
+            v2 -= c * a2;
+            v3 -= c * a3;
+        }
+        const XT t0 = (XT)v0, t1 = (XT)v1, t2 = (XT)v2, t3 = (XT)v3;
+        w[i] = t0;
+        w[i + S] = t1;
+        w[i + 2 * S] = t2;
+        w[i + 3 * S] = t3;
+        nacc += (A)t0 * (A)t0;
+        nacc += (A)t1 * (A)t1;
+        nacc += (A)t2 * (A)t2;
+        nacc += (A)t3 * (A)t3;
+    }
+    for (; i < n; i += S) {
+        A v = (A)w[i];
+        for (int k = 0; k < nv; k++) v -= sc[k] * (A)ld_stream(V + (long long)k * ldv + i);
         const XT vt = (XT)v;
         w[i] = vt;
-        nacc += (double)vt * (double)vt;
+        nacc += (A)vt * (A)vt;
     }
     __shared__ double sh[32];
-    double t = block_sum(nacc, sh);
+    double t = block_sum((double)nacc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     if (last_cta_arrives(ticket, gridDim.x)) {
         double s = 0;
@@ -359,18 +461,36 @@ __global__ void __launch_bounds__(kThreads)
 k_gmres_combine(XT *__restrict__ V, long long ldv, const double *__restrict__ y, const KrylovState *st,
                 XT *__restrict__ x, long long n, int m)
 {
-    __shared__ double sy[64];
+    using A = typename Acc<XT>::type;
+    __shared__ A sy[64];
     const int J = st->done ? st->jconv : m;
-    if (threadIdx.x < J) sy[threadIdx.x] = y[threadIdx.x];
+    if (threadIdx.x < J) sy[threadIdx.x] = (A)y[threadIdx.x];
     __syncthreads();
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long S = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * S < n; i += 4 * S) {  // four independent elements per step
+        A v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = PRE ? sy[0] * (A)V[i + u * S] : (A)x[i + u * S];
+        for (int k = PRE ? 1 : 0; k < J; k++) {
+            const XT *vk = V + (long long)k * ldv + i;
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] += sy[k] * (A)vk[u * S];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (PRE) V[i + u * S] = (XT)v[u];
+            else x[i + u * S] = (XT)v[u];
+        }
+    }
+    for (; i < n; i += S) {
         if (PRE) {
-            double v = sy[0] * (double)V[i];
-            for (int k = 1; k < J; k++) v += sy[k] * (double)V[(long long)k * ldv + i];
+            A v = sy[0] * (A)V[i];
+            for (int k = 1; k < J; k++) v += sy[k] * (A)V[(long long)k * ldv + i];
             V[i] = (XT)v;
         } else {
-            double v = (double)x[i];
-            for (int k = 0; k < J; k++) v += sy[k] * (double)V[(long long)k * ldv + i];
+            A v = (A)x[i];
+            for (int k = 0; k < J; k++) v += sy[k] * (A)V[(long long)k * ldv + i];
             x[i] = (XT)v;
         }
     }

@@ -12,7 +12,7 @@ namespace senkgpu {
 
 namespace {
 
-constexpr int kRedCtas = 2 * kNumSMs;  // CTAs of the multi-dot / update kernels
+constexpr int kRedCtas = 4 * kNumSMs;  // CTAs of the multi-dot / update kernels
 
 template <typename T, int OP>
 void ew(const T *x, T *y, T *z, long long n, T a, T b, const double *a_dev, double a_mul, cudaStream_t s,
