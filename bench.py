@@ -8,12 +8,15 @@ x_true ~ U(-1,1) (seed 0); ABMC ordering with block size 16 ("connect",
 A + A^T graph); ILU(0); right-preconditioned GMRES(30) in FP64 to a 1e-8
 relative residual (x0 = 0).
 
-A step is one complete solve. ``value`` is the mean solve time with A, the
-factors, b and the Krylov workspace resident in HBM (CUDA events on the
-library's stream); ``e2e`` is the same solve through the drop-in C ABI call with
-host arrays (upload, factor re-layout, solve and copy-back of x inside the timed
-region). Inputs are larger than L2 (A + L + U + V is about 0.9 GB), so no flush
-is needed between steps.
+A step is one complete solve. ``value`` is the mean time of the mixed-precision
+solve (GMRES-IR: FP32 ILU factors, sweeps, inner SpMV and Krylov basis inside an
+FP64 refinement loop that stops when the FP64 true residual ||b-Ax||/||b|| is
+below 1e-8) with A, the factors, b and the workspaces resident in HBM (CUDA
+events on the library's stream); the plain FP64 ABMC-ILU(0)-GMRES(30) solve on
+the same GPU is reported beside it (``plain_fp64``). ``e2e`` is the mixed solve
+through the drop-in C ABI call with host arrays (upload, factor re-layout, solve
+and copy-back of x inside the timed region). Inputs are larger than L2 (A, L, U
+and the Krylov bases are about 1.2 GB), so no flush is needed between steps.
 
     python bench.py [--steps K] [--warmup W] [--impl reference]
 """
@@ -33,7 +36,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "solve ms to 1e-8 rel. residual (ABMC-ILU(0)-GMRES(30), FP64)"
+METRIC = "solve ms to 1e-8 FP64 true rel. residual (ABMC-ILU(0) GMRES(30), mixed-precision GMRES-IR)"
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
 
 
@@ -51,6 +54,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-kernels", action="store_true", help="skip the per-kernel timings (profiling runs)")
+    ap.add_argument("--only", default="both", choices=["both", "mixed", "plain"], help="which solves to time")
+    ap.add_argument("--inner-tol", type=float, default=1e-4)
+    ap.add_argument("--inner-cycles", type=int, default=2)
     return ap.parse_args()
 
 
@@ -208,47 +214,65 @@ def run_gpu(args, rank, world):
     orth = {"cgs2": L.ORTH_CGS2, "cgs": L.ORTH_CGS, "mgs": L.ORTH_MGS}[args.orth]
     spmv = {"auto": L.SPMV_AUTO, "csr": L.SPMV_CSR, "sell": L.SPMV_SELL}[args.spmv]
     outer = 10000 // args.m
-    sysm = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=args.m, orth=orth, spmv=spmv)
+    ir_outer = 20
+    sysm = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=args.m, mixed=True, orth=orth, spmv=spmv)
     sysm.set_rhs(b)
+    do_mixed, do_plain = args.only in ("both", "mixed"), args.only in ("both", "plain")
+    mixed = lambda: sysm.gmres_ir(nb, ir_outer, args.m, args.eps, args.inner_tol, args.inner_cycles)
+    plain = lambda: sysm.gmres(nb, outer, args.m, args.eps)
     for _ in range(args.warmup):
-        sysm.zero_x()
-        sysm.gmres(nb, outer, args.m, args.eps)
+        if do_mixed:
+            sysm.zero_x()
+            mixed()
+        if do_plain:
+            sysm.zero_x()
+            plain()
     barrier(world)
-    results = []
+    res_m, res_p = [], []
     with Clocks(local) as clk:
         for _ in range(args.steps):
+            if do_mixed:
+                sysm.zero_x()
+                res_m.append(mixed())
+    if do_mixed:
+        x = sysm.get_x()
+        true_m = float(np.linalg.norm(b - Ar.matvec(x)) / nb)
+    for _ in range(args.steps):
+        if do_plain:
             sysm.zero_x()
-            results.append(sysm.gmres(nb, outer, args.m, args.eps))
+            res_p.append(plain())
+    if do_plain:
+        x = sysm.get_x()
+        true_p = float(np.linalg.norm(b - Ar.matvec(x)) / nb)
     barrier(world)
-    dev_ms = sum(r.solve_ms for r in results) / len(results)
-    dev_ms = allmax(world, dev_ms)
-    x = sysm.get_x()
-    true_res = float(np.linalg.norm(b - Ar.matvec(x)) / nb)
-    r = results[-1]
+    mean = lambda rs: sum(r.solve_ms for r in rs) / len(rs)
     hbm, peak_kind = peaks()
-    # kernel-level figures, CUDA events on the system's stream
     reps = 0 if args.no_kernels else 20
     timed = lambda op: sysm.time_op(op, reps) if reps else (float("nan"), 0)
-    pre_ms, pre_bytes = timed(L.OP_PRECOND)
-    l_ms, l_bytes = timed(L.OP_SWEEP_L)
-    u_ms, u_bytes = timed(L.OP_SWEEP_U)
-    sp_ms, sp_bytes = timed(L.OP_SPMV)
-    dot_ms, dot_bytes = timed(L.OP_DOT)
-    gbs = lambda by, ms: by / (ms * 1e-3) / 1e9
+    gbs = lambda by, ms: by / (ms * 1e-3) / 1e9 if ms == ms and ms > 0 else float("nan")
+    kern = {}
+    for tag, base in (("f32", L.OP_INNER), ("f64", 0)):
+        for name, op in (("ilu_apply", L.OP_PRECOND), ("sptrsv_l", L.OP_SWEEP_L), ("sptrsv_u", L.OP_SWEEP_U),
+                         ("spmv", L.OP_SPMV), ("dot", L.OP_DOT)):
+            ms, by = timed(base + op)
+            kern[f"{name}_{tag}_ms"] = ms
+            kern[f"{name}_{tag}_gbs"] = gbs(by, ms)
+            kern[f"{name}_{tag}_bytes"] = by
     sysm.close()
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and do_mixed:
         e2e_ms, rr = [], None
         for i in range(max(1, min(args.steps, 3))):
             xh = np.zeros(Ar.n)
             t0 = time.perf_counter()
-            rr = SV.AbmcIluGmresm(Ar.val, Ar.cind, Ar.rptr, Lf.val, Lf.cind, Lf.rptr, Uf.val, Uf.cind, Uf.rptr, sc,
-                                  nc, 16, b, xh, nb, outer, args.m, Ar.n, args.eps, orth=orth, spmv=spmv)
+            rr = SV.AbmcIluGmresIr(Ar.val, Ar.cind, Ar.rptr, Lf.val, Lf.cind, Lf.rptr, Uf.val, Uf.cind, Uf.rptr, sc,
+                                   nc, 16, b, xh, nb, ir_outer, args.m, Ar.n, args.eps, args.inner_tol,
+                                   args.inner_cycles, orth=orth, spmv=spmv)
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
         e2e = {"value": allmax(world, sum(e2e_ms) / len(e2e_ms)), "unit": "ms",
                "h2d_bytes_per_step": int(rr.h2d_bytes), "d2h_bytes_per_step": int(rr.d2h_bytes),
                "steps": len(e2e_ms), "iterations": rr.iters,
-               "note": "drop-in C ABI call senk_abmc_ilu_gmres_d with host arrays; wall clock"}
+               "note": "drop-in C ABI call senk_abmc_ilu_gmres_ir_d with host arrays; wall clock"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -256,29 +280,37 @@ def run_gpu(args, rank, world):
         threads = os.cpu_count() or 1
         cms, cit, _ = cpu_solve(port, Ar, Lf, Uf, nc, sc, b, args.eps, args.m, threads)
         cpu = {"value": cms, "unit": "ms", "cores": threads, "kind": "port",
-               "sample": f"one full solve of the workload ({cit} iterations), oracle C restatement of the "
+               "sample": f"one full FP64 solve of the workload ({cit} iterations), oracle C restatement of the "
                          "reference with OpenMP"}
     if rank != 0:
         return
-    pre_gbs = gbs(pre_bytes, pre_ms)
+    value = allmax(world, mean(res_m)) if do_mixed else allmax(world, mean(res_p))
+    rm = res_m[-1] if do_mixed else None
+    rp = res_p[-1] if do_plain else None
+    dom = "ilu_apply_f32" if do_mixed else "ilu_apply_f64"
     line = {
-        "metric": METRIC, "value": dev_ms, "unit": "ms", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if do_mixed else "f64", "data": "synthetic",
         "config": {"workload": workload_name(args.n), "N": Ar.n, "nnz": Ar.nnz, "colours": nc,
-                   "orth": args.orth, "spmv": args.spmv, "iterations": r.iters, "cycles": r.cycles,
-                   "implicit_residual": r.res, "true_residual": true_res,
-                   "l2": "inputs larger than L2 (A, L, U and the 31 basis vectors, about 0.9 GB)",
+                   "orth": args.orth, "spmv": args.spmv, "inner_tol": args.inner_tol,
+                   "inner_cycles": args.inner_cycles,
+                   "iterations": rm.iters if rm else rp.iters,
+                   "outer_steps": rm.cycles if rm else None,
+                   "true_residual": true_m if rm else true_p,
+                   "l2": "inputs larger than L2 (A, L, U and the Krylov bases, about 1.2 GB)",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "plain_fp64": None if rp is None else {"ms": allmax(world, mean(res_p)), "iterations": rp.iters,
+                                               "cycles": rp.cycles, "implicit_residual": rp.res,
+                                               "true_residual": true_p},
         "e2e": e2e,
-        "gpu_launches": int(sum(x.launches for x in results)),
-        "roofline": {"kernel": "ILU(0) application: ABMC L and U sweeps, all colours", "bound": "hbm",
-                     "achieved": pre_gbs, "peak": hbm, "unit": "GB/s", "frac": pre_gbs / hbm,
-                     "peak_source": peak_kind, "traffic": traffic_for("ilu_apply"),
-                     "bytes_per_launch": pre_bytes, "ms_per_launch": pre_ms},
-        "kernels": {"spmv_gbs": gbs(sp_bytes, sp_ms), "spmv_ms": sp_ms,
-                    "sptrsv_l_gbs": gbs(l_bytes, l_ms), "sptrsv_u_gbs": gbs(u_bytes, u_ms),
-                    "ilu_apply_gbs": pre_gbs, "ilu_apply_ms": pre_ms, "dot_gbs": gbs(dot_bytes, dot_ms)},
+        "gpu_launches": int(sum(x.launches for x in (res_m if do_mixed else res_p))),
+        "roofline": {"kernel": "ILU(0) application (ABMC L and U sweeps, all colours), "
+                               + ("FP32 factors" if do_mixed else "FP64"),
+                     "bound": "hbm", "achieved": kern[dom + "_gbs"], "peak": hbm, "unit": "GB/s",
+                     "frac": kern[dom + "_gbs"] / hbm, "peak_source": peak_kind, "traffic": traffic_for(dom),
+                     "bytes_per_launch": kern[dom + "_bytes"], "ms_per_launch": kern[dom + "_ms"]},
+        "kernels": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in kern.items()},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }

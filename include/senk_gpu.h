@@ -123,6 +123,19 @@ int senk_abmc_ilu_gmres_s(const float *val, const int *cind, const int *rptr,
                           int outer, int m, int N, float epsilon,
                           const senk_options *opt, senk_result *res);
 
+/* AbmcIluGmresm arguments, solved by mixed-precision GMRES-IR (see
+ * senk_system_gmres_ir): FP32 ILU factors, SpTRSV sweeps, inner SpMV and Krylov
+ * basis inside an FP64 refinement loop that stops on the FP64 true residual.
+ * No direct counterpart in the reference (its FP32/FP64 refinement prototypes
+ * are commented out, include/senk_bicgstab.hpp:269-296). */
+int senk_abmc_ilu_gmres_ir_d(const double *val, const int *cind, const int *rptr,
+                             const double *lval, const int *lcind, const int *lrptr,
+                             const double *uval, const int *ucind, const int *urptr,
+                             const int *cptr, int cnum, int bsize,
+                             const double *b, double *x, double nrm_b,
+                             int max_outer, int m, int N, double epsilon, double inner_tol,
+                             int inner_cycles, const senk_options *opt, senk_result *res);
+
 /* ================================================ device-resident systems ==
  * Upload once, solve many times (the timed path of the benchmark). */
 typedef struct senk_system senk_system;
@@ -138,7 +151,9 @@ typedef struct {
     const void *lval; const int *lcind; const int *lrptr; /* split L (host) */
     const void *uval; const int *ucind; const int *urptr; /* split U (host) */
     const int *cptr; int cnum; int bsize;                 /* colour schedule */
-    int m_max;                 /* largest restart length to be used (<= 64) */
+    int m_max;                 /* largest restart length to be used (<= 63) */
+    int mixed;                 /* 1 (SENK_F64 systems): also build the FP32 copies
+                                  (A, factors, Krylov basis) used by GMRES-IR */
 } senk_system_desc;
 
 int senk_system_create(senk_system **out, const senk_system_desc *desc, const senk_options *opt);
@@ -160,6 +175,17 @@ void *senk_system_x(senk_system *sys);
 int senk_system_gmres(senk_system *sys, double nrm_b, int outer, int m, double epsilon,
                       senk_result *res);
 
+/* Mixed-precision GMRES iterative refinement on a system created with
+ * desc->mixed = 1 (new: the reference has only commented-out FP32/FP64 refinement
+ * prototypes, include/senk_bicgstab.hpp:269-296). Outer loop in FP64: r = b - A x,
+ * stop when ||r|| <= epsilon * nrm_b (the FP64 true residual), else solve
+ * A d = r / ||r|| with FP32 right-preconditioned GMRES(m) (FP32 A, ILU factors,
+ * sweeps and Krylov basis; FP64 Hessenberg/Givens) to inner_tol or
+ * inner_cycles restart cycles, and x += ||r|| d in FP64. res->iters counts inner
+ * iterations, res->cycles outer steps, res->res is the final FP64 true residual. */
+int senk_system_gmres_ir(senk_system *sys, double nrm_b, int max_outer, int m, double epsilon,
+                         double inner_tol, int inner_cycles, senk_result *res);
+
 /* Times `reps` back-to-back runs of one operation of the system's solve path on
  * its stream with CUDA events (after one untimed run). Reports the mean time of
  * one run and its algorithmic bytes (matrix values and indices once, each vector
@@ -168,7 +194,8 @@ int senk_system_gmres(senk_system *sys, double nrm_b, int outer, int m, double e
 #define SENK_OP_PRECOND 1   /* t = U^-1 L^-1 v, all colours of both sweeps */
 #define SENK_OP_SWEEP_L 2   /* the L sweep alone */
 #define SENK_OP_SWEEP_U 3   /* the U sweep alone (in place) */
-#define SENK_OP_DOT 4       /* one FP64 dot product of two vectors */
+#define SENK_OP_DOT 4       /* one dot product of two vectors */
+#define SENK_OP_INNER 16    /* added to an op: the FP32 copy of a mixed system */
 int senk_system_time_op(senk_system *sys, int op, int reps, double *ms_per_rep, long long *bytes_per_rep);
 
 /* ================================================ device kernels (one op) ==

@@ -199,10 +199,20 @@ struct System {
     long long cycle_nodes = 0;       // kernel nodes of the captured cycle
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
+    // Mixed precision (FP64 systems created with desc.mixed): the FP32 copy
+    // that runs the inner solves of GMRES-IR on the same stream.
+    std::unique_ptr<System<float>> inner;
+    DevBuf<double> irs;               // ||r||, 1/||r|| of the outer residual
+    double *ir_host = nullptr;        // pinned mirror of irs
+    bool own_stream = true;
+
     System() = default;
     System(const System &) = delete;
     ~System();
-    void create(const senk_system_desc &d, const senk_options *o);
+    // `shared` (optional): run on this stream instead of creating one.
+    void create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared = nullptr);
+    int gmres_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
+                 senk_result *res);
     void ensure_gmres(int m);
     void enqueue_gmres_cycle(int m);
     int gmres(double nrm_b, int outer, int m, double eps, senk_result *res);

@@ -26,20 +26,27 @@ void ew(const T *x, T *y, T *z, long long n, T a, T b, const double *a_dev, doub
 template <typename T>
 System<T>::~System()
 {
+    inner.reset();
     if (cycle) cudaGraphExecDestroy(cycle);
     if (st_host) cudaFreeHost(st_host);
+    if (ir_host) cudaFreeHost(ir_host);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    if (stream) cudaStreamDestroy(stream);
+    if (stream && own_stream) cudaStreamDestroy(stream);
 }
 
 template <typename T>
-void System<T>::create(const senk_system_desc &d, const senk_options *o)
+void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared)
 {
     SENK_REQUIRE(d.N > 0, "N must be positive");
     n = d.N;
     if (o) opt = *o;
-    SENK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    if (shared) {
+        stream = shared;
+        own_stream = false;
+    } else {
+        SENK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    }
     SENK_CUDA(cudaEventCreate(&ev0));
     SENK_CUDA(cudaEventCreate(&ev1));
     SENK_CUDA(cudaMallocHost((void **)&st_host, sizeof(KrylovState)));
@@ -64,6 +71,34 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o)
         for (const SweepFactor<T> *F : {&pc->L, &pc->U})
             h2d_bytes += (long long)(F->val.bytes() + F->col.bytes() + F->dinv.bytes() + F->rowmap.bytes() +
                                      F->groups.bytes() + F->widths.bytes());
+    }
+    if (d.mixed) {
+        SENK_REQUIRE(sizeof(T) == sizeof(double), "mixed precision needs an FP64 system");
+        // FP32 copies of A and the factors, as senk::utils::Convert makes them
+        // (include/senk_utils.hpp:103-110).
+        auto demote = [](const void *src, int cnt) {
+            std::vector<float> v(cnt);
+            const double *p = static_cast<const double *>(src);
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < cnt; i++) v[i] = (float)p[i];
+            return v;
+        };
+        std::vector<float> a32 = demote(d.val, d.rptr[n]), l32, u32;
+        senk_system_desc di = d;
+        di.dtype = SENK_F32;
+        di.mixed = 0;
+        di.val = a32.data();
+        if (d.precond != SENK_PC_NONE) {
+            l32 = demote(d.lval, d.lrptr[n]);
+            u32 = demote(d.uval, d.urptr[n]);
+            di.lval = l32.data();
+            di.uval = u32.data();
+        }
+        inner = std::make_unique<System<float>>();
+        inner->create(di, &opt, stream);
+        h2d_bytes += inner->h2d_bytes;
+        irs.alloc(2);
+        SENK_CUDA(cudaMallocHost((void **)&ir_host, 2 * sizeof(double)));
     }
 }
 
@@ -280,6 +315,70 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
     *bytes_out = bytes;
 }
 
+template <typename T>
+int System<T>::gmres_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
+                        senk_result *res)
+{
+    SENK_REQUIRE(inner, "GMRES-IR needs a system created with mixed = 1");
+    SENK_REQUIRE(max_outer >= 0 && inner_cycles >= 1 && inner_tol > 0, "bad GMRES-IR parameters");
+    inner->ensure_gmres(m);
+    const int grid = stream_grid(n, kThreads, 8);
+    SENK_CUDA(cudaEventRecord(ev0, stream));
+    long long iters = 0, launches = 0;
+    int outer = 0, conv = 0, brk = 0;
+    double rel = -1;
+    for (int k = 0;; k++) {
+        // FP64 true residual r = b - A x (into t), its norm and inverse
+        A.residual(x.p, b.p, t.p, red, irs.p, irs.p + 1, stream);
+        SENK_CUDA(cudaMemcpyAsync(ir_host, irs.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SENK_CUDA(cudaStreamSynchronize(stream));
+        launches++;
+        rel = ir_host[0] / nrm_b;
+        if (ir_host[0] <= eps * nrm_b) {
+            conv = 1;
+            break;
+        }
+        if (k == max_outer || !(ir_host[0] == ir_host[0])) break;
+        // inner FP32 solve of A d = r/||r|| from d = 0
+        k_ir_demote<<<grid, kThreads, 0, stream>>>(t.p, irs.p + 1, inner->b.p, n);
+        SENK_CUDA(cudaMemsetAsync(inner->x.p, 0, inner->x.bytes(), stream));
+        senk_result ri{};
+        inner->gmres(1.0, inner_cycles, m, inner_tol, &ri);
+        iters += ri.iters;
+        launches += ri.launches + 2;
+        brk |= ri.breakdown;
+        // x += ||r|| d in FP64
+        k_ir_correct<<<grid, kThreads, 0, stream>>>((double *)x.p, irs.p, inner->x.p, n);
+        SENK_LAUNCH_CHECK();
+        outer++;
+    }
+    SENK_CUDA(cudaEventRecord(ev1, stream));
+    SENK_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0;
+    SENK_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    if (opt.verbose) {
+        printf(conv ? "I iter %lld\n" : "# iter %lld\n", iters);
+        printf("# res %e\n", rel);
+        fflush(stdout);
+    }
+    if (res) {
+        res->iters = (int)iters;
+        res->converged = conv;
+        res->res = rel;
+        res->solve_ms = ms;
+        res->breakdown = brk;
+        res->cycles = outer;
+        res->launches = launches;
+    }
+    return kOk;
+}
+
+template <>
+int System<float>::gmres_ir(double, int, int, double, double, int, senk_result *)
+{
+    throw ArgError("GMRES-IR runs on an FP64 system");
+}
+
 template struct System<double>;
 template struct System<float>;
 
@@ -427,11 +526,63 @@ int senk_system_time_op(senk_system *sys, int op, int reps, double *ms_per_rep, 
         SENK_REQUIRE(sys && reps > 0, "bad argument");
         double ms = 0;
         long long bytes = 0;
-        if (sys->d) sys->d->time_op(op, reps, &ms, &bytes);
-        else sys->f->time_op(op, reps, &ms, &bytes);
+        if (op >= SENK_OP_INNER) {
+            SENK_REQUIRE(sys->d && sys->d->inner, "system has no FP32 copy (mixed = 0)");
+            sys->d->inner->time_op(op - SENK_OP_INNER, reps, &ms, &bytes);
+        } else if (sys->d) {
+            sys->d->time_op(op, reps, &ms, &bytes);
+        } else {
+            sys->f->time_op(op, reps, &ms, &bytes);
+        }
         if (ms_per_rep) *ms_per_rep = ms;
         if (bytes_per_rep) *bytes_per_rep = bytes;
         return (int)kOk;
+    });
+}
+
+int senk_system_gmres_ir(senk_system *sys, double nrm_b, int max_outer, int m, double epsilon, double inner_tol,
+                         int inner_cycles, senk_result *res)
+{
+    return guarded("senk_system_gmres_ir", [&] {
+        SENK_REQUIRE(sys && sys->d, "GMRES-IR needs an FP64 system");
+        senk_result r{};
+        sys->d->gmres_ir(nrm_b, max_outer, m, epsilon, inner_tol, inner_cycles, &r);
+        if (res) *res = r;
+        return r.breakdown ? (int)kErrBreakdown : (int)kOk;
+    });
+}
+
+int senk_abmc_ilu_gmres_ir_d(const double *val, const int *cind, const int *rptr, const double *lval,
+                             const int *lcind, const int *lrptr, const double *uval, const int *ucind,
+                             const int *urptr, const int *cptr, int cnum, int bsize, const double *b, double *x,
+                             double nrm_b, int max_outer, int m, int N, double epsilon, double inner_tol,
+                             int inner_cycles, const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_abmc_ilu_gmres_ir_d", [&] {
+        SENK_REQUIRE(val && cind && rptr && b && x, "null argument");
+        senk_system_desc d{};
+        d.N = N;
+        d.dtype = SENK_F64;
+        d.val = val; d.cind = cind; d.rptr = rptr;
+        d.precond = SENK_PC_ILU_ABMC;
+        d.lval = lval; d.lcind = lcind; d.lrptr = lrptr;
+        d.uval = uval; d.ucind = ucind; d.urptr = urptr;
+        d.cptr = cptr; d.cnum = cnum; d.bsize = bsize;
+        d.mixed = 1;
+        senk_options o{};
+        if (opt) o = *opt;
+        System<double> S;
+        S.create(d, &o);
+        S.b.upload(b, N, S.stream);
+        S.x.upload(x, N, S.stream);
+        senk_result r{};
+        S.gmres_ir(nrm_b, max_outer, m, epsilon, inner_tol, inner_cycles, &r);
+        SENK_CUDA(cudaMemcpyAsync(x, S.x.p, sizeof(double) * N, cudaMemcpyDeviceToHost, S.stream));
+        SENK_CUDA(cudaStreamSynchronize(S.stream));
+        r.h2d_bytes = S.h2d_bytes + 2LL * sizeof(double) * N;
+        r.d2h_bytes = (long long)sizeof(double) * N;
+        if (res) *res = r;
+        return r.breakdown ? (int)kErrBreakdown : (int)kOk;
     });
 }
 

@@ -19,7 +19,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_BREAKDOWN, ERR_ZERO_PIVOT = range(6)
 ORTH_CGS, ORTH_CGS2, ORTH_MGS = 0, 1, 2
 SPMV_AUTO, SPMV_CSR, SPMV_SELL = 0, 1, 2
 PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC = 0, 1, 2, 3
-OP_SPMV, OP_PRECOND, OP_SWEEP_L, OP_SWEEP_U, OP_DOT = 0, 1, 2, 3, 4
+OP_SPMV, OP_PRECOND, OP_SWEEP_L, OP_SWEEP_U, OP_DOT, OP_INNER = 0, 1, 2, 3, 4, 16
 F64, F32 = 0, 1
 
 _P = C.c_void_p
@@ -50,7 +50,7 @@ class Options(C.Structure):
 class SystemDesc(C.Structure):
     _fields_ = [("N", _I), ("dtype", _I), ("val", _P), ("cind", _P), ("rptr", _P), ("precond", _I),
                 ("lval", _P), ("lcind", _P), ("lrptr", _P), ("uval", _P), ("ucind", _P), ("urptr", _P),
-                ("cptr", _P), ("cnum", _I), ("bsize", _I), ("m_max", _I)]
+                ("cptr", _P), ("cnum", _I), ("bsize", _I), ("m_max", _I), ("mixed", _I)]
 
 
 _lib = None
@@ -96,6 +96,8 @@ def _declare(L):
     d("senk_system_zero_x", [_P])
     d("senk_system_gmres", [_P, _D, _I, _I, _D, Rp])
     d("senk_system_time_op", [_P, _I, _I, C.POINTER(_D), C.POINTER(C.c_longlong)])
+    d("senk_system_gmres_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
+    d("senk_abmc_ilu_gmres_ir_d", [_P] * 10 + [_I, _I, _P, _P, _D, _I, _I, _I, _D, _D, _I, Op, Rp])
     d("senk_dev_spmv_csr_d", [_P, _P, _P, _P, _P, _I, _I, _P])
     d("senk_dev_spmv_csr_s", [_P, _P, _P, _P, _P, _I, _I, _P])
     d("senk_dev_spmv_csr_diag_d", [_P, _P, _P, _P, _P, _P, _I, _P])

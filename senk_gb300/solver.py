@@ -79,12 +79,27 @@ def AbmcIluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr,
     return r
 
 
+def AbmcIluGmresIr(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, bsize, b, x, nrm_b,
+                   max_outer, m, N, epsilon, inner_tol=1e-4, inner_cycles=2, **opt) -> Result:
+    """AbmcIluGmresm's arguments solved by mixed-precision GMRES-IR (FP32 inner
+    solves, FP64 refinement stopping on the FP64 true residual)."""
+    r = Result()
+    keep = [_arr(val, np.float64), _arr(cind, np.int32), _arr(rptr, np.int32), _arr(lval, np.float64),
+            _arr(lcind, np.int32), _arr(lrptr, np.int32), _arr(uval, np.float64), _arr(ucind, np.int32),
+            _arr(urptr, np.int32), _arr(cptr, np.int32)]
+    check("senk_abmc_ilu_gmres_ir_d",
+          lib().senk_abmc_ilu_gmres_ir_d(*[ptr(a) for a in keep], cnum, bsize, ptr(_arr(b, np.float64)), ptr(x), nrm_b,
+                                         max_outer, m, N, epsilon, inner_tol, inner_cycles, C.byref(_opts(**opt)),
+                                         C.byref(r)))
+    return r
+
+
 class System:
     """A device-resident system: A (+ split ILU factors and their schedule) uploaded
     once; b and x live on the device between solves."""
 
     def __init__(self, A: Csr, L: Csr = None, U: Csr = None, precond: int = PC_NONE, cptr=None, cnum: int = 0,
-                 bsize: int = 1, dtype=np.float64, m_max: int = 30, **opt):
+                 bsize: int = 1, dtype=np.float64, m_max: int = 30, mixed: bool = False, **opt):
         self.dtype = np.dtype(dtype)
         T = self.dtype
         self.n = A.n
@@ -104,6 +119,7 @@ class System:
                 d.cptr = ptr(cp)
             d.cnum, d.bsize = cnum, bsize
         d.m_max = m_max
+        d.mixed = int(mixed)
         self._h = C.c_void_p()
         check("senk_system_create", lib().senk_system_create(C.byref(self._h), C.byref(d), C.byref(_opts(**opt))))
         self._keep = None
@@ -143,6 +159,12 @@ class System:
     def gmres(self, nrm_b, outer, m, epsilon) -> Result:
         r = Result()
         check("senk_system_gmres", lib().senk_system_gmres(self._h, nrm_b, outer, m, epsilon, C.byref(r)))
+        return r
+
+    def gmres_ir(self, nrm_b, max_outer, m, epsilon, inner_tol=1e-4, inner_cycles=2) -> Result:
+        r = Result()
+        check("senk_system_gmres_ir", lib().senk_system_gmres_ir(self._h, nrm_b, max_outer, m, epsilon, inner_tol,
+                                                                 inner_cycles, C.byref(r)))
         return r
 
     def close(self):
