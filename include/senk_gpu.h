@@ -73,6 +73,8 @@ typedef struct {
 #define SENK_PC_ILU 1       /* natural order: sweeps run level set by level set */
 #define SENK_PC_ILU_AMC 2   /* AMC order: cptr counts rows, cnum colours */
 #define SENK_PC_ILU_ABMC 3  /* ABMC order: cptr counts blocks of bsize rows */
+#define SENK_PC_ILUB 4      /* BCSR factors (bnl x bnw blocks), natural order */
+#define SENK_PC_ILUB_ABMC 5 /* BCSR factors of an ABMC-ordered system */
 
 /* ======================================================= drop-in solvers ==
  * Host arrays in, x updated in place; one call uploads, solves on the GPU and
@@ -136,6 +138,92 @@ int senk_abmc_ilu_gmres_ir_d(const double *val, const int *cind, const int *rptr
                              int max_outer, int m, int N, double epsilon, double inner_tol,
                              int inner_cycles, const senk_options *opt, senk_result *res);
 
+/* senk::solver::Gmresm<T,bnl,bnw> on a BCSR matrix (include/senk_gmres.hpp:113-117).
+ * Every block entry, zeros included, enters the products as in SpmvBcsr. */
+int senk_bcsr_gmres_d(const double *bval, const int *bcind, const int *brptr,
+                      const double *b, double *x, double nrm_b,
+                      int outer, int m, int N, double epsilon, int bnl, int bnw,
+                      const senk_options *opt, senk_result *res);
+
+/* senk::solver::BjIluGmresm<double> (include/senk_gmres.hpp:487-494): factors of
+ * the block-Jacobi matrix (RemoveOffDiagonal with bnum blocks); a factor entry
+ * that couples two blocks is rejected (SENK_ERR_ARG). */
+int senk_bj_ilu_gmres_d(const double *val, const int *cind, const int *rptr,
+                        const double *lval, const int *lcind, const int *lrptr,
+                        const double *uval, const int *ucind, const int *urptr, int bnum,
+                        const double *b, double *x, double nrm_b,
+                        int outer, int m, int N, double epsilon,
+                        const senk_options *opt, senk_result *res);
+
+/* ILUB preconditioning: the split factors in BCSR form (Csr2Bcsr of the split
+ * L/U of the AllocBlockZero pattern), bnl x bnw blocks; the template arguments
+ * bnl/bnw of the reference are run-time arguments here.
+ * senk::solver::IlubGmresm<T,bnl,bnw> (include/senk_gmres.hpp:582-588) */
+int senk_ilub_gmres_d(const double *val, const int *cind, const int *rptr,
+                      const double *blval, const int *blcind, const int *blrptr,
+                      const double *buval, const int *bucind, const int *burptr,
+                      const double *b, double *x, double nrm_b,
+                      int outer, int m, int N, double epsilon, int bnl, int bnw,
+                      const senk_options *opt, senk_result *res);
+/* senk::solver::AbmcIlubGmresm<T,bnl,bnw> (include/senk_gmres.hpp:679-686) */
+int senk_abmc_ilub_gmres_d(const double *val, const int *cind, const int *rptr,
+                           const double *blval, const int *blcind, const int *blrptr,
+                           const double *buval, const int *bucind, const int *burptr,
+                           const int *cptr, int cnum, int bsize,
+                           const double *b, double *x, double nrm_b,
+                           int outer, int m, int N, double epsilon, int bnl, int bnw,
+                           const senk_options *opt, senk_result *res);
+
+/* senk::solver::Gcrm<double> (include/senk_gcr.hpp:30-34). The residual is
+ * tested at restarts only; res->iters = the i*m of the restart that met it. */
+int senk_gcr_d(const double *val, const int *cind, const int *rptr,
+               const double *b, double *x, double nrm_b,
+               int outer, int m, int N, double epsilon,
+               const senk_options *opt, senk_result *res);
+/* senk::solver::IluGcrm<double> (include/senk_gcr.hpp:93-99) */
+int senk_ilu_gcr_d(const double *val, const int *cind, const int *rptr,
+                   const double *lval, const int *lcind, const int *lrptr,
+                   const double *uval, const int *ucind, const int *urptr,
+                   const double *b, double *x, double nrm_b,
+                   int outer, int m, int N, double epsilon,
+                   const senk_options *opt, senk_result *res);
+/* senk::solver::IlubGcrm<double,bnl,bnw> (include/senk_gcr.hpp:163-169) */
+int senk_ilub_gcr_d(const double *val, const int *cind, const int *rptr,
+                    const double *blval, const int *blcind, const int *blrptr,
+                    const double *buval, const int *bucind, const int *burptr,
+                    const double *b, double *x, double nrm_b,
+                    int outer, int m, int N, double epsilon, int bnl, int bnw,
+                    const senk_options *opt, senk_result *res);
+
+/* senk::solver::Bicgstab<double> (include/senk_bicgstab.hpp:29-33) */
+int senk_bicgstab_d(const double *val, const int *cind, const int *rptr,
+                    const double *b, double *x, double nrm_b,
+                    int max_iter, int N, double epsilon,
+                    const senk_options *opt, senk_result *res);
+/* senk::solver::IluBicgstab<double> (include/senk_bicgstab.hpp:107-113) */
+int senk_ilu_bicgstab_d(const double *val, const int *cind, const int *rptr,
+                        const double *lval, const int *lcind, const int *lrptr,
+                        const double *uval, const int *ucind, const int *urptr,
+                        const double *b, double *x, double nrm_b,
+                        int max_iter, int N, double epsilon,
+                        const senk_options *opt, senk_result *res);
+/* IluBicgstab's arguments plus an ABMC colour schedule for the sweeps (new: the
+ * reference pairs ABMC only with GMRES). */
+int senk_abmc_ilu_bicgstab_d(const double *val, const int *cind, const int *rptr,
+                             const double *lval, const int *lcind, const int *lrptr,
+                             const double *uval, const int *ucind, const int *urptr,
+                             const int *cptr, int cnum, int bsize,
+                             const double *b, double *x, double nrm_b,
+                             int max_iter, int N, double epsilon,
+                             const senk_options *opt, senk_result *res);
+/* senk::solver::IlubBicgstab<double,bnl,bnw> (include/senk_bicgstab.hpp:198-204) */
+int senk_ilub_bicgstab_d(const double *val, const int *cind, const int *rptr,
+                         const double *blval, const int *blcind, const int *blrptr,
+                         const double *buval, const int *bucind, const int *burptr,
+                         const double *b, double *x, double nrm_b,
+                         int max_iter, int N, double epsilon, int bnl, int bnw,
+                         const senk_options *opt, senk_result *res);
+
 /* ================================================ device-resident systems ==
  * Upload once, solve many times (the timed path of the benchmark). */
 typedef struct senk_system senk_system;
@@ -154,6 +242,8 @@ typedef struct {
     int m_max;                 /* largest restart length to be used (<= 63) */
     int mixed;                 /* 1 (SENK_F64 systems): also build the FP32 copies
                                   (A, factors, Krylov basis) used by GMRES-IR */
+    int bnl, bnw;              /* SENK_PC_ILUB*: block shape; l* and u* then hold
+                                  the BCSR factors (bval, bcind, brptr) */
 } senk_system_desc;
 
 int senk_system_create(senk_system **out, const senk_system_desc *desc, const senk_options *opt);
@@ -185,6 +275,15 @@ int senk_system_gmres(senk_system *sys, double nrm_b, int outer, int m, double e
  * iterations, res->cycles outer steps, res->res is the final FP64 true residual. */
 int senk_system_gmres_ir(senk_system *sys, double nrm_b, int max_outer, int m, double epsilon,
                          double inner_tol, int inner_cycles, senk_result *res);
+
+/* Restarted GCR(m) on the resident system (include/senk_gcr.hpp:30-91 /
+ * 93-161): one CUDA graph per restart cycle. */
+int senk_system_gcr(senk_system *sys, double nrm_b, int outer, int m, double epsilon,
+                    senk_result *res);
+/* BiCGStab on the resident system (include/senk_bicgstab.hpp:29-105 / 107-196):
+ * one CUDA graph per iteration, launched a few at a time; res->iters is exact. */
+int senk_system_bicgstab(senk_system *sys, double nrm_b, int max_iter, double epsilon,
+                         senk_result *res);
 
 /* Times `reps` back-to-back runs of one operation of the system's solve path on
  * its stream with CUDA events (after one untimed run). Reports the mean time of
@@ -252,6 +351,14 @@ int senk_ilu_plan_create(senk_ilu_plan **out, int dtype, int N,
                          const void *lval, const int *lcind, const int *lrptr,
                          const void *uval, const int *ucind, const int *urptr,
                          int precond, const int *cptr, int cnum, int bsize);
+/* The same plan for BCSR (ILUB) factors, FP64: SptrsvBcsr_l/_u
+ * (include/senk_sparse.hpp:392-465; with cptr, the ABMC forms 481-581, cptr
+ * counting blocks of bsize rows). The factors are checked against the schedule:
+ * a block row that would read a row the schedule has not finished is rejected. */
+int senk_ilub_plan_create(senk_ilu_plan **out, int N, int bnl, int bnw,
+                          const double *blval, const int *blcind, const int *blrptr,
+                          const double *buval, const int *bucind, const int *burptr,
+                          const int *cptr, int cnum, int bsize);
 /* y = U^-1 L^-1 x (device vectors of the plan's dtype); x == y allowed. */
 int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *stream);
 /* One triangular sweep: y = L^-1 x (upper=0) or y = U^-1 x (upper=1). */
@@ -288,6 +395,8 @@ int senk_setup_alloc_block_zero(double **val, int **cind, int **rptr, int N, int
  * (include/senk_matrix.hpp:450-549 / 551-650) */
 int senk_setup_ilup(double **val, int **cind, int **rptr, int N, int p);
 int senk_setup_alloc_level_zero(double **val, int **cind, int **rptr, int N, int p);
+/* senk::matrix::RemoveOffDiagonal<double> (include/senk_matrix.hpp:668-689) */
+int senk_setup_remove_off_diagonal(double **val, int **cind, int **rptr, int N, int bnum);
 
 #ifdef __cplusplus
 }

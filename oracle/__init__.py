@@ -210,6 +210,21 @@ class _Lib:
         nnz = int(rptr[-1])
         return type(A)(_take(self, pv.value, nnz, np.float64), _take(self, pc.value, nnz, np.int32), rptr)
 
+    def remove_off_diagonal(self, A, bnum):
+        """Keep the bnum diagonal blocks of A (RemoveOffDiagonal); returns a new matrix."""
+        if self.prefix == "oracle_":
+            f = self.fn("remove_off_diagonal", [_P, _P, _P, _I, _I], _I)
+            v, c, r = A.val.astype(np.float64).copy(), _i32(A.cind).copy(), _i32(A.rptr).copy()
+            nnz = f(_ptr(v), _ptr(c), _ptr(r), A.n, bnum)
+            return type(A)(v[:nnz].copy(), c[:nnz].copy(), r)
+        f = self.fn("remove_off_diagonal", [_P, _P, _P, _I, _I], None)
+        v, c, r = self._to_malloc(A)
+        pv, pc, pr = _P(v), _P(c), _P(r)
+        f(C.byref(pv), C.byref(pc), C.byref(pr), A.n, bnum)
+        rptr = _take(self, pr.value, A.n + 1, np.int32)
+        nnz = int(rptr[-1])
+        return type(A)(_take(self, pv.value, nnz, np.float64), _take(self, pc.value, nnz, np.int32), rptr)
+
     def split(self, A, key="L-DU", invDiag=True):
         N = A.n
         pc_ = [_P() for _ in range(7)]
@@ -296,6 +311,25 @@ class Port(_Lib):
     def ilu_apply(self, L, U, x, cptr=None, cnum=0, bsize=0, amc=False, dtype=np.float64):
         t = self.sptrsv(L, x, False, cptr, cnum, bsize, amc, dtype)
         return self.sptrsv(U, t, True, cptr, cnum, bsize, amc, dtype)
+
+    def ilub_sweep(self, F, x, upper, bnl, bnw, cptr=None, cnum=0, bsize=0):
+        """SptrsvBcsr_l/_u on a BCSR factor F = (bval, bcind, brptr); sequential or
+        ABMC (cptr counting blocks of bsize rows)."""
+        bv, bc, br = (np.ascontiguousarray(F[0], np.float64), _i32(F[1]), _i32(F[2]))
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(x.size)
+        side = "u" if upper else "l"
+        if cptr is None:
+            f = self.fn(f"sptrsv_bcsr_{side}_d", [_P, _P, _P, _P, _P, _I, _I, _I])
+            f(_ptr(bv), _ptr(bc), _ptr(br), _ptr(x), _ptr(y), x.size, bnl, bnw)
+        else:
+            f = self.fn(f"sptrsv_bcsr_{side}_abmc_d", [_P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I])
+            f(_ptr(bv), _ptr(bc), _ptr(br), _ptr(x), _ptr(y), x.size, _ptr(_i32(cptr)), cnum, bsize, bnl, bnw)
+        return y
+
+    def ilub_apply(self, Lb, Ub, x, bnl, bnw, cptr=None, cnum=0, bsize=0):
+        t = self.ilub_sweep(Lb, x, False, bnl, bnw, cptr, cnum, bsize)
+        return self.ilub_sweep(Ub, t, True, bnl, bnw, cptr, cnum, bsize)
 
     def dot(self, x, y):
         f = self.fn("dot_d", [_P, _P, _I], _D)
@@ -388,6 +422,25 @@ class Ref(_Lib):
             f = self.fn(f"sptrsv_{side}_abmc_d", [_P, _P, _P, _P, _P, _I, _P, _I, _I])
             f(_ptr(F.val), _ptr(F.cind), _ptr(F.rptr), _ptr(x), _ptr(y), F.n, _ptr(_i32(cptr)), cnum, bsize)
         return y
+
+    def ilub_sweep(self, F, x, upper, bnl, bnw, cptr=None, cnum=0, bsize=0):
+        bv, bc, br = (np.ascontiguousarray(F[0], np.float64), _i32(F[1]), _i32(F[2]))
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(x.size)
+        if cptr is None:
+            f = self.fn("sptrsv_bcsr_d", [_I, _P, _P, _P, _P, _P, _I, _I, _I], _I)
+            rc = f(int(upper), _ptr(bv), _ptr(bc), _ptr(br), _ptr(x), _ptr(y), x.size, bnl, bnw)
+        else:
+            f = self.fn("sptrsv_bcsr_abmc_d", [_I, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I], _I)
+            rc = f(int(upper), _ptr(bv), _ptr(bc), _ptr(br), _ptr(x), _ptr(y), x.size, _ptr(_i32(cptr)), cnum,
+                   bsize, bnl, bnw)
+        if rc != 0:
+            raise ValueError(f"block shape {bnl}x{bnw} not instantiated in the reference shim")
+        return y
+
+    def ilub_apply(self, Lb, Ub, x, bnl, bnw, cptr=None, cnum=0, bsize=0):
+        t = self.ilub_sweep(Lb, x, False, bnl, bnw, cptr, cnum, bsize)
+        return self.ilub_sweep(Ub, t, True, bnl, bnw, cptr, cnum, bsize)
 
     def solve_text(self, name, *args):
         """Call a ref_* solver wrapper; returns the reference's captured stdout."""

@@ -209,7 +209,15 @@ void SFX(oracle_sptrsv_u_bj)(const T *val, const int *cind, const int *rptr,
     }
 }
 
-/* One bnl-row block row of the BCSR lower sweep (senk_sparse.hpp:399-415). */
+/* One bnl-row block row of the BCSR lower sweep (senk_sparse.hpp:399-415).
+ * The reference's row loop is `omp simd` and g++ -O3 builds it from vectors of
+ * two doubles: y[xc + c] is read again for every pair of rows (r, r+1), after
+ * the pairs before have been updated. This differs from a row-by-row loop
+ * (re-read for every row) and from a single read when the block holds a value
+ * on the diagonal: Csr2Bcsr (senk_matrix.hpp:144-211) gives an empty L row the
+ * next row's first entry. The pairwise reading reproduces the reference's
+ * output bit for bit on every block shape it instantiates. */
+#define ORACLE_BCSR_LANES 2
 static void SFX(bcsr_l_row)(const T *bval, const int *bcind, const int *brptr,
                             const T *x, T *y, int i, int bnl, int bnw)
 {
@@ -220,7 +228,11 @@ static void SFX(bcsr_l_row)(const T *bval, const int *bcind, const int *brptr,
         int xc = bcind[blk] * bnw;
         for (int c = 0; c < bnw; c++) {
             int off = blk * bs + c * bnl;
-            for (int r = 0; r < bnl; r++) y[i + r] -= bval[off + r] * y[xc + c];
+            for (int r0 = 0; r0 < bnl; r0 += ORACLE_BCSR_LANES) {
+                const T yc = y[xc + c];
+                const int r1 = r0 + ORACLE_BCSR_LANES < bnl ? r0 + ORACLE_BCSR_LANES : bnl;
+                for (int r = r0; r < r1; r++) y[i + r] -= bval[off + r] * yc;
+            }
         }
     }
 }

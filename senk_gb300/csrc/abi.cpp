@@ -140,4 +140,14 @@ int senk_setup_alloc_level_zero(double **val, int **cind, int **rptr, int N, int
     return SENK_OK;
 }
 
+int senk_setup_remove_off_diagonal(double **val, int **cind, int **rptr, int N, int bnum)
+{
+    if (!val || !cind || !rptr || N <= 0 || bnum <= 0 || N % bnum) {
+        senkgpu::set_last_error("senk_setup_remove_off_diagonal: bad argument");
+        return SENK_ERR_ARG;
+    }
+    senk::matrix::RemoveOffDiagonal<double>(val, cind, rptr, N, bnum);
+    return SENK_OK;
+}
+
 }  // extern "C"

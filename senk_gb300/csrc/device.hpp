@@ -176,6 +176,37 @@ struct IluPlan {
     void check_status(cudaStream_t s) const;
 };
 
+// ILUB: split factors kept in BCSR (bnl x bnw blocks, block-column-major
+// values), swept block row by block row. A chain is a run of consecutive block
+// rows swept in order by one group of lanes (ascending for L, descending for
+// U); chains of one phase run concurrently, phases one after another (L in
+// order, U in reverse). Natural order: one phase holding one chain of every
+// block row. ABMC: one phase per colour, one chain per ABMC block.
+template <typename T>
+struct IlubPlan {
+    int n = 0, bnl = 1, bnw = 1, nbr = 0;
+    DevBuf<T> lval, uval;
+    DevBuf<int> lcind, lrptr, ucind, urptr;
+    DevBuf<int2> chains;               // (first block row, block rows)
+    std::vector<int> phase_chains;     // chain range of each phase
+    long long lblocks = 0, ublocks = 0;
+
+    void build(int N, int bnl, int bnw, const T *blval, const int *blcind, const int *blrptr, const T *buval,
+               const int *bucind, const int *burptr, const int *cptr, int cnum, int bsize, cudaStream_t s);
+    void sweep(bool upper, const T *x, T *y, cudaStream_t s, const int *gate) const;
+    void apply(const T *x, T *y, cudaStream_t s, const int *gate) const
+    {
+        sweep(false, x, y, s, gate);
+        sweep(true, (const T *)y, y, s, gate);
+    }
+    long long apply_bytes() const;
+    long long h2d_bytes() const
+    {
+        return (long long)(lval.bytes() + uval.bytes() + lcind.bytes() + lrptr.bytes() + ucind.bytes() +
+                           urptr.bytes() + chains.bytes());
+    }
+};
+
 // --------------------------------------------------------- Krylov system
 
 template <typename T>
@@ -185,6 +216,11 @@ struct System {
     senk_options opt{};
     SpmvOp<T> A;
     std::unique_ptr<IluPlan<T>> pc;
+    std::unique_ptr<IlubPlan<T>> pcb;  // ILUB (BCSR factors) instead of pc
+    bool has_pc() const { return pc || pcb; }
+    // out = K v (the identity copy when the system has no preconditioner)
+    void precondition(const T *v, T *out, const int *gate);
+    void check_pc() const;
     DevBuf<T> b, x, t;
     // GMRES workspace
     int m_alloc = 0;
@@ -218,6 +254,19 @@ struct System {
     int gmres(double nrm_b, int outer, int m, double eps, senk_result *res);
     void time_op(int op, int reps, double *ms, long long *bytes);
     long long h2d_bytes = 0;         // bytes uploaded by create()
+    // GCR(m): directions p_0..p_m and Kr in P; A p_0..A p_m, r and A K r in AP
+    int gcr_m = -1;
+    DevBuf<T> P, AP;
+    DevBuf<double> dAp;
+    cudaGraphExec_t gcr_cycle = nullptr;
+    long long gcr_nodes = 0;
+    int gcr(double nrm_b, int outer, int m, double eps, senk_result *res);
+    // BiCGStab: r, r*, p, Kp, AKp, s, AKs, Ks (s and AKs adjacent)
+    DevBuf<T> BW;
+    DevBuf<double> hist;             // ||r||/||b|| after each iteration
+    cudaGraphExec_t bicg_step = nullptr;
+    long long bicg_nodes = 0;
+    int bicgstab(double nrm_b, int max_iter, double eps, senk_result *res);
 };
 
 }  // namespace senkgpu
@@ -233,4 +282,5 @@ struct senk_ilu_plan {
     int dtype = SENK_F64;
     std::unique_ptr<senkgpu::IluPlan<double>> d;
     std::unique_ptr<senkgpu::IluPlan<float>> f;
+    std::unique_ptr<senkgpu::IlubPlan<double>> b;  // senk_ilub_plan_create
 };

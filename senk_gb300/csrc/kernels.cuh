@@ -24,6 +24,8 @@ struct KrylovState {
     int done;          // 1 once converged (gates the rest of the cycle)
     int jconv;         // number of basis vectors of the converged cycle
     int breakdown;     // a pivot scalar was zero or not finite
+    int count;         // BiCGStab: iterations completed
+    int maxit;         // BiCGStab: iteration limit (done = 2 when reached)
     int pad;
     double s[8];       // scratch scalars (BiCGStab/GCR coefficients)
 };

@@ -28,6 +28,8 @@ System<T>::~System()
 {
     inner.reset();
     if (cycle) cudaGraphExecDestroy(cycle);
+    if (gcr_cycle) cudaGraphExecDestroy(gcr_cycle);
+    if (bicg_step) cudaGraphExecDestroy(bicg_step);
     if (st_host) cudaFreeHost(st_host);
     if (ir_host) cudaFreeHost(ir_host);
     if (ev0) cudaEventDestroy(ev0);
@@ -51,7 +53,14 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     SENK_CUDA(cudaEventCreate(&ev1));
     SENK_CUDA(cudaMallocHost((void **)&st_host, sizeof(KrylovState)));
     A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream);
-    if (d.precond != SENK_PC_NONE) {
+    if (d.precond == SENK_PC_ILUB || d.precond == SENK_PC_ILUB_ABMC) {
+        SENK_REQUIRE(sizeof(T) == sizeof(double) && !d.mixed, "ILUB systems are FP64 only");
+        SENK_REQUIRE((d.precond == SENK_PC_ILUB_ABMC) == (d.cptr != nullptr),
+                     "SENK_PC_ILUB_ABMC needs cptr; SENK_PC_ILUB takes none");
+        pcb = std::make_unique<IlubPlan<T>>();
+        pcb->build(n, d.bnl, d.bnw, (const T *)d.lval, d.lcind, d.lrptr, (const T *)d.uval, d.ucind, d.urptr, d.cptr,
+                   d.cnum, d.bsize, stream);
+    } else if (d.precond != SENK_PC_NONE) {
         pc = std::make_unique<IluPlan<T>>();
         pc->build(n, (const T *)d.lval, d.lcind, d.lrptr, (const T *)d.uval, d.ucind, d.urptr, d.precond, d.cptr,
                   d.cnum, d.bsize, stream);
@@ -67,6 +76,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     SENK_CUDA(cudaStreamSynchronize(stream));
     h2d_bytes = (long long)(A.val.bytes() + A.cind.bytes() + A.rptr.bytes() + A.sval.bytes() + A.scol.bytes() +
                             A.soff.bytes());
+    if (pcb) h2d_bytes += pcb->h2d_bytes();
     if (pc) {
         for (const SweepFactor<T> *F : {&pc->L, &pc->U})
             h2d_bytes += (long long)(F->val.bytes() + F->col.bytes() + F->dinv.bytes() + F->rowmap.bytes() +
@@ -177,8 +187,8 @@ void System<T>::enqueue_gmres_cycle(int m)
     for (int j = 0; j < m; j++) {
         T *vj = V.p + (long long)j * ld;
         T *w = V.p + (long long)(j + 1) * ld;
-        if (pc) {
-            pc->apply(vj, t.p, stream, gate);
+        if (has_pc()) {
+            precondition(vj, t.p, gate);
             A.apply(t.p, w, stream, gate);
         } else {
             A.apply(vj, w, stream, gate);
@@ -188,9 +198,9 @@ void System<T>::enqueue_gmres_cycle(int m)
     }
     k_gmres_trsv<<<1, 32, 0, stream>>>(st.p, H.p, e.p, y.p, m);
     const int grid = stream_grid(n, kThreads, 8);
-    if (pc) {
+    if (has_pc()) {
         k_gmres_combine<T, true><<<grid, kThreads, 0, stream>>>(V.p, ld, y.p, st.p, x.p, n, m);
-        pc->apply(V.p, t.p, stream, nullptr);
+        precondition(V.p, t.p, nullptr);
         ew<T, 0>(t.p, x.p, nullptr, n, T(1), T(0), nullptr, 1.0, stream, nullptr);
     } else {
         k_gmres_combine<T, false><<<grid, kThreads, 0, stream>>>(V.p, ld, y.p, st.p, x.p, n, m);
@@ -251,7 +261,7 @@ int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *re
     SENK_CUDA(cudaEventSynchronize(ev1));
     float ms = 0;
     SENK_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-    if (pc) pc->check_status(stream);
+    check_pc();
     if (opt.verbose) {
         if (conv) {
             printf("I iter %d\n", iters);
@@ -277,6 +287,7 @@ int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *re
 template <typename T>
 void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
 {
+    SENK_REQUIRE(op == SENK_OP_SPMV || op == SENK_OP_DOT || has_pc(), "system has no preconditioner");
     ensure_gmres(std::max(m_alloc, 1));
     T *v0 = V.p, *v1 = V.p + n;
     const long long vb = sizeof(T);
@@ -284,9 +295,15 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
     auto run = [&]() {
         switch (op) {
         case SENK_OP_SPMV: A.apply(v0, v1, stream, nullptr); break;
-        case SENK_OP_PRECOND: SENK_REQUIRE(pc, "system has no preconditioner"); pc->apply(v0, t.p, stream, nullptr); break;
-        case SENK_OP_SWEEP_L: SENK_REQUIRE(pc, "system has no preconditioner"); pc->sweep(pc->L, v0, t.p, stream, nullptr); break;
-        case SENK_OP_SWEEP_U: SENK_REQUIRE(pc, "system has no preconditioner"); pc->sweep(pc->U, (const T *)t.p, t.p, stream, nullptr); break;
+        case SENK_OP_PRECOND: SENK_REQUIRE(has_pc(), "system has no preconditioner"); precondition(v0, t.p, nullptr); break;
+        case SENK_OP_SWEEP_L:
+            if (pcb) pcb->sweep(false, v0, t.p, stream, nullptr);
+            else pc->sweep(pc->L, v0, t.p, stream, nullptr);
+            break;
+        case SENK_OP_SWEEP_U:
+            if (pcb) pcb->sweep(true, (const T *)t.p, t.p, stream, nullptr);
+            else pc->sweep(pc->U, (const T *)t.p, t.p, stream, nullptr);
+            break;
         case SENK_OP_DOT:
             k_multidot<T, false><<<dim3(kRedCtas, 1), kThreads, 0, stream>>>(v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
             break;
@@ -295,9 +312,15 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
     };
     switch (op) {
     case SENK_OP_SPMV: bytes = (long long)A.nnz * (vb + 4) + 4LL * (n + 1) + 2LL * n * vb; break;
-    case SENK_OP_PRECOND: bytes = pc->apply_bytes(); break;
-    case SENK_OP_SWEEP_L: bytes = pc->L.nnz * (vb + 4) + 2LL * n * vb; break;
-    case SENK_OP_SWEEP_U: bytes = (pc->U.nnz - n) * (vb + 4) + 3LL * n * vb; break;
+    case SENK_OP_PRECOND: bytes = pcb ? pcb->apply_bytes() : pc->apply_bytes(); break;
+    case SENK_OP_SWEEP_L:
+        bytes = pcb ? pcb->lblocks * (pcb->bnl * pcb->bnw * vb + 4) + 4LL * (pcb->nbr + 1) + 2LL * n * vb
+                    : pc->L.nnz * (vb + 4) + 2LL * n * vb;
+        break;
+    case SENK_OP_SWEEP_U:
+        bytes = pcb ? pcb->ublocks * (pcb->bnl * pcb->bnw * vb + 4) + 4LL * (pcb->nbr + 1) + 2LL * n * vb
+                    : (pc->U.nnz - n) * (vb + 4) + 3LL * n * vb;
+        break;
     case SENK_OP_DOT: bytes = 2LL * n * vb; break;
     }
     // deterministic finite inputs

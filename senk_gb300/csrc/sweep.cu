@@ -381,12 +381,28 @@ int senk_ilu_plan_create(senk_ilu_plan **out, int dtype, int N, const void *lval
     });
 }
 
+int senk_ilub_plan_create(senk_ilu_plan **out, int N, int bnl, int bnw, const double *blval, const int *blcind,
+                          const int *blrptr, const double *buval, const int *bucind, const int *burptr,
+                          const int *cptr, int cnum, int bsize)
+{
+    return guarded("senk_ilub_plan_create", [&] {
+        SENK_REQUIRE(out != nullptr, "out is null");
+        auto h = std::make_unique<senk_ilu_plan>();
+        h->dtype = SENK_F64;
+        h->b = std::make_unique<IlubPlan<double>>();
+        h->b->build(N, bnl, bnw, blval, blcind, blrptr, buval, bucind, burptr, cptr, cnum, bsize, nullptr);
+        *out = h.release();
+        return (int)kOk;
+    });
+}
+
 int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *stream)
 {
     return guarded("senk_ilu_plan_apply", [&] {
         SENK_REQUIRE(plan && x && y, "null argument");
         cudaStream_t s = (cudaStream_t)stream;
-        if (plan->d) plan->d->apply((const double *)x, (double *)y, s, nullptr);
+        if (plan->b) plan->b->apply((const double *)x, (double *)y, s, nullptr);
+        else if (plan->d) plan->d->apply((const double *)x, (double *)y, s, nullptr);
         else plan->f->apply((const float *)x, (float *)y, s, nullptr);
         SENK_LAUNCH_CHECK();
         return (int)kOk;
@@ -398,7 +414,8 @@ int senk_ilu_plan_sweep(senk_ilu_plan *plan, int upper, const void *x, void *y, 
     return guarded("senk_ilu_plan_sweep", [&] {
         SENK_REQUIRE(plan && x && y, "null argument");
         cudaStream_t s = (cudaStream_t)stream;
-        if (plan->d) plan->d->sweep(upper ? plan->d->U : plan->d->L, (const double *)x, (double *)y, s, nullptr);
+        if (plan->b) plan->b->sweep(upper != 0, (const double *)x, (double *)y, s, nullptr);
+        else if (plan->d) plan->d->sweep(upper ? plan->d->U : plan->d->L, (const double *)x, (double *)y, s, nullptr);
         else plan->f->sweep(upper ? plan->f->U : plan->f->L, (const float *)x, (float *)y, s, nullptr);
         return (int)kOk;
     });

@@ -18,7 +18,7 @@ LIB_PATH = _build.LIB
 OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_BREAKDOWN, ERR_ZERO_PIVOT = range(6)
 ORTH_CGS, ORTH_CGS2, ORTH_MGS = 0, 1, 2
 SPMV_AUTO, SPMV_CSR, SPMV_SELL = 0, 1, 2
-PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC = 0, 1, 2, 3
+PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC, PC_ILUB, PC_ILUB_ABMC = 0, 1, 2, 3, 4, 5
 OP_SPMV, OP_PRECOND, OP_SWEEP_L, OP_SWEEP_U, OP_DOT, OP_INNER = 0, 1, 2, 3, 4, 16
 F64, F32 = 0, 1
 
@@ -50,7 +50,7 @@ class Options(C.Structure):
 class SystemDesc(C.Structure):
     _fields_ = [("N", _I), ("dtype", _I), ("val", _P), ("cind", _P), ("rptr", _P), ("precond", _I),
                 ("lval", _P), ("lcind", _P), ("lrptr", _P), ("uval", _P), ("ucind", _P), ("urptr", _P),
-                ("cptr", _P), ("cnum", _I), ("bsize", _I), ("m_max", _I), ("mixed", _I)]
+                ("cptr", _P), ("cnum", _I), ("bsize", _I), ("m_max", _I), ("mixed", _I), ("bnl", _I), ("bnw", _I)]
 
 
 _lib = None
@@ -98,6 +98,21 @@ def _declare(L):
     d("senk_system_time_op", [_P, _I, _I, C.POINTER(_D), C.POINTER(C.c_longlong)])
     d("senk_system_gmres_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
     d("senk_abmc_ilu_gmres_ir_d", [_P] * 10 + [_I, _I, _P, _P, _D, _I, _I, _I, _D, _D, _I, Op, Rp])
+    gd = [_D, _I, _I, _I, _D]
+    d("senk_bcsr_gmres_d", [_P] * 5 + gd + [_I, _I, Op, Rp])
+    d("senk_bj_ilu_gmres_d", [_P] * 9 + [_I, _P, _P] + gd + [Op, Rp])
+    d("senk_ilub_gmres_d", [_P] * 11 + gd + [_I, _I, Op, Rp])
+    d("senk_abmc_ilub_gmres_d", [_P] * 10 + [_I, _I, _P, _P] + gd + [_I, _I, Op, Rp])
+    d("senk_gcr_d", [_P] * 5 + gd + [Op, Rp])
+    d("senk_ilu_gcr_d", [_P] * 11 + gd + [Op, Rp])
+    d("senk_ilub_gcr_d", [_P] * 11 + gd + [_I, _I, Op, Rp])
+    bd = [_D, _I, _I, _D]
+    d("senk_bicgstab_d", [_P] * 5 + bd + [Op, Rp])
+    d("senk_ilu_bicgstab_d", [_P] * 11 + bd + [Op, Rp])
+    d("senk_abmc_ilu_bicgstab_d", [_P] * 10 + [_I, _I, _P, _P] + bd + [Op, Rp])
+    d("senk_ilub_bicgstab_d", [_P] * 11 + bd + [_I, _I, Op, Rp])
+    d("senk_system_gcr", [_P, _D, _I, _I, _D, Rp])
+    d("senk_system_bicgstab", [_P, _D, _I, _D, Rp])
     d("senk_dev_spmv_csr_d", [_P, _P, _P, _P, _P, _I, _I, _P])
     d("senk_dev_spmv_csr_s", [_P, _P, _P, _P, _P, _I, _I, _P])
     d("senk_dev_spmv_csr_diag_d", [_P, _P, _P, _P, _P, _P, _I, _P])
@@ -111,6 +126,7 @@ def _declare(L):
     d("senk_dev_scal_d", [_D, _P, _I, _P])
     d("senk_dev_copy_d", [_P, _P, _I, _P])
     d("senk_ilu_plan_create", [C.POINTER(_P), _I, _I, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I])
+    d("senk_ilub_plan_create", [C.POINTER(_P), _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I, _I])
     d("senk_ilu_plan_apply", [_P, _P, _P, _P])
     d("senk_ilu_plan_sweep", [_P, _I, _P, _P, _P])
     d("senk_ilu_plan_destroy", [_P])
@@ -124,6 +140,7 @@ def _declare(L):
     d("senk_setup_alloc_block_zero", [PP, PP, PP, _I, _I, _I])
     d("senk_setup_ilup", [PP, PP, PP, _I, _I])
     d("senk_setup_alloc_level_zero", [PP, PP, PP, _I, _I])
+    d("senk_setup_remove_off_diagonal", [PP, PP, PP, _I, _I])
 
 
 def check(fn: str, code: int) -> int:

@@ -144,5 +144,14 @@ def AllocLevelZero(A: Csr, p: int) -> Csr:
     return out
 
 
+def RemoveOffDiagonal(A: Csr, bnum: int) -> Csr:
+    """senk::matrix::RemoveOffDiagonal: keep the bnum diagonal blocks of N/bnum
+    rows (input freed here, see Ilup)."""
+    out, olds = _realloc_call("senk_setup_remove_off_diagonal", A, bnum)
+    for q in olds:
+        lib().senk_free(q)
+    return out
+
+
 __all__ = ["Ilu0", "Split", "GetABMCPermutation", "GetAMCPermutation", "Reordering", "Csr2Bcsr",
-           "AllocBlockZero", "Ilup", "AllocLevelZero", "SenkError"]
+           "AllocBlockZero", "Ilup", "AllocLevelZero", "RemoveOffDiagonal", "SenkError"]

@@ -94,6 +94,106 @@ def AbmcIluGmresIr(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr
     return r
 
 
+def _csr_args(T, *arrays):
+    """Contiguous copies: value arrays in T, index arrays in int32 (alternating
+    val/cind/rptr triples)."""
+    out = []
+    for k, a in enumerate(arrays):
+        out.append(_arr(a, T if k % 3 == 0 else np.int32))
+    return out
+
+
+def _call(fn, *args):
+    r = Result()
+    check(fn, getattr(lib(), fn)(*args, C.byref(r)))
+    return r
+
+
+def BcsrGmresm(bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, **opt) -> Result:
+    """senk::solver::Gmresm<double,bnl,bnw> (include/senk_gmres.hpp:113-195)."""
+    k = _csr_args(np.float64, bval, bcind, brptr)
+    return _call("senk_bcsr_gmres_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+                 epsilon, bnl, bnw, C.byref(_opts(**opt)))
+
+
+def BjIluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, bnum, b, x, nrm_b, outer, m, N, epsilon,
+                **opt) -> Result:
+    """senk::solver::BjIluGmresm<double> (include/senk_gmres.hpp:487-580)."""
+    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_bj_ilu_gmres_d", *[ptr(a) for a in k], bnum, ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer,
+                 m, N, epsilon, C.byref(_opts(**opt)))
+
+
+def IlubGmresm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, outer, m, N, epsilon,
+               bnl, bnw, **opt) -> Result:
+    """senk::solver::IlubGmresm<double,bnl,bnw> (include/senk_gmres.hpp:582-677)."""
+    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_ilub_gmres_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+                 epsilon, bnl, bnw, C.byref(_opts(**opt)))
+
+
+def AbmcIlubGmresm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, cptr, cnum, bsize, b, x, nrm_b,
+                   outer, m, N, epsilon, bnl, bnw, **opt) -> Result:
+    """senk::solver::AbmcIlubGmresm<double,bnl,bnw> (include/senk_gmres.hpp:679-776)."""
+    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_abmc_ilub_gmres_d", *[ptr(a) for a in k], ptr(_arr(cptr, np.int32)), cnum, bsize,
+                 ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N, epsilon, bnl, bnw, C.byref(_opts(**opt)))
+
+
+def Gcrm(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, **opt) -> Result:
+    """senk::solver::Gcrm<double> (include/senk_gcr.hpp:30-91)."""
+    k = _csr_args(np.float64, val, cind, rptr)
+    return _call("senk_gcr_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N, epsilon,
+                 C.byref(_opts(**opt)))
+
+
+def IluGcrm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, outer, m, N, epsilon,
+            **opt) -> Result:
+    """senk::solver::IluGcrm<double> (include/senk_gcr.hpp:93-161)."""
+    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_ilu_gcr_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+                 epsilon, C.byref(_opts(**opt)))
+
+
+def IlubGcrm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, outer, m, N, epsilon,
+             bnl, bnw, **opt) -> Result:
+    """senk::solver::IlubGcrm<double,bnl,bnw> (include/senk_gcr.hpp:163-231)."""
+    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_ilub_gcr_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+                 epsilon, bnl, bnw, C.byref(_opts(**opt)))
+
+
+def Bicgstab(val, cind, rptr, b, x, nrm_b, max_iter, N, epsilon, **opt) -> Result:
+    """senk::solver::Bicgstab<double> (include/senk_bicgstab.hpp:29-105)."""
+    k = _csr_args(np.float64, val, cind, rptr)
+    return _call("senk_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter, N,
+                 epsilon, C.byref(_opts(**opt)))
+
+
+def IluBicgstab(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, max_iter, N, epsilon,
+                **opt) -> Result:
+    """senk::solver::IluBicgstab<double> (include/senk_bicgstab.hpp:107-196)."""
+    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_ilu_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter, N,
+                 epsilon, C.byref(_opts(**opt)))
+
+
+def AbmcIluBicgstab(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, bsize, b, x, nrm_b,
+                    max_iter, N, epsilon, **opt) -> Result:
+    """IluBicgstab with the ABMC colour schedule for its sweeps."""
+    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_abmc_ilu_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(cptr, np.int32)), cnum, bsize,
+                 ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter, N, epsilon, C.byref(_opts(**opt)))
+
+
+def IlubBicgstab(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, max_iter, N, epsilon,
+                 bnl, bnw, **opt) -> Result:
+    """senk::solver::IlubBicgstab<double,bnl,bnw> (include/senk_bicgstab.hpp:198-267)."""
+    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_ilub_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter,
+                 N, epsilon, bnl, bnw, C.byref(_opts(**opt)))
+
+
 class System:
     """A device-resident system: A (+ split ILU factors and their schedule) uploaded
     once; b and x live on the device between solves."""
@@ -165,6 +265,16 @@ class System:
         r = Result()
         check("senk_system_gmres_ir", lib().senk_system_gmres_ir(self._h, nrm_b, max_outer, m, epsilon, inner_tol,
                                                                  inner_cycles, C.byref(r)))
+        return r
+
+    def gcr(self, nrm_b, outer, m, epsilon) -> Result:
+        r = Result()
+        check("senk_system_gcr", lib().senk_system_gcr(self._h, nrm_b, outer, m, epsilon, C.byref(r)))
+        return r
+
+    def bicgstab(self, nrm_b, max_iter, epsilon) -> Result:
+        r = Result()
+        check("senk_system_bicgstab", lib().senk_system_bicgstab(self._h, nrm_b, max_iter, epsilon, C.byref(r)))
         return r
 
     def close(self):

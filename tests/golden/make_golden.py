@@ -97,6 +97,38 @@ def c1_record(R):
                                           10000 // 30, 30, N, 1e-8, 8, 1)
     rec["ilub_8x1"] = {"nnz": Ab.nnz, "pattern_sha": sha(np.concatenate([Ab.rptr, Ab.cind])),
                        "Lb_sha": sha(bl[0]), "Ub_sha": sha(bu[0])}
+    x = np.zeros(N)
+    rec["IlubGcrm_8x1_m20"] = solve_ref(R, "ilub_gcr_d", A.val, A.cind, A.rptr, *bl, *bu, b, x, nb,
+                                        10000 // 20, 20, N, 1e-8, 8, 1)
+    x = np.zeros(N)
+    rec["IlubBicgstab_8x1"] = solve_ref(R, "ilub_bicgstab_d", A.val, A.cind, A.rptr, *bl, *bu, b, x, nb,
+                                        10000, N, 1e-8, 8, 1)
+    # ILUB 2x2: blocks two columns wide
+    Ab2 = R.alloc_block_zero(A, 2, 2)
+    Lb2, Ub2, _ = R.split(R.ilu0(Ab2), "L-DU", True)
+    x = np.zeros(N)
+    rec["IlubGmresm_2x2_m30"] = solve_ref(R, "ilub_gmres_d", A.val, A.cind, A.rptr, *R.csr2bcsr(Lb2, 2, 2),
+                                          *R.csr2bcsr(Ub2, 2, 2), b, x, nb, 10000 // 30, 30, N, 1e-8, 2, 2)
+    # ABMC (bsize 16) + ILUB 8x1 on the reordered system (the reference's main.cpp flow)
+    Abr = R.alloc_block_zero(Ar, 8, 1)
+    Lbr, Ubr, _ = R.split(R.ilu0(Abr), "L-DU", True)
+    x = np.zeros(N)
+    rec["AbmcIlubGmresm_8x1_m30"] = solve_ref(R, "abmc_ilub_gmres_d", Ar.val, Ar.cind, Ar.rptr,
+                                              *R.csr2bcsr(Lbr, 8, 1), *R.csr2bcsr(Ubr, 8, 1), sc, nc, 16,
+                                              br, x, nb, 10000 // 30, 30, N, 1e-8, 8, 1)
+    # block Jacobi, 16 blocks: ILU(0) of RemoveOffDiagonal(A)
+    Aj = R.remove_off_diagonal(A, 16)
+    Lj, Uj, _ = R.split(R.ilu0(Aj), "L-DU", True)
+    x = np.zeros(N)
+    rec["BjIluGmresm_16_m30"] = solve_ref(R, "bj_ilu_gmres_d", A.val, A.cind, A.rptr, Lj.val, Lj.cind, Lj.rptr,
+                                          Uj.val, Uj.cind, Uj.rptr, 16, b, x, nb, 10000 // 30, 30, N, 1e-8)
+    rec["bj16"] = {"nnz": Aj.nnz, "pattern_sha": sha(np.concatenate([Aj.rptr, Aj.cind]))}
+    # unpreconditioned GCR(20) and GMRES(30) on the 2x2 BCSR form of A
+    x = np.zeros(N)
+    rec["Gcrm_m20"] = solve_ref(R, "gcr_d", A.val, A.cind, A.rptr, b, x, nb, 10000 // 20, 20, N, 1e-8)
+    x = np.zeros(N)
+    rec["BcsrGmresm_2x2_m30"] = solve_ref(R, "bcsr_gmres_d", *R.csr2bcsr(A, 2, 2), b, x, nb, 10000 // 30, 30, N,
+                                          1e-8, 2, 2)
     # FP32 ILU-GMRES at 1e-6 (the reference instantiated with T=float)
     Af = A.astype(np.float32)
     xf = np.zeros(N, np.float32)
@@ -131,7 +163,14 @@ def small_arrays(R):
     x2 = np.zeros(N)
     h = solve_ref(R, "ilu_bicgstab_d", Ar.val, Ar.cind, Ar.rptr, L.val, L.cind, L.rptr, U.val, U.cind,
                   U.rptr, b, x2, nb, 1000, N, 1e-8)
-    arrays = dict(A_val=A.val, A_cind=A.cind, A_rptr=A.rptr, LP=LP, RP=RP, size_color=sc,
+    # ILUB 8x1 on the reordered system: BCSR factors and both sweep schedules
+    Lb, Ub, _ = R.split(R.ilu0(R.alloc_block_zero(Ar, 8, 1)), "L-DU", True)
+    bl, bu = R.csr2bcsr(Lb, 8, 1), R.csr2bcsr(Ub, 8, 1)
+    y_ilub_seq = R.ilub_apply(bl, bu, v, 8, 1)
+    y_ilub_abmc = R.ilub_apply(bl, bu, v, 8, 1, sc, nc, 16)
+    ilub = dict(Lb_val=bl[0], Lb_cind=bl[1], Lb_rptr=bl[2], Ub_val=bu[0], Ub_cind=bu[1], Ub_rptr=bu[2],
+                y_ilub_seq=y_ilub_seq, y_ilub_abmc=y_ilub_abmc)
+    arrays = dict(**ilub, A_val=A.val, A_cind=A.cind, A_rptr=A.rptr, LP=LP, RP=RP, size_color=sc,
                   Ar_val=Ar.val, Ar_cind=Ar.cind, Ar_rptr=Ar.rptr, L_val=L.val, L_cind=L.cind,
                   L_rptr=L.rptr, U_val=U.val, U_cind=U.cind, U_rptr=U.rptr, v=v, y_spmv=y_spmv,
                   y_ilu_abmc=y_ilu_abmc, y_ilu_seq=y_ilu_seq, b=b, x_gmres=x, x_bicgstab=x2)

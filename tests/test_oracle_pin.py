@@ -91,6 +91,53 @@ def test_c1_ilub_matches_golden(port, c1, golden):
     assert it == golden["c1"]["IlubGmresm_8x1_m30"]["iters"]
 
 
+def test_c1_ilub_gcr_bicgstab_and_2x2_match_golden(port, c1, golden):
+    A, b = c1
+    L, U, _ = port.split(port.ilu0(port.alloc_block_zero(A, 8, 1)), "L-DU", True)
+    bl, bu = port.csr2bcsr(L, 8, 1), port.csr2bcsr(U, 8, 1)
+    _, it, _, _ = port.solve("gcr", A, b, L=bl, U=bu, pc=oracle.PC_ILUB, bnl=8, bnw=1, outer=10000 // 20, m=20,
+                             eps=1e-8)
+    assert it == golden["c1"]["IlubGcrm_8x1_m20"]["iters"]
+    _, it, _, _ = port.solve("bicgstab", A, b, L=bl, U=bu, pc=oracle.PC_ILUB, bnl=8, bnw=1, max_iter=10000,
+                             eps=1e-8)
+    assert it == golden["c1"]["IlubBicgstab_8x1"]["iters"]
+    L2, U2, _ = port.split(port.ilu0(port.alloc_block_zero(A, 2, 2)), "L-DU", True)
+    _, it, _, _ = port.solve("gmres", A, b, L=port.csr2bcsr(L2, 2, 2), U=port.csr2bcsr(U2, 2, 2),
+                             pc=oracle.PC_ILUB, bnl=2, bnw=2, outer=10000 // 30, m=30, eps=1e-8)
+    assert it == golden["c1"]["IlubGmresm_2x2_m30"]["iters"]
+
+
+def test_c1_abmc_ilub_matches_golden(port, c1, golden):
+    A, b = c1
+    nc, sc, LP, RP = port.abmc_permutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = port.reordering(A, LP, RP)
+    L, U, _ = port.split(port.ilu0(port.alloc_block_zero(Ar, 8, 1)), "L-DU", True)
+    _, it, _, _ = port.solve("gmres", Ar, b[LP], L=port.csr2bcsr(L, 8, 1), U=port.csr2bcsr(U, 8, 1),
+                             pc=oracle.PC_ILUB_ABMC, cptr=sc, cnum=nc, bsize=16, bnl=8, bnw=1, outer=10000 // 30,
+                             m=30, eps=1e-8, nrm_b=float(np.linalg.norm(b)))
+    assert it == golden["c1"]["AbmcIlubGmresm_8x1_m30"]["iters"]
+
+
+def test_c1_block_jacobi_matches_golden(port, c1, golden):
+    A, b = c1
+    Aj = port.remove_off_diagonal(A, 16)
+    g = golden["c1"]["bj16"]
+    assert Aj.nnz == g["nnz"] and sha(np.concatenate([Aj.rptr, Aj.cind])) == g["pattern_sha"]
+    L, U, _ = port.split(port.ilu0(Aj), "L-DU", True)
+    _, it, _, _ = port.solve("gmres", A, b, L=L, U=U, pc=oracle.PC_ILU_BJ, bnum=16, outer=10000 // 30, m=30,
+                             eps=1e-8)
+    assert it == golden["c1"]["BjIluGmresm_16_m30"]["iters"]
+
+
+def test_c1_unpreconditioned_gcr_and_bcsr_gmres_match_golden(port, c1, golden):
+    A, b = c1
+    _, it, _, _ = port.solve("gcr", A, b, pc=oracle.PC_NONE, outer=10000 // 20, m=20, eps=1e-8)
+    assert it == golden["c1"]["Gcrm_m20"]["iters"]
+    _, it, _, _ = port.solve("gmres", port.csr2bcsr(A, 2, 2), b, pc=oracle.PC_NONE, op=oracle.OP_BCSR, bnl=2,
+                             bnw=2, outer=10000 // 30, m=30, eps=1e-8)
+    assert it == golden["c1"]["BcsrGmresm_2x2_m30"]["iters"]
+
+
 def test_c1_float_gmres_matches_golden(port, c1, golden):
     A, b = c1
     L, U, _ = port.split(port.ilu0(A), "L-DU", True)
@@ -171,6 +218,36 @@ def test_live_setup_matches_reference(port, ref):
             if u is not None:
                 assert all(np.array_equal(p, q) for p, q in zip((u.val, u.cind, u.rptr) if hasattr(u, "val") else (u,),
                                                                 (v.val, v.cind, v.rptr) if hasattr(v, "val") else (v,)))
+
+
+def test_small_ilub_sweeps_match_golden(port, small):
+    s = small
+    bl = (s["Lb_val"], s["Lb_cind"], s["Lb_rptr"])
+    bu = (s["Ub_val"], s["Ub_cind"], s["Ub_rptr"])
+    sc = s["size_color"]
+    assert np.array_equal(port.ilub_apply(bl, bu, s["v"], 8, 1), s["y_ilub_seq"])
+    assert np.array_equal(port.ilub_apply(bl, bu, s["v"], 8, 1, sc, len(sc) - 1, 16), s["y_ilub_abmc"])
+    # the first row of the reordered system has no lower entries: Csr2Bcsr gave
+    # it a value on the diagonal, and the sweep must differ from the CSR one
+    assert bl[0][0] != 0.0
+    assert not np.array_equal(s["y_ilub_seq"], s["y_ilu_seq"])
+
+
+@pytest.mark.parametrize("bnl,bnw", [(1, 1), (2, 1), (2, 2), (3, 3), (4, 1), (4, 2), (8, 1), (8, 2)])
+def test_live_ilub_sweeps_match_reference(port, ref, bnl, bnw):
+    A = P.convdiff3d(12, 0.5)  # N = 1728: a multiple of every block shape
+    N = A.n
+    v = np.random.default_rng(3).uniform(-1, 1, N)
+    L, U, _ = port.split(port.ilu0(port.alloc_block_zero(A, bnl, bnw)), "L-DU", True)
+    bl, bu = port.csr2bcsr(L, bnl, bnw), port.csr2bcsr(U, bnl, bnw)
+    assert np.array_equal(port.ilub_apply(bl, bu, v, bnl, bnw), ref.ilub_apply(bl, bu, v, bnl, bnw))
+    bs = 24  # a multiple of every bnl
+    nc, sc, LP, RP = port.abmc_permutation(A.cind, A.rptr, N, bs, False, "connect")
+    Ar = port.reordering(A, LP, RP)
+    L, U, _ = port.split(port.ilu0(port.alloc_block_zero(Ar, bnl, bnw)), "L-DU", True)
+    bl, bu = port.csr2bcsr(L, bnl, bnw), port.csr2bcsr(U, bnl, bnw)
+    assert np.array_equal(port.ilub_apply(bl, bu, v, bnl, bnw, sc, nc, bs),
+                          ref.ilub_apply(bl, bu, v, bnl, bnw, sc, nc, bs))
 
 
 def test_live_solvers_match_reference(port, ref):
