@@ -204,13 +204,17 @@ void IlubPlan<T>::build(int N, int bnl_, int bnw_, const T *blval, const int *bl
     lblocks = blrptr[nbr];
     ublocks = burptr[nbr];
     const size_t bs = (size_t)bnl * bnw;
-    lval.upload(blval, (size_t)lblocks * bs, s);
-    lcind.upload(blcind, (size_t)lblocks, s);
-    lrptr.upload(blrptr, (size_t)nbr + 1, s);
-    uval.upload(buval, (size_t)ublocks * bs, s);
-    ucind.upload(bucind, (size_t)ublocks, s);
-    urptr.upload(burptr, (size_t)nbr + 1, s);
-    chains.upload(ch.data(), ch.size(), s);
+    auto put = [s](auto &buf, const auto *h, size_t count) {
+        buf.alloc(count);
+        buf.upload(h, count, s);
+    };
+    put(lval, blval, (size_t)lblocks * bs);
+    put(lcind, blcind, (size_t)lblocks);
+    put(lrptr, blrptr, (size_t)nbr + 1);
+    put(uval, buval, (size_t)ublocks * bs);
+    put(ucind, bucind, (size_t)ublocks);
+    put(urptr, burptr, (size_t)nbr + 1);
+    put(chains, ch.data(), ch.size());
     SENK_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
 }
 

@@ -146,10 +146,9 @@ def AllocLevelZero(A: Csr, p: int) -> Csr:
 
 def RemoveOffDiagonal(A: Csr, bnum: int) -> Csr:
     """senk::matrix::RemoveOffDiagonal: keep the bnum diagonal blocks of N/bnum
-    rows (input freed here, see Ilup)."""
-    out, olds = _realloc_call("senk_setup_remove_off_diagonal", A, bnum)
-    for q in olds:
-        lib().senk_free(q)
+    rows. It reallocates val and cind and edits rptr in place, so the input
+    buffers are the output's (nothing else to free)."""
+    out, _ = _realloc_call("senk_setup_remove_off_diagonal", A, bnum)
     return out
 
 

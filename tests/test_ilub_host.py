@@ -51,3 +51,12 @@ def test_ilub_plan_rejects_a_u_factor_without_its_diagonal_square():
     bc[br[0]] = bc[br[0] + 1]  # first block of block row 0 no longer the diagonal column 0
     code, msg = _create(bl, (bv, bc, br), A.n, 8, 1)
     assert code == L.ERR_ARG and "diagonal square" in msg
+
+
+def test_remove_off_diagonal_matches_the_oracle(port):
+    A = P.poisson2d(32)
+    a, b = S.RemoveOffDiagonal(A, 8), port.remove_off_diagonal(A, 8)
+    assert np.array_equal(a.rptr, b.rptr) and np.array_equal(a.cind, b.cind) and np.array_equal(a.val, b.val)
+    # twice in a row: the buffers handed back must be owned exactly once
+    a2 = S.RemoveOffDiagonal(a, 16)
+    assert a2.nnz < a.nnz
