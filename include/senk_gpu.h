@@ -15,6 +15,8 @@
 #ifndef SENK_GPU_H
 #define SENK_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -297,6 +299,16 @@ int senk_system_bicgstab(senk_system *sys, double nrm_b, int max_iter, double ep
 #define SENK_OP_INNER 16    /* added to an op: the FP32 copy of a mixed system */
 int senk_system_time_op(senk_system *sys, int op, int reps, double *ms_per_rep, long long *bytes_per_rep);
 
+/* ==================================================== device memory ======
+ * For host code that stages arrays without CUDA headers (the drop-in headers). */
+int senk_mem_alloc(void **p, size_t bytes);
+int senk_mem_free(void *p);
+int senk_mem_h2d(void *dst, const void *src, size_t bytes);  /* synchronous */
+int senk_mem_d2h(void *dst, const void *src, size_t bytes);  /* synchronous */
+int senk_mem_sync(void);
+/* 1: device or managed memory; 0: host memory; < 0: error */
+int senk_mem_is_device(const void *p);
+
 /* ================================================ device kernels (one op) ==
  * Device pointers; stream is a cudaStream_t (NULL = legacy default stream). */
 
@@ -335,6 +347,9 @@ int senk_dev_nrm2_d(const double *x, int N, double *result, void *stream);
  * e.g. on two streams at once, race and give wrong results. */
 int senk_dev_multidot_d_noalloc(const double *V, long long ldv, int nv, const double *w, int N,
                                 double *out, void *stream);
+/* senk::blas1::HadProd / HadDiv (include/senk_blas1.hpp:120-136): y *= x, y /= x */
+int senk_dev_hadprod_d(const double *x, double *y, int N, void *stream);
+int senk_dev_haddiv_d(const double *x, double *y, int N, void *stream);
 /* senk::blas1::Axpy / Axpby / Axpyz / Scal / Copy (include/senk_blas1.hpp:26-83) */
 int senk_dev_axpy_d(double a, const double *x, double *y, int N, void *stream);
 int senk_dev_axpby_d(double a, const double *x, double b, double *y, int N, void *stream);

@@ -1,0 +1,69 @@
+"""The drop-in C++ API: a SenK program written against the reference's headers
+(tests/cpp/driver.cpp) compiles with include/ and links libsenk_gpu.so; on a GPU
+it solves with the reference's iteration counts and stdout lines."""
+import os
+import re
+import subprocess
+
+import pytest
+
+from senk_gb300 import build as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _compile(tmp_path, src, extra=()):
+    exe = str(tmp_path / "driver")
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-Wall", "-Wno-unknown-pragmas", "-I" + os.path.join(ROOT, "include"),
+           src, "-L" + os.path.dirname(B.LIB), "-lsenk_gpu", "-Wl,-rpath," + os.path.dirname(B.LIB), "-o", exe,
+           *extra]
+    return subprocess.run(cmd, capture_output=True, text=True), exe
+
+
+def test_driver_compiles_against_the_dropin_headers(tmp_path):
+    if not os.path.exists(B.LIB):
+        pytest.skip("libsenk_gpu.so not built")
+    r, exe = _compile(tmp_path, os.path.join(ROOT, "tests", "cpp", "driver.cpp"))
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(exe)
+
+
+def test_unsupported_instantiation_fails_at_compile_time(tmp_path):
+    src = tmp_path / "bad.cpp"
+    src.write_text('#include "senk.hpp"\nint main(){float*v=nullptr;int*c=nullptr;'
+                   'senk::solver::Gcrm<float>(v,c,c,v,v,1.f,1,1,1,1e-6f);}\n')
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "the GPU library implements T = double" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_runs_with_the_reference_counts(tmp_path, golden):
+    r, exe = _compile(tmp_path, os.path.join(ROOT, "tests", "cpp", "driver.cpp"))
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    text = out.stdout
+    sections = dict(re.findall(r"^## (\w+)[^\n]*\n(.*?)(?=^## )", text, re.M | re.S))
+    g = golden["c1"]
+
+    def it(name):
+        return int(re.search(r"^I iter (\d+)$", sections[name], re.M).group(1))
+
+    def test_res(name):
+        return float(re.search(r"^# test ([-+0-9.eE]+)$", sections[name], re.M).group(1))
+
+    assert abs(it("IluGmresm") - g["IluGmresm_m30"]["iters"]) <= 2
+    assert abs(it("AbmcIluGmresm") - g["AbmcIluGmresm_m30"]["iters"]) <= 2
+    assert abs(it("IlubGmresm") - g["IlubGmresm_8x1_m30"]["iters"]) <= 2
+    bic = int(re.search(r"^# iter (\d+)$", sections["IluBicgstab"], re.M).group(1))
+    assert abs(bic - g["IluBicgstab"]["iters"]) <= 2
+    gcr = re.findall(r"^(\d+) ([-+0-9.eE]+)$", sections["IluGcrm"], re.M)
+    assert int(gcr[-1][0]) == g["IluGcrm_m20"]["iters"]
+    for name in ("IluGmresm", "AbmcIluGmresm", "IlubGmresm", "IluGcrm"):
+        assert test_res(name) < 1e-8, name
+    assert test_res("IluBicgstab") < 2e-8
+    chk = dict((k, float(v)) for k, v in re.findall(r"(\w+) ([-+0-9.eE]+)", " ".join(
+        re.findall(r"^# check (.*)$", text, re.M))))
+    assert chk["spmv"] == 0.0 and chk["nrm2"] < 1e-14
+    assert chk["sptrsv_l"] <= 1e-12 and chk["sptrsv_u"] <= 1e-12 and chk["dot"] < 1e-13
