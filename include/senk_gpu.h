@@ -380,6 +380,45 @@ int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *strea
 int senk_ilu_plan_sweep(senk_ilu_plan *plan, int upper, const void *x, void *y, void *stream);
 int senk_ilu_plan_destroy(senk_ilu_plan *plan);
 
+/* ============================================= learned preconditioner ==
+ * New (no counterpart in the reference): a message-passing network over the
+ * matrix graph (4 layers, hidden 64; node features a_ii, sum_j |a_ij| and the
+ * residual) whose output corrects the ILU application inside flexible GCR(m):
+ *     K(r) = ILU(r) + (||r||_rms / mean a_ii) * net(r).
+ * Node MLPs run as BF16 tcgen05 GEMMs with FP32 accumulation; aggregation is a
+ * CSR SpMM. Parameters are senk_mpnn_num_params() FP32 values:
+ * W_in[3][64], b_in[64], then per layer Theta[128][64], beta[64], then w_out[64],
+ * b_out. Vectors passed to the functions below are device vectors of the bound
+ * (FP64, ILU-preconditioned) system. */
+typedef struct senk_mpnn senk_mpnn;
+int senk_mpnn_num_params(void);
+int senk_mpnn_create(senk_mpnn **out, const float *params, int nparams);
+int senk_mpnn_destroy(senk_mpnn *net);
+int senk_mpnn_get_params(senk_mpnn *net, float *params, int nparams);
+int senk_mpnn_set_params(senk_mpnn *net, const float *params, int nparams);
+/* Graph data (row-normalised |A| off-diagonal, its transpose, diagonal and row
+ * sums) and activations for the system's matrix. */
+int senk_mpnn_bind(senk_mpnn *net, senk_system *sys);
+/* Loss of one residual/error pair: t = (e - ILU(r)) mean(a_ii) / ||r||_rms,
+ * loss = sum (net(r) - t)^2 / sum t^2; gradient to grad (host, may be NULL). */
+int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const double *e, double *loss,
+                        float *grad);
+/* loss_grad, then one Adam step (beta 0.9 / 0.999, eps 1e-8) with rate lr. */
+int senk_mpnn_train_step(senk_mpnn *net, senk_system *sys, const double *r, const double *e, float lr,
+                         double *loss);
+/* out = K(r) (device vectors). */
+int senk_mpnn_apply(senk_mpnn *net, senk_system *sys, const double *r, double *out);
+/* Use K in the system's GCR (net NULL: plain ILU again). When a restart cycle
+ * reduces the residual by less than `stall`, the solve falls back to plain ILU
+ * for its remaining cycles; senk_system_learned_fallback gives that cycle. */
+int senk_system_set_learned(senk_system *sys, senk_mpnn *net, double stall);
+int senk_system_learned_fallback(senk_system *sys);
+/* The tensor-core products alone, for tests: C = A Bt^T (A n x K, Bt NO x K,
+ * BF16; C FP32; K = 128 with NO = 64, or K = 64 with NO = 128) and
+ * out[128][64] = X^T dZ (X n x 128, dZ n x 64, BF16). */
+int senk_dev_gemm_bf16(const void *A, const void *Bt, float *C, int n, int K, int NO, void *stream);
+int senk_dev_gemm_tn_bf16(const void *X, const void *dZ, float *out, int n, void *stream);
+
 /* ===================================================== host setup (CPU) ==
  * The reference's setup functions, bit-exact, for callers without C++ headers.
  * Outputs are malloc'd; release them with senk_free. */

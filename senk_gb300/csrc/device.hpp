@@ -218,8 +218,17 @@ struct System {
     std::unique_ptr<IluPlan<T>> pc;
     std::unique_ptr<IlubPlan<T>> pcb;  // ILUB (BCSR factors) instead of pc
     bool has_pc() const { return pc || pcb; }
-    // out = K v (the identity copy when the system has no preconditioner)
+    // out = K v: the ILU/ILUB application (the identity copy when the system
+    // has no preconditioner), plus the learned correction when one is attached
     void precondition(const T *v, T *out, const int *gate);
+    void precondition_base(const T *v, T *out, const int *gate);
+    // learned correction (FP64 systems): a bound senk_mpnn, used by GCR; the
+    // GCR falls back to the plain preconditioner when a restart cycle reduces
+    // the residual by less than the factor learned_stall
+    void *learned = nullptr;
+    double learned_stall = 0.9;
+    int learned_fallback = -1;        // restart cycle of the last solve's fall-back (-1: none)
+    bool gcr_learned_in_graph = false;
     void check_pc() const;
     DevBuf<T> b, x, t;
     // GMRES workspace

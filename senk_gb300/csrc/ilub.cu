@@ -258,8 +258,19 @@ long long IlubPlan<T>::apply_bytes() const
 template struct IlubPlan<double>;
 template struct IlubPlan<float>;
 
+void learned_apply(void *net, const void *sys, const double *v, double *out, cudaStream_t s);
+
 template <typename T>
 void System<T>::precondition(const T *v, T *out, const int *gate)
+{
+    precondition_base(v, out, gate);
+    if constexpr (std::is_same<T, double>::value) {
+        if (learned) learned_apply(learned, this, v, out, stream);
+    }
+}
+
+template <typename T>
+void System<T>::precondition_base(const T *v, T *out, const int *gate)
 {
     if (pcb) pcb->apply(v, out, stream, gate);
     else if (pc) pc->apply(v, out, stream, gate);
@@ -277,6 +288,8 @@ void System<T>::check_pc() const
 
 template void System<double>::precondition(const double *, double *, const int *);
 template void System<float>::precondition(const float *, float *, const int *);
+template void System<double>::precondition_base(const double *, double *, const int *);
+template void System<float>::precondition_base(const float *, float *, const int *);
 template void System<double>::check_pc() const;
 template void System<float>::check_pc() const;
 

@@ -223,8 +223,20 @@ int System<T>::gcr(double nrm_b, int outer, int m, double eps, senk_result *res)
     }
     const long long ld = n;
     T *r = AP.p + (long long)(m + 1) * ld, *AKr = AP.p + (long long)(m + 2) * ld, *Kr = P.p + (long long)(m + 1) * ld;
-    if (!gcr_cycle) {
-        gcr_cycle = capture<T>(*this, &gcr_nodes, [&] {
+    // The learned correction (if attached) is part of the captured cycle; after
+    // a fall-back the cycle is captured again without it.
+    void *const attached = learned;
+    learned_fallback = -1;
+    auto recapture_if = [&](bool with_learned) {
+        if (gcr_cycle && gcr_learned_in_graph != with_learned) {
+            cudaGraphExecDestroy(gcr_cycle);
+            gcr_cycle = nullptr;
+        }
+        learned = with_learned ? attached : nullptr;
+        gcr_learned_in_graph = with_learned;
+    };
+    recapture_if(attached != nullptr);
+    const std::function<void()> body = [&] {
             const int *gate = &st.p->done;
             A.residual(x.p, b.p, r, red, &st.p->s[0], nullptr, stream);
             k_gcr_check<<<1, 32, 0, stream>>>(st.p, &st.p->s[0]);
@@ -241,8 +253,8 @@ int System<T>::gcr(double nrm_b, int outer, int m, double eps, senk_result *res)
                 k_gcr_dir<T><<<grid, kThreads, 0, stream>>>(coef.p, dAp.p, j, P.p, AP.p, ld, Kr, AKr, n, gate);
             }
             SENK_LAUNCH_CHECK();
-        });
-    }
+    };
+    if (!gcr_cycle) gcr_cycle = capture<T>(*this, &gcr_nodes, body);
     KrylovState init{};
     init.nrm_b = nrm_b;
     init.eps = eps;
@@ -250,7 +262,7 @@ int System<T>::gcr(double nrm_b, int outer, int m, double eps, senk_result *res)
     SENK_CUDA(cudaMemcpyAsync(st.p, st_host, sizeof(KrylovState), cudaMemcpyHostToDevice, stream));
     SENK_CUDA(cudaEventRecord(ev0, stream));
     int cycles = 0, iters = outer * m, conv = 0;
-    double resid = -1;
+    double resid = -1, prev = -1;
     for (int i = 0; i < outer; i++) {
         SENK_CUDA(cudaGraphLaunch(gcr_cycle, stream));
         SENK_CUDA(cudaMemcpyAsync(st_host, st.p, sizeof(KrylovState), cudaMemcpyDeviceToHost, stream));
@@ -263,7 +275,16 @@ int System<T>::gcr(double nrm_b, int outer, int m, double eps, senk_result *res)
             iters = i * m;
             break;
         }
+        // stagnation of the learned preconditioner: the residual measured at
+        // this restart did not fall below learned_stall times the previous one
+        if (learned && prev > 0 && !(resid < learned_stall * prev)) {
+            learned_fallback = i;
+            recapture_if(false);
+            gcr_cycle = capture<T>(*this, &gcr_nodes, body);
+        }
+        prev = resid;
     }
+    learned = attached;
     SENK_CUDA(cudaEventRecord(ev1, stream));
     SENK_CUDA(cudaEventSynchronize(ev1));
     float ms = 0;

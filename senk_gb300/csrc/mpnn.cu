@@ -1,0 +1,703 @@
+// Learned preconditioner: a message-passing network over the matrix graph whose
+// output corrects the ILU(0) application,
+//     K(r) = ILU(r) + (||r||_rms / d) * net(r),
+// used inside flexible GCR(m). No counterpart in the reference.
+//
+// Network (all node-wise, N nodes = matrix rows, hidden width 64):
+//   features f_i = (a_ii / d, sum_j |a_ij| / d, r_i / ||r||_rms), d = mean a_ii
+//   h0 = relu(f W_in + b_in)                                       (3 -> 64)
+//   layer l = 0..3: m = W h (W_ij = |a_ij| / sum_{k != i} |a_ik|, i != j)
+//                   z = [h, m] Theta_l + beta_l                     (128 -> 64, tcgen05)
+//                   h <- h + relu(z)
+//   c = h w_out + b_out                                            (64 -> 1)
+// Training target for a residual/error pair (r, e): t = (e - ILU(r)) d / ||r||_rms,
+// loss = sum (c - t)^2 / sum t^2. GEMM operands are BF16 with FP32 accumulation;
+// the residual stream, gradients and the Adam state are FP32.
+#include <cmath>
+#include <vector>
+
+#include "device.hpp"
+#include "tc_gemm.cuh"
+
+namespace senkgpu {
+
+namespace {
+
+// Dynamic shared memory of the tensor-core GEMMs. Besides the two tiles it caps
+// the CTAs resident on an SM so that their TMEM accumulators fit in its 512
+// columns: 48 KB -> 4 CTAs x 64 columns; 56 KB -> 4 CTAs x 128 columns.
+constexpr int kSmemFwd = 128 * 128 * 2 + 64 * 128 * 2;  // 48 KB
+constexpr int kSmemDx = 56 * 1024;                      // tiles need 32 KB
+constexpr int kSmemTn = 8 * 1024;                       // + 24 KB static: 7 CTAs x 64 columns
+
+constexpr int kHid = 64;
+constexpr int kLayers = 4;
+constexpr int kIn = 3;
+// parameter vector: W_in[3][64], b_in[64], {Theta_l[128][64], beta_l[64]} x 4, w_out[64], b_out
+constexpr int kOffWin = 0;
+constexpr int kOffBin = kOffWin + kIn * kHid;
+constexpr int kOffLayer = kOffBin + kHid;
+constexpr int kLayerSize = 2 * kHid * kHid + kHid;
+constexpr int kOffWout = kOffLayer + kLayers * kLayerSize;
+constexpr int kOffBout = kOffWout + kHid;
+constexpr int kParams = kOffBout + 1;
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ float relu(float v) { return v > 0.f ? v : 0.f; }
+
+// ||r||_rms and 1/||r||_rms of a double vector (one block per slice, last CTA finishes)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_rms(const T *r, long long n, double *part, unsigned *ticket, float *out)
+{
+    double s = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s += (double)r[i] * (double)r[i];
+    __shared__ double sh[32];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    if (last_cta_arrives(ticket, gridDim.x)) {
+        double t = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += part[i];
+        t = block_sum(t, sh);
+        if (threadIdx.x == 0) {
+            const double rms = sqrt(t / (double)n);
+            out[0] = (float)rms;
+            out[1] = rms > 0 ? (float)(1.0 / rms) : 0.f;
+        }
+    }
+}
+
+// h0 = relu(f W_in + b_in), one thread per (node, feature); X0[:, :64] = bf16(h0)
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_encode(const float *fd, const float *fs, const T *r, const float *rms, const float *P, float *H, bf16 *X, long long n)
+{
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * kHid) return;
+    const long long i = idx / kHid;
+    const int j = (int)(idx % kHid);
+    const float f2 = (float)r[i] * rms[1];
+    const float z = fd[i] * P[kOffWin + j] + fs[i] * P[kOffWin + kHid + j] + f2 * P[kOffWin + 2 * kHid + j] +
+                    P[kOffBin + j];
+    const float h = relu(z);
+    H[idx] = h;
+    X[i * 128 + j] = __float2bfloat16_rn(h);
+}
+
+// m = W h: warp per row, lane l holds features 2l, 2l+1; h = X[:, :64] (bf16),
+// m -> X[:, 64:128] (bf16), FP32 accumulation.
+__global__ void __launch_bounds__(kThreads)
+k_aggregate(const int *rptr, const int *cind, const float *w, bf16 *X, long long n)
+{
+    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    float a0 = 0.f, a1 = 0.f;
+    for (int p = rptr[row]; p < rptr[row + 1]; p++) {
+        const int c = cind[p];
+        const float wv = w[p];
+        const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(X + (long long)c * 128 + 2 * lane);
+        a0 += wv * __bfloat162float(h.x);
+        a1 += wv * __bfloat162float(h.y);
+    }
+    *reinterpret_cast<__nv_bfloat162 *>(X + row * 128 + 64 + 2 * lane) = __floats2bfloat162_rn(a0, a1);
+}
+
+// dH += W^T dM (fp32), warp per row of W^T, lane holds two features
+__global__ void __launch_bounds__(kThreads)
+k_aggregate_back(const int *rptr, const int *cind, const float *w, const float *dM, float *dH, long long n)
+{
+    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    float a0 = 0.f, a1 = 0.f;
+    for (int p = rptr[row]; p < rptr[row + 1]; p++) {
+        const float2 d = *reinterpret_cast<const float2 *>(dM + (long long)cind[p] * 64 + 2 * lane);
+        a0 += w[p] * d.x;
+        a1 += w[p] * d.y;
+    }
+    float2 *o = reinterpret_cast<float2 *>(dH + row * 64 + 2 * lane);
+    float2 v = *o;
+    v.x += a0;
+    v.y += a1;
+    *o = v;
+}
+
+// Inference epilogue: out_i = ilu_i + (rms / d) * (h_i . w_out + b_out); warp per node.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_decode_apply(const float *H, const float *P, const float *rms, float inv_d, T *out, long long n)
+{
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const float2 h = *reinterpret_cast<const float2 *>(H + i * 64 + 2 * lane);
+    float s = h.x * P[kOffWout + 2 * lane] + h.y * P[kOffWout + 2 * lane + 1];
+    s = warp_sum(s);
+    if (lane == 0) out[i] = (T)((double)out[i] + (double)(rms[0] * inv_d) * (double)(s + P[kOffBout]));
+}
+
+// t_i = (e_i - ilu_i) d / rms; sum t^2 -> acc[0] (last CTA)
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_target(const T *e, const T *ilu, const float *rms, float d, float *t, long long n, double *part, unsigned *ticket,
+         double *acc)
+{
+    double s = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float v = (float)(((double)e[i] - (double)ilu[i]) * (double)d * (double)rms[1]);
+        t[i] = v;
+        s += (double)v * v;
+    }
+    __shared__ double sh[32];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+    if (last_cta_arrives(ticket, gridDim.x)) {
+        double u = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) u += part[i];
+        u = block_sum(u, sh);
+        if (threadIdx.x == 0) acc[0] = u;
+    }
+}
+
+// Training decoder: c_i = h_i . w_out + b_out; loss = sum (c - t)^2 / sum t^2;
+// dc = 2 (c - t) / sum t^2; dH4 = dc w_out; grad w_out += dc h; grad b_out += dc.
+// Warp per node; per-CTA partial sums, then atomics. acc[0] = sum t^2, acc[1] += sum (c-t)^2.
+__global__ void __launch_bounds__(kThreads)
+k_decode_train(const float *H, const float *P, const float *t, float *dH, float *G, double *acc, long long n)
+{
+    __shared__ float gw[kThreads / 32][kHid];
+    __shared__ float gb[kThreads / 32];
+    __shared__ double gl[kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const float inv = acc[0] > 0 ? (float)(1.0 / acc[0]) : 0.f;
+    const float w0 = P[kOffWout + 2 * lane], w1 = P[kOffWout + 2 * lane + 1];
+    float g0 = 0.f, g1 = 0.f, gbs = 0.f;
+    double ls = 0;
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const float2 h = *reinterpret_cast<const float2 *>(H + i * 64 + 2 * lane);
+        float c = warp_sum(h.x * w0 + h.y * w1) + P[kOffBout];
+        const float diff = c - t[i];
+        const float dc = 2.f * diff * inv;
+        ls += (double)diff * diff;
+        *reinterpret_cast<float2 *>(dH + i * 64 + 2 * lane) = make_float2(dc * w0, dc * w1);
+        g0 += dc * h.x;
+        g1 += dc * h.y;
+        gbs += dc;
+    }
+    gw[wid][2 * lane] = g0;
+    gw[wid][2 * lane + 1] = g1;
+    if (lane == 0) {
+        gb[wid] = gbs;
+        gl[wid] = ls;
+    }
+    __syncthreads();
+    if (threadIdx.x < kHid) {
+        float s = 0;
+        for (int w = 0; w < kThreads / 32; w++) s += gw[w][threadIdx.x];
+        atomicAdd(G + kOffWout + threadIdx.x, s);
+    }
+    if (threadIdx.x == 0) {
+        float s = 0;
+        double l = 0;
+        for (int w = 0; w < kThreads / 32; w++) {
+            s += gb[w];
+            l += gl[w];
+        }
+        atomicAdd(G + kOffBout, s);
+        atomicAdd(acc + 1, l);
+    }
+}
+
+// dZ = bf16(dH (.) [z > 0]); grad beta += column sums of the FP32 product.
+// Block of 256 threads = 4 nodes x 64 features, grid-stride over nodes.
+__global__ void __launch_bounds__(kThreads)
+k_relu_back(const float *dH, const bf16 *Z, bf16 *dZ, float *gbeta, long long n)
+{
+    const int j = threadIdx.x & 63, sub = threadIdx.x >> 6;
+    float s = 0.f;
+    for (long long i = (long long)blockIdx.x * 4 + sub; i < n; i += (long long)gridDim.x * 4) {
+        const float g = __bfloat162float(Z[i * 64 + j]) > 0.f ? dH[i * 64 + j] : 0.f;
+        dZ[i * 64 + j] = __float2bfloat16_rn(g);
+        s += g;
+    }
+    __shared__ float sh[4][64];
+    sh[sub][j] = s;
+    __syncthreads();
+    if (threadIdx.x < 64) atomicAdd(gbeta + j, sh[0][j] + sh[1][j] + sh[2][j] + sh[3][j]);
+}
+
+// Encoder backward: dz = dH0 (.) [z0 > 0] (z0 recomputed); grad W_in += f dz, grad b_in += dz.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_encode_back(const float *fd, const float *fs, const T *r, const float *rms, const float *P, const float *dH, float *G,
+              long long n)
+{
+    const int j = threadIdx.x & 63, sub = threadIdx.x >> 6;
+    float s0 = 0, s1 = 0, s2 = 0, sb = 0;
+    const float w0 = P[kOffWin + j], w1 = P[kOffWin + kHid + j], w2 = P[kOffWin + 2 * kHid + j], b = P[kOffBin + j];
+    for (long long i = (long long)blockIdx.x * 4 + sub; i < n; i += (long long)gridDim.x * 4) {
+        const float f2 = (float)r[i] * rms[1];
+        const float z = fd[i] * w0 + fs[i] * w1 + f2 * w2 + b;
+        const float g = z > 0.f ? dH[i * 64 + j] : 0.f;
+        s0 += g * fd[i];
+        s1 += g * fs[i];
+        s2 += g * f2;
+        sb += g;
+    }
+    __shared__ float sh[4][4][64];
+    sh[0][sub][j] = s0;
+    sh[1][sub][j] = s1;
+    sh[2][sub][j] = s2;
+    sh[3][sub][j] = sb;
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        float a[4];
+        for (int q = 0; q < 4; q++) a[q] = sh[q][0][j] + sh[q][1][j] + sh[q][2][j] + sh[q][3][j];
+        atomicAdd(G + kOffWin + j, a[0]);
+        atomicAdd(G + kOffWin + kHid + j, a[1]);
+        atomicAdd(G + kOffWin + 2 * kHid + j, a[2]);
+        atomicAdd(G + kOffBin + j, a[3]);
+    }
+}
+
+// Adam (decoupled moments, bias-corrected), then the BF16 weight copies:
+// Theta_l (128 x 64) and its transpose (64 x 128).
+__global__ void __launch_bounds__(kThreads)
+k_adam(float *P, const float *G, float *M, float *V, int np, float lr, float b1, float b2, float eps, float c1,
+       float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const float g = G[i];
+    const float m = b1 * M[i] + (1.f - b1) * g;
+    const float v = b2 * V[i] + (1.f - b2) * g * g;
+    M[i] = m;
+    V[i] = v;
+    P[i] -= lr * (m * c1) / (sqrtf(v * c2) + eps);
+}
+
+__global__ void __launch_bounds__(kThreads) k_weights_bf16(const float *P, bf16 *Wb, bf16 *WTb)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= kLayers * 128 * 64) return;
+    const int l = idx / (128 * 64), e = idx % (128 * 64), i = e / 64, j = e % 64;
+    const bf16 v = __float2bfloat16_rn(P[kOffLayer + l * kLayerSize + e]);
+    Wb[idx] = v;                                  // Theta_l[i][j]
+    WTb[(long long)l * 128 * 64 + j * 128 + i] = v;  // Theta_l^T[j][i]
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ the network
+
+struct Mpnn {
+    // parameters and optimiser state (device, FP32)
+    DevBuf<float> P, G, M, V;
+    DevBuf<bf16> Wb, WTb;  // per layer Theta (128x64) and Theta^T (64x128)
+    int step = 0;
+    // bound graph
+    const void *bound = nullptr;  // the System it was bound to
+    long long n = 0;
+    float d = 1.f;                // mean diagonal
+    DevBuf<int> wr, wc, tr, tcol; // W and W^T (CSR)
+    DevBuf<float> wv, tv, fd, fs;
+    // activations
+    DevBuf<bf16> X[kLayers], Z[kLayers], dZ;
+    DevBuf<float> H[kLayers + 1], dH, dH2, dM, t;
+    DevBuf<float> rms;            // rms, 1/rms
+    DevBuf<double> red, acc;
+    DevBuf<unsigned> ticket;
+    DevBuf<int> status;
+
+    void init(const float *host_params)
+    {
+        P.alloc(kParams);
+        G.alloc(kParams);
+        M.alloc(kParams);
+        V.alloc(kParams);
+        Wb.alloc((size_t)kLayers * 128 * 64);
+        WTb.alloc((size_t)kLayers * 128 * 64);
+        SENK_CUDA(cudaMemcpy(P.p, host_params, sizeof(float) * kParams, cudaMemcpyHostToDevice));
+        SENK_CUDA(cudaMemset(M.p, 0, M.bytes()));
+        SENK_CUDA(cudaMemset(V.p, 0, V.bytes()));
+        status.alloc(1);
+        SENK_CUDA(cudaMemset(status.p, 0, sizeof(int)));
+        rms.alloc(2);
+        red.alloc(kNumSMs * 4);
+        acc.alloc(2);
+        ticket.alloc(1);
+        SENK_CUDA(cudaMemset(ticket.p, 0, sizeof(unsigned)));
+        refresh_weights(nullptr);
+        SENK_CUDA(cudaDeviceSynchronize());
+    }
+
+    void refresh_weights(cudaStream_t s)
+    {
+        k_weights_bf16<<<ceil_div(kLayers * 128 * 64, kThreads), kThreads, 0, s>>>(P.p, Wb.p, WTb.p);
+        SENK_LAUNCH_CHECK();
+    }
+
+    // Graph data of a CSR matrix (host copy): W, W^T, diagonal and |row| sums.
+    void bind_matrix(const double *val, const int *cind, const int *rptr, int N, cudaStream_t s)
+    {
+        std::vector<int> r(N + 1, 0), c, tr_(N + 1, 0), tc_;
+        std::vector<float> w, tw, hd(N), hs(N);
+        double dsum = 0;
+        for (int i = 0; i < N; i++) {
+            double diag = 0, off = 0;
+            for (int p = rptr[i]; p < rptr[i + 1]; p++) {
+                if (cind[p] == i) diag = val[p];
+                else off += std::fabs(val[p]);
+            }
+            hd[i] = (float)diag;
+            hs[i] = (float)(off + std::fabs(diag));
+            dsum += diag;
+            for (int p = rptr[i]; p < rptr[i + 1]; p++) {
+                if (cind[p] == i) continue;
+                c.push_back(cind[p]);
+                w.push_back(off > 0 ? (float)(std::fabs(val[p]) / off) : 0.f);
+                tr_[cind[p] + 1]++;
+            }
+            r[i + 1] = (int)c.size();
+        }
+        d = (float)(dsum / N);
+        SENK_REQUIRE(d > 0, "the learned preconditioner needs a positive mean diagonal");
+        for (int i = 0; i < N; i++) {
+            hd[i] /= d;
+            hs[i] /= d;
+        }
+        for (int i = 0; i < N; i++) tr_[i + 1] += tr_[i];
+        tc_.resize(c.size());
+        tw.resize(c.size());
+        std::vector<int> fill(tr_.begin(), tr_.end() - 1);
+        for (int i = 0; i < N; i++)
+            for (int p = r[i]; p < r[i + 1]; p++) {
+                const int q = fill[c[p]]++;
+                tc_[q] = i;
+                tw[q] = w[p];
+            }
+        auto put = [s](auto &buf, const auto &h) {
+            buf.alloc(h.size());
+            buf.upload(h.data(), h.size(), s);
+        };
+        put(wr, r);
+        put(wc, c);
+        put(wv, w);
+        put(tr, tr_);
+        put(tcol, tc_);
+        put(tv, tw);
+        put(fd, hd);
+        put(fs, hs);
+        if (n != N) {
+            n = N;
+            for (int l = 0; l < kLayers; l++) {
+                X[l].alloc((size_t)N * 128);
+                Z[l].alloc((size_t)N * 64);
+            }
+            for (int l = 0; l <= kLayers; l++) H[l].alloc((size_t)N * 64);
+            dZ.alloc((size_t)N * 64);
+            dH.alloc((size_t)N * 64);
+            dH2.alloc((size_t)N * 64);
+            dM.alloc((size_t)N * 64);
+            t.alloc(N);
+        }
+        SENK_CUDA(cudaStreamSynchronize(s));
+    }
+
+    template <typename T>
+    void forward(const T *r, cudaStream_t s, bool keep_z)
+    {
+        const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
+        k_rms<T><<<rg, kThreads, 0, s>>>(r, n, red.p, ticket.p, rms.p);
+        k_encode<T><<<ceil_div(n * kHid, kThreads), kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, H[0].p, X[0].p, n);
+        const int tiles = ceil_div(n, 128);
+        for (int l = 0; l < kLayers; l++) {
+            k_aggregate<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(wr.p, wc.p, wv.p, X[l].p, n);
+            TcArgs a;
+            a.bias = P.p + kOffLayer + l * kLayerSize + 2 * kHid * kHid;
+            a.hin = H[l].p;
+            a.hout = H[l + 1].p;
+            a.xout = l + 1 < kLayers ? X[l + 1].p : nullptr;  // the last layer's bf16 copy is not read
+            a.xld = 128;
+            a.zout = keep_z ? Z[l].p : nullptr;
+            k_tc_gemm<128, 64, kTcLayerFwd><<<tiles, 128, kSmemFwd, s>>>(
+                X[l].p, 128, WTb.p + (size_t)l * 64 * 128, (int)n, a, status.p);
+        }
+        SENK_LAUNCH_CHECK();
+    }
+
+    // out += (rms / d) * net(r): out already holds ILU(r)
+    template <typename T>
+    void apply(const T *r, T *out, cudaStream_t s)
+    {
+        forward<T>(r, s, false);
+        k_decode_apply<T><<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(H[kLayers].p, P.p, rms.p, 1.f / d, out, n);
+        SENK_LAUNCH_CHECK();
+    }
+
+    // Loss and gradient of one (r, ILU(r), e) triple into G (zeroed first).
+    template <typename T>
+    void loss_grad(const T *r, const T *ilu, const T *e, cudaStream_t s)
+    {
+        SENK_CUDA(cudaMemsetAsync(G.p, 0, G.bytes(), s));
+        SENK_CUDA(cudaMemsetAsync(acc.p, 0, acc.bytes(), s));
+        forward<T>(r, s, true);
+        const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
+        k_target<T><<<rg, kThreads, 0, s>>>(e, ilu, rms.p, d, t.p, n, red.p, ticket.p, acc.p);
+        k_decode_train<<<kNumSMs * 4, kThreads, 0, s>>>(H[kLayers].p, P.p, t.p, dH.p, G.p, acc.p, n);
+        float *dh = dH.p, *dh2 = dH2.p;
+        const int tiles = ceil_div(n, 128);
+        for (int l = kLayers - 1; l >= 0; l--) {
+            float *gl = G.p + kOffLayer + l * kLayerSize;
+            k_relu_back<<<kNumSMs * 8, kThreads, 0, s>>>(dh, Z[l].p, dZ.p, gl + 2 * kHid * kHid, n);
+            k_tc_gemm_tn<64><<<kNumSMs * 2, 128, kSmemTn, s>>>(X[l].p, 128, dZ.p, (int)n, gl, status.p);
+            TcArgs a;
+            a.hin = dh;
+            a.hout = dh2;
+            a.dm = dM.p;
+            k_tc_gemm<64, 128, kTcDx><<<tiles, 128, kSmemDx, s>>>(
+                dZ.p, 64, Wb.p + (size_t)l * 128 * 64, (int)n, a, status.p);
+            k_aggregate_back<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(tr.p, tcol.p, tv.p, dM.p, dh2, n);
+            std::swap(dh, dh2);
+        }
+        k_encode_back<T><<<kNumSMs * 8, kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, dh, G.p, n);
+        SENK_LAUNCH_CHECK();
+    }
+
+    void adam(float lr, cudaStream_t s)
+    {
+        step++;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f / (1.f - std::pow(b1, (float)step)), c2 = 1.f / (1.f - std::pow(b2, (float)step));
+        k_adam<<<ceil_div(kParams, kThreads), kThreads, 0, s>>>(P.p, G.p, M.p, V.p, kParams, lr, b1, b2, 1e-8f, c1, c2);
+        refresh_weights(s);
+    }
+
+    void check_status(cudaStream_t s)
+    {
+        int h = 0;
+        SENK_CUDA(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SENK_CUDA(cudaStreamSynchronize(s));
+        if (h) throw CudaError{cudaErrorLaunchTimeout, "tensor-core MMA completion wait ran out", __FILE__, __LINE__};
+    }
+};
+
+static void set_smem_limits()
+{
+    static bool done = false;
+    if (done) return;
+    SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm<128, 64, kTcLayerFwd>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   kSmemFwd));
+    SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm<128, 64, kTcPlain>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   kSmemFwd));
+    SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm<64, 128, kTcDx>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemDx));
+    SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm<64, 128, kTcPlain>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   kSmemDx));
+    done = true;
+}
+
+// The learned correction hook of System<double>::precondition.
+void learned_apply(void *net, const void *sys, const double *v, double *out, cudaStream_t s)
+{
+    Mpnn *m = static_cast<Mpnn *>(net);
+    SENK_REQUIRE(m->bound == sys, "the network is bound to another system");
+    m->apply<double>(v, out, s);
+}
+
+}  // namespace senkgpu
+
+using namespace senkgpu;
+
+struct senk_mpnn {
+    Mpnn net;
+};
+
+extern "C" {
+
+int senk_mpnn_num_params(void) { return kParams; }
+
+int senk_mpnn_create(senk_mpnn **out, const float *params, int nparams)
+{
+    return guarded("senk_mpnn_create", [&] {
+        SENK_REQUIRE(out && params && nparams == kParams, "params must hold senk_mpnn_num_params() floats");
+        set_smem_limits();
+        auto h = std::make_unique<senk_mpnn>();
+        h->net.init(params);
+        *out = h.release();
+        return (int)kOk;
+    });
+}
+
+int senk_mpnn_destroy(senk_mpnn *net)
+{
+    return guarded("senk_mpnn_destroy", [&] {
+        delete net;
+        return (int)kOk;
+    });
+}
+
+int senk_mpnn_get_params(senk_mpnn *net, float *host, int nparams)
+{
+    return guarded("senk_mpnn_get_params", [&] {
+        SENK_REQUIRE(net && host && nparams == kParams, "bad arguments");
+        SENK_CUDA(cudaDeviceSynchronize());
+        SENK_CUDA(cudaMemcpy(host, net->net.P.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
+        return (int)kOk;
+    });
+}
+
+int senk_mpnn_set_params(senk_mpnn *net, const float *host, int nparams)
+{
+    return guarded("senk_mpnn_set_params", [&] {
+        SENK_REQUIRE(net && host && nparams == kParams, "bad arguments");
+        SENK_CUDA(cudaDeviceSynchronize());
+        SENK_CUDA(cudaMemcpy(net->net.P.p, host, sizeof(float) * kParams, cudaMemcpyHostToDevice));
+        net->net.refresh_weights(nullptr);
+        SENK_CUDA(cudaDeviceSynchronize());
+        return (int)kOk;
+    });
+}
+
+int senk_mpnn_bind(senk_mpnn *net, senk_system *sys)
+{
+    return guarded("senk_mpnn_bind", [&] {
+        SENK_REQUIRE(net && sys && sys->d, "needs an FP64 system");
+        System<double> &S = *sys->d;
+        SENK_REQUIRE(S.has_pc(), "the learned correction needs the system's ILU preconditioner");
+        const int N = S.n, nnz = S.A.nnz;
+        std::vector<double> v(nnz);
+        std::vector<int> c(nnz), r(N + 1);
+        SENK_CUDA(cudaStreamSynchronize(S.stream));
+        SENK_CUDA(cudaMemcpy(v.data(), S.A.val.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
+        SENK_CUDA(cudaMemcpy(c.data(), S.A.cind.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+        SENK_CUDA(cudaMemcpy(r.data(), S.A.rptr.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost));
+        net->net.bind_matrix(v.data(), c.data(), r.data(), N, S.stream);
+        net->net.bound = &S;
+        return (int)kOk;
+    });
+}
+
+// loss of one residual/error pair (device vectors of the bound system); the
+// gradient goes to grad (host, may be NULL) and stays on the device for a step.
+int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const double *e, double *loss,
+                        float *grad)
+{
+    return guarded("senk_mpnn_loss_grad", [&] {
+        SENK_REQUIRE(net && sys && sys->d && r && e, "null argument");
+        System<double> &S = *sys->d;
+        Mpnn &m = net->net;
+        SENK_REQUIRE(m.bound == &S, "bind the network to this system first");
+        S.precondition_base(r, S.t.p, nullptr);  // ILU(r) alone
+        m.loss_grad<double>(r, S.t.p, e, S.stream);
+        double a[2];
+        SENK_CUDA(cudaMemcpyAsync(a, m.acc.p, sizeof(a), cudaMemcpyDeviceToHost, S.stream));
+        if (grad) SENK_CUDA(cudaMemcpyAsync(grad, m.G.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost, S.stream));
+        m.check_status(S.stream);
+        if (loss) *loss = a[0] > 0 ? a[1] / a[0] : 0.0;
+        return (int)kOk;
+    });
+}
+
+int senk_mpnn_train_step(senk_mpnn *net, senk_system *sys, const double *r, const double *e, float lr, double *loss)
+{
+    return guarded("senk_mpnn_train_step", [&] {
+        const int rc = senk_mpnn_loss_grad(net, sys, r, e, loss, nullptr);
+        if (rc != kOk) return rc;
+        net->net.adam(lr, sys->d->stream);
+        return (int)kOk;
+    });
+}
+
+// out = K(r) = ILU(r) + correction, device vectors of the bound system
+int senk_mpnn_apply(senk_mpnn *net, senk_system *sys, const double *r, double *out)
+{
+    return guarded("senk_mpnn_apply", [&] {
+        SENK_REQUIRE(net && sys && sys->d && r && out, "null argument");
+        System<double> &S = *sys->d;
+        SENK_REQUIRE(net->net.bound == &S, "bind the network to this system first");
+        S.precondition_base(r, out, nullptr);
+        net->net.apply<double>(r, out, S.stream);
+        net->net.check_status(S.stream);
+        return (int)kOk;
+    });
+}
+
+// Attach a bound network to the system's GCR as K(r) = ILU(r) + correction
+// (net NULL: detach). stall: the GCR falls back to plain ILU for the rest of a
+// solve once a restart cycle reduces the residual by less than this factor.
+int senk_system_set_learned(senk_system *sys, senk_mpnn *net, double stall)
+{
+    return guarded("senk_system_set_learned", [&] {
+        SENK_REQUIRE(sys && sys->d, "needs an FP64 system");
+        SENK_REQUIRE(stall > 0 && stall <= 1, "stall must be in (0, 1]");
+        if (net) SENK_REQUIRE(net->net.bound == sys->d.get(), "bind the network to this system first");
+        sys->d->learned = net ? &net->net : nullptr;
+        sys->d->learned_stall = stall;
+        return (int)kOk;
+    });
+}
+
+// Restart cycle at which the last GCR solve fell back to plain ILU (-1: never).
+int senk_system_learned_fallback(senk_system *sys) { return sys && sys->d ? sys->d->learned_fallback : -1; }
+
+// C (n x NO, fp32) = A (n x K, bf16) * Bt (NO x K, bf16)^T, for tests of the
+// tensor-core path. K in {64, 128}, NO in {64, 128} (K = 128 needs NO = 64).
+int senk_dev_gemm_bf16(const void *A, const void *Bt, float *C, int n, int K, int NO, void *stream)
+{
+    return guarded("senk_dev_gemm_bf16", [&] {
+        SENK_REQUIRE(A && Bt && C && n > 0, "null argument");
+        SENK_REQUIRE(((uintptr_t)A & 15) == 0 && ((uintptr_t)Bt & 15) == 0, "operands must be 16-byte aligned");
+        set_smem_limits();
+        static DevBuf<int> st;
+        if (!st.p) {
+            st.alloc(1);
+            SENK_CUDA(cudaMemset(st.p, 0, sizeof(int)));
+        }
+        cudaStream_t s = (cudaStream_t)stream;
+        TcArgs a;
+        a.c = C;
+        const int tiles = ceil_div(n, 128);
+        const bf16 *a16 = (const bf16 *)A, *b16 = (const bf16 *)Bt;
+        if (K == 128 && NO == 64)
+            k_tc_gemm<128, 64, kTcPlain><<<tiles, 128, kSmemFwd, s>>>(a16, 128, b16, n, a, st.p);
+        else if (K == 64 && NO == 128)
+            k_tc_gemm<64, 128, kTcPlain><<<tiles, 128, kSmemDx, s>>>(a16, 64, b16, n, a, st.p);
+        else
+            throw ArgError("supported shapes: K=128 NO=64, K=64 NO=128");
+        SENK_LAUNCH_CHECK();
+        int h = 0;
+        SENK_CUDA(cudaMemcpyAsync(&h, st.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SENK_CUDA(cudaStreamSynchronize(s));
+        SENK_REQUIRE(h == 0, "tensor-core MMA completion wait ran out");
+        return (int)kOk;
+    });
+}
+
+// out (128 x 64, fp32) = X^T dZ, X n x 128 and dZ n x 64 (bf16): the weight
+// gradient product, for tests.
+int senk_dev_gemm_tn_bf16(const void *X, const void *dZ, float *out, int n, void *stream)
+{
+    return guarded("senk_dev_gemm_tn_bf16", [&] {
+        SENK_REQUIRE(X && dZ && out && n > 0, "null argument");
+        static DevBuf<int> st;
+        if (!st.p) {
+            st.alloc(1);
+            SENK_CUDA(cudaMemset(st.p, 0, sizeof(int)));
+        }
+        cudaStream_t s = (cudaStream_t)stream;
+        SENK_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * 128 * 64, s));
+        k_tc_gemm_tn<64><<<std::min(ceil_div(n, 64), kNumSMs * 2), 128, kSmemTn, s>>>((const bf16 *)X, 128,
+                                                                                (const bf16 *)dZ, n, out, st.p);
+        SENK_LAUNCH_CHECK();
+        int h = 0;
+        SENK_CUDA(cudaMemcpyAsync(&h, st.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SENK_CUDA(cudaStreamSynchronize(s));
+        SENK_REQUIRE(h == 0, "tensor-core MMA completion wait ran out");
+        return (int)kOk;
+    });
+}
+
+}  // extern "C"

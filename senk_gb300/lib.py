@@ -130,6 +130,27 @@ def _declare(L):
     d("senk_ilu_plan_apply", [_P, _P, _P, _P])
     d("senk_ilu_plan_sweep", [_P, _I, _P, _P, _P])
     d("senk_ilu_plan_destroy", [_P])
+    d("senk_mpnn_num_params", [])
+    d("senk_mpnn_create", [C.POINTER(_P), _P, _I])
+    d("senk_mpnn_destroy", [_P])
+    d("senk_mpnn_get_params", [_P, _P, _I])
+    d("senk_mpnn_set_params", [_P, _P, _I])
+    d("senk_mpnn_bind", [_P, _P])
+    d("senk_mpnn_loss_grad", [_P, _P, _P, _P, C.POINTER(_D), _P])
+    d("senk_mpnn_train_step", [_P, _P, _P, _P, _Fl, C.POINTER(_D)])
+    d("senk_mpnn_apply", [_P, _P, _P, _P])
+    d("senk_system_set_learned", [_P, _P, _D])
+    d("senk_system_learned_fallback", [_P])
+    d("senk_dev_gemm_bf16", [_P, _P, _P, _I, _I, _I, _P])
+    d("senk_dev_gemm_tn_bf16", [_P, _P, _P, _I, _P])
+    d("senk_mem_alloc", [C.POINTER(_P), C.c_size_t])
+    d("senk_mem_free", [_P])
+    d("senk_mem_h2d", [_P, _P, C.c_size_t])
+    d("senk_mem_d2h", [_P, _P, C.c_size_t])
+    d("senk_mem_sync", [])
+    d("senk_mem_is_device", [_P])
+    d("senk_dev_hadprod_d", [_P, _P, _I, _P])
+    d("senk_dev_haddiv_d", [_P, _P, _I, _P])
     PP = C.POINTER(_P)
     d("senk_setup_ilu0", [_P, _P, _P, _I])
     d("senk_setup_split", [_P, _P, _P, PP, PP, PP, PP, PP, PP, PP, _I, C.c_char_p, _I])

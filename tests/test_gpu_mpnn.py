@@ -1,0 +1,135 @@
+"""The learned preconditioner on the GPU: the tcgen05 BF16 GEMMs against a plain
+PyTorch FP32 product of the same BF16 inputs, the network's output, loss and
+gradient against the CPU oracle (oracle/mpnn.py, BF16 rounding points
+reproduced), training, and flexible GCR with K = ILU + net."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mpnn as M
+from senk_gb300 import learned as LN
+from senk_gb300 import lib as L
+from senk_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return torch
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("n,K,NO", [(1000, 128, 64), (4096, 128, 64), (1000, 64, 128), (257, 64, 128)])
+def test_tc_gemm_matches_fp32_product(torch, n, K, NO):
+    g = torch.Generator(device="cuda").manual_seed(n + K)
+    A = torch.randn(n, K, device="cuda", generator=g).to(torch.bfloat16).contiguous()
+    Bt = torch.randn(NO, K, device="cuda", generator=g).to(torch.bfloat16).contiguous()
+    C = torch.full((n, NO), float("nan"), device="cuda", dtype=torch.float32)
+    L.check("gemm", L.lib().senk_dev_gemm_bf16(A.data_ptr(), Bt.data_ptr(), C.data_ptr(), n, K, NO, None))
+    want = A.float() @ Bt.float().T
+    torch.cuda.synchronize()
+    err = (C - want).abs().max().item() / want.abs().max().item()
+    assert err <= 1e-5, err
+
+
+@pytest.mark.parametrize("n", [64, 1000, 70000])
+def test_tc_gemm_tn_matches_fp32_product(torch, n):
+    g = torch.Generator(device="cuda").manual_seed(n)
+    X = torch.randn(n, 128, device="cuda", generator=g).to(torch.bfloat16).contiguous()
+    dZ = torch.randn(n, 64, device="cuda", generator=g).to(torch.bfloat16).contiguous()
+    out = torch.full((128, 64), float("nan"), device="cuda", dtype=torch.float32)
+    L.check("gemm_tn", L.lib().senk_dev_gemm_tn_bf16(X.data_ptr(), dZ.data_ptr(), out.data_ptr(), n, None))
+    want = X.float().T @ dZ.float()
+    torch.cuda.synchronize()
+    err = (out - want).abs().max().item() / want.abs().max().item()
+    assert err <= 1e-5, err
+
+
+@pytest.fixture(scope="module")
+def small_member():
+    return LN.family_member(16, 11)
+
+
+def _trained_like_params(seed=3):
+    p = M.init_params(seed)
+    rng = np.random.default_rng(seed)
+    p[M.OFF_WOUT:M.OFF_BOUT] = rng.normal(0, 0.1, M.HID)
+    p[M.OFF_BOUT] = 0.01
+    return p
+
+
+def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
+    mb = small_member
+    sysm = LN.make_system(mb)
+    params = _trained_like_params()
+    net = LN.Net(params)
+    try:
+        net.bind(sysm)
+        rng = np.random.default_rng(5)
+        r = rng.standard_normal(mb.A.n)
+        e = rng.standard_normal(mb.A.n) * 0.05
+        rd, ed = LN._dev(torch, r), LN._dev(torch, e)
+        out = torch.zeros_like(rd)
+        net.apply(sysm, rd.data_ptr(), out.data_ptr())
+        import oracle
+        port = oracle.port()
+        ilu_h = port.ilu_apply(mb.L, mb.U, r, mb.cptr, mb.cnum, 16)
+        g = M.Graph(mb.A.val, mb.A.cind, mb.A.rptr)
+        want = M.apply(params, g, r, ilu_h, rounding=True)
+        got = out.cpu().numpy()
+        corr_got, corr_want = got - ilu_h, want - ilu_h
+        assert rel(corr_got, corr_want) <= 1e-2
+        assert rel(got, want) <= 1e-3
+        loss, grad = net.loss_grad(sysm, rd.data_ptr(), ed.data_ptr())
+        lw, gw = M.loss_grad(params, g, r, ilu_h, e, rounding=True)
+        assert abs(loss - lw) <= 1e-3 * lw
+        for lo, hi in [(M.OFF_WIN, M.OFF_LAYER)] + [
+                (M.OFF_LAYER + l * M.LAYER_SIZE, M.OFF_LAYER + (l + 1) * M.LAYER_SIZE) for l in range(M.LAYERS)] + [
+                (M.OFF_WOUT, M.NPARAMS)]:
+            assert rel(grad[lo:hi], gw[lo:hi]) <= 2e-2, (lo, hi, rel(grad[lo:hi], gw[lo:hi]))
+    finally:
+        net.close()
+        sysm.close()
+
+
+def test_training_lowers_the_loss_and_flexible_gcr_converges(torch):
+    net = LN.Net(seed=0)
+    try:
+        losses = LN.train(torch, net, 16, seeds=range(100, 116), epochs=3, lr=2e-3)
+        first, last = np.mean(losses[:8]), np.mean(losses[-8:])
+        assert np.isfinite(last) and last < first
+        res = {}
+        for s in (900, 901):
+            mb = LN.family_member(16, s)
+            c = LN.compare_gcr(net, mb, m=20)
+            assert c["plain"]["converged"] and c["plain"]["true_res"] < 1e-8
+            assert c["learned"]["converged"] and c["learned"]["true_res"] < 1e-8
+            res[s] = c
+        out = os.path.join(os.environ.get("GRAFT_REPO_ROOT", "."), "gpurun_out")
+        if os.path.isdir(out):
+            with open(os.path.join(out, "learned_gcr16.json"), "w") as f:
+                json.dump(dict(loss_first=first, loss_last=last, results=res), f, indent=1)
+    finally:
+        net.close()
+
+
+def test_stagnating_network_falls_back_to_plain_ilu(torch):
+    mb = LN.family_member(16, 902)
+    p = M.init_params(1)
+    p[M.OFF_WOUT:M.OFF_BOUT] = 50.0  # a large, useless correction
+    net = LN.Net(p)
+    try:
+        c = LN.compare_gcr(net, mb, m=20, stall=0.9)
+        assert c["learned"]["converged"] and c["learned"]["true_res"] < 1e-8
+        assert c["learned"]["fallback_cycle"] >= 1
+    finally:
+        net.close()

@@ -1,0 +1,56 @@
+"""The network oracle (oracle/mpnn.py) against itself: its hand-derived backward
+pass agrees with finite differences of its forward pass (plain float64), and the
+BF16-rounded variant stays close to the plain one."""
+import numpy as np
+
+from oracle import mpnn as M
+from senk_gb300 import problems as P
+
+
+def _case(seed=0):
+    A = P.vardiff3d(8, 1.0, 3.0, seed)
+    g = M.Graph(A.val, A.cind, A.rptr)
+    rng = np.random.default_rng(seed + 1)
+    r = rng.standard_normal(A.n)
+    ilu = rng.standard_normal(A.n) * 0.1
+    e = ilu + rng.standard_normal(A.n) * 0.05
+    params = M.init_params(seed).astype(np.float64)
+    params[M.OFF_WOUT:M.OFF_BOUT] = rng.normal(0, 0.1, M.HID)  # let gradients reach every layer
+    params[M.OFF_BOUT] = 0.01
+    return g, r, ilu, e, params
+
+
+def test_backward_matches_finite_differences():
+    g, r, ilu, e, params = _case()
+    loss, G = M.loss_grad(params, g, r, ilu, e, rounding=False)
+    rng = np.random.default_rng(7)
+    eps = 1e-6
+    for _ in range(4):
+        v = rng.standard_normal(M.NPARAMS)
+        v /= np.linalg.norm(v)
+        lp, _ = M.loss_grad(params + eps * v, g, r, ilu, e, rounding=False)
+        lm, _ = M.loss_grad(params - eps * v, g, r, ilu, e, rounding=False)
+        fd = (lp - lm) / (2 * eps)
+        assert abs(fd - G @ v) <= 1e-5 * max(1.0, abs(fd))
+    # every parameter block receives gradient
+    for lo, hi in [(M.OFF_WIN, M.OFF_BIN), (M.OFF_LAYER, M.OFF_LAYER + M.LAYER_SIZE),
+                   (M.OFF_LAYER + 3 * M.LAYER_SIZE, M.OFF_WOUT), (M.OFF_WOUT, M.OFF_BOUT)]:
+        assert np.linalg.norm(G[lo:hi]) > 0
+
+
+def test_rounded_network_stays_close():
+    g, r, ilu, e, params = _case(1)
+    a, _ = M.forward(params, g, r, rounding=False)
+    b, _ = M.forward(params, g, r, rounding=True)
+    assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(a)
+    la, Ga = M.loss_grad(params, g, r, ilu, e, rounding=False)
+    lb, Gb = M.loss_grad(params, g, r, ilu, e, rounding=True)
+    assert abs(la - lb) <= 2e-2 * la
+    assert np.linalg.norm(Ga - Gb) <= 5e-2 * np.linalg.norm(Ga)
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.0 + 2**-8, 1.0 + 3 * 2**-8, -2.5, 3.0e-3], np.float64)
+    y = M.bf16(x)
+    assert y[0] == 1.0 and y[1] == 1.0 and y[2] == 1.0 + 2**-6 and y[3] == -2.5
+    assert abs(y[4] - 3.0e-3) <= 3.0e-3 * 2**-8
