@@ -149,11 +149,6 @@ struct SweepFactor {
     std::vector<size_t> colour_smem; // bytes to stage the largest group of each colour
     long long elems = 0;           // padded slots
     long long nnz = 0;             // stored off-diagonal entries (+N for U's diagonal)
-    // Warp-row layout (chains of bs >= 2 rows): a warp group is 32 consecutive
-    // schedule positions of one colour (32 / bs whole chains), one row per lane.
-    bool warp_rows = false;
-    DevBuf<int4> wgroups;           // (pos0, slot offset, we | wi << 8 | rows << 16, 0)
-    std::vector<int> colour_maxslots; // widest warp group (we + wi) of each colour
 };
 
 // A split ILU factorisation with its sweep schedule.

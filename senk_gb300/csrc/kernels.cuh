@@ -642,89 +642,4 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     if (live) y[row] = tsh[l][q];
 }
 
-// Sweep of one colour on the warp-row layout (chains of BS >= 2 rows): one warp
-// per warp group of 32 consecutive schedule positions, lane = row, 32 / BS
-// chains per warp, no block-level barrier. The factor slots are loaded before
-// the kernel waits for the previous colour (programmatic dependent launch);
-// REG keeps up to kSweepRegSlots of them in registers. Per row: the entries of
-// other chains (final before the colour starts) are gathered at once, then the
-// chain's own entries run as a recurrence over the chain's rows in solve order,
-// the earlier rows' values read from their lanes by warp shuffles. The per-row
-// subtraction order is the reference's.
-constexpr int kSweepWarps = 8;      // warps per CTA
-constexpr int kSweepRegSlots = 8;   // slots held in registers when a colour needs at most this many
-
-template <typename VT, typename XT, int BS, bool UPPER, bool REG>
-__global__ void __launch_bounds__(kSweepWarps * 32)
-k_sweep_warp(const int4 *__restrict__ wg, int g_begin, int g_end, const VT *__restrict__ val,
-             const int *__restrict__ col, const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate)
-{
-    static_assert(BS >= 2 && BS <= 32 && (32 % BS) == 0, "chain length must divide 32");
-    const int lane = threadIdx.x & 31;
-    const int g = g_begin + blockIdx.x * kSweepWarps + (threadIdx.x >> 5);
-    const bool have = g < g_end;  // uniform over the warp
-    int4 d = make_int4(0, 0, 0, 0);
-    if (have) d = wg[g];
-    const int we = d.z & 255, wi = (d.z >> 8) & 255, rows = d.z >> 16;
-    const bool live = lane < rows;
-    const int pos = d.x + lane;
-    const long long base = (long long)d.y + lane;
-    VT rv[REG ? kSweepRegSlots : 1];
-    int rc[REG ? kSweepRegSlots : 1];
-    if (REG) {
-#pragma unroll
-        for (int k = 0; k < kSweepRegSlots; k++) {
-            const bool in = have && k < we + wi;
-            rc[k] = in ? ld_stream(col + base + (long long)k * 32) : -1;
-            rv[k] = in ? ld_stream(val + base + (long long)k * 32) : VT(0);
-        }
-    }
-    const XT dg = (UPPER && have && live) ? (XT)__ldg(dinv + pos) : XT(0);
-    pdl_launch_dependents();
-    pdl_wait();  // the previous colour (or the producer of x) has finished
-    if (!have || gated(gate)) return;
-    XT t = live ? x[pos] : XT(0);
-    // entries of other chains
-    if (REG) {
-        XT yv[kSweepRegSlots];
-#pragma unroll
-        for (int k = 0; k < kSweepRegSlots; k++) yv[k] = (k < we && rc[k] >= 0) ? y[rc[k]] : XT(0);
-#pragma unroll
-        for (int k = 0; k < kSweepRegSlots; k++)
-            if (k < we && rc[k] >= 0) t -= (XT)rv[k] * yv[k];
-    } else {
-        for (int k = 0; k < we; k++) {
-            const int c = ld_stream(col + base + (long long)k * 32);
-            const VT v = ld_stream(val + base + (long long)k * 32);
-            if (c >= 0) t -= (XT)v * y[c];
-        }
-    }
-    // the chain's own entries, rows in solve order
-    const int cbase = lane - lane % BS, rin = lane - cbase;
-#pragma unroll
-    for (int step = 0; step < BS; step++) {
-        const int active = UPPER ? BS - 1 - step : step;
-        const bool me = rin == active;
-        if (REG) {
-#pragma unroll
-            for (int q = 0; q < kSweepRegSlots; q++) {
-                if (q >= we && q < we + wi) {  // uniform over the warp
-                    const int c = rc[q];
-                    const XT tv = __shfl_sync(0xffffffffu, t, cbase + (c >= 0 ? c : rin));
-                    if (me && c >= 0) t -= (XT)rv[q] * tv;
-                }
-            }
-        } else {
-            for (int k = 0; k < wi; k++) {
-                const int c = ld_stream(col + base + (long long)(we + k) * 32);
-                const VT v = ld_stream(val + base + (long long)(we + k) * 32);
-                const XT tv = __shfl_sync(0xffffffffu, t, cbase + (c >= 0 ? c : rin));
-                if (me && c >= 0) t -= (XT)v * tv;
-            }
-        }
-        if (UPPER && me) t *= dg;
-    }
-    if (live) y[pos] = t;
-}
-
 }  // namespace senkgpu

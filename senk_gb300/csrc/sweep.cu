@@ -24,87 +24,6 @@ struct Group {
     int p0, p1;  // schedule positions [p0, p1)
 };
 
-// Warp-row layout: per colour, warp groups of 32 consecutive positions (whole
-// chains); in a warp group, slot k of lane l is element (off + k) * 32 + l, slots
-// [0, we) hold entries of other chains (global column), [we, we + wi) entries of
-// the lane's own chain (chain-local row), -1 marks padding. Each part keeps the
-// reference's order (ascending columns for L, descending for U).
-template <typename VT>
-void build_warp_rows(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
-                     const std::vector<Group> &groups, int bs, const std::vector<int> &next,
-                     const std::vector<int> &nint, cudaStream_t s)
-{
-    F.warp_rows = true;
-    std::vector<int4> wg;
-    F.colour_groups.assign(1, 0);
-    F.colour_maxslots.clear();
-    long long off = 0;
-    for (const Group &g : groups) {
-        int maxs = 0;
-        for (int p0 = g.p0; p0 < g.p1; p0 += 32) {
-            const int rows = std::min(32, g.p1 - p0);
-            int we = 0, wi = 0;
-            for (int p = p0; p < p0 + rows; p++) {
-                we = std::max(we, next[p]);
-                wi = std::max(wi, nint[p]);
-            }
-            wg.push_back(make_int4(p0, (int)off, we | (wi << 8) | (rows << 16), 0));
-            off += (long long)(we + wi) * 32;
-            SENK_REQUIRE(off < INT_MAX, "factor too large for 32-bit slot offsets");
-            maxs = std::max(maxs, we + wi);
-        }
-        F.colour_groups.push_back((int)wg.size());
-        F.colour_maxslots.push_back(maxs);
-    }
-    const int ng = (int)wg.size();
-    F.elems = off;
-    std::vector<VT> hv((size_t)std::max<long long>(off, 1), VT(0));
-    std::vector<int> hc((size_t)std::max<long long>(off, 1), -1);
-    std::vector<VT> hd(upper ? N : 0);
-    long long stored = 0;
-#pragma omp parallel for schedule(static) reduction(+ : stored)
-    for (int i = 0; i < ng; i++) {
-        const int4 d = wg[i];
-        const int we = d.z & 255, rows = d.z >> 16;
-        for (int lane = 0; lane < rows; lane++) {
-            const int row = d.x + lane;
-            const int cs = row - row % bs, ce = cs + bs;
-            int ke = 0, ki = 0;
-            auto put = [&](int j) {
-                const int c = cind[j];
-                long long at;
-                if (c >= cs && c < ce) {
-                    at = d.y + (long long)(we + ki++) * 32 + lane;
-                    hc[at] = c - cs;
-                } else {
-                    at = d.y + (long long)(ke++) * 32 + lane;
-                    hc[at] = c;
-                }
-                hv[at] = val[j];
-                stored++;
-            };
-            if (upper) {
-                hd[row] = val[rptr[row]];
-                for (int j = rptr[row + 1] - 1; j >= rptr[row] + 1; j--) put(j);
-            } else {
-                for (int j = rptr[row]; j < rptr[row + 1]; j++) put(j);
-            }
-        }
-    }
-    F.nnz = stored + (upper ? N : 0);
-    F.val.alloc(hv.size());
-    F.val.upload(hv.data(), hv.size(), s);
-    F.col.alloc(hc.size());
-    F.col.upload(hc.data(), hc.size(), s);
-    if (upper) {
-        F.dinv.alloc(N);
-        F.dinv.upload(hd.data(), N, s);
-    }
-    F.wgroups.alloc(std::max(ng, 1));
-    F.wgroups.upload(wg.data(), ng, s);
-    SENK_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
-}
-
 template <typename VT>
 void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
                   const std::vector<Group> &groups, const std::vector<int> *rowmap, int bs,
@@ -144,10 +63,6 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     SENK_REQUIRE(bad < 0, std::string(upper ? "U" : "L") + " factor row " + std::to_string(bad) +
                               " does not fit the schedule (diagonal first in U, strictly triangular, "
                               "columns of other chains in earlier colours, at most 255 entries)");
-    if (chains) {
-        build_warp_rows(F, upper, N, val, cind, rptr, groups, bs, next, nint, s);
-        return;
-    }
     // Groups of up to 32 chains inside each colour, in processing order.
     std::vector<GroupDesc> gd;
     F.colour_groups.assign(1, 0);
@@ -329,56 +244,24 @@ void allow_smem()
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStagedBytes));
 }
 
-template <typename VT, typename XT, int BS, bool UPPER, bool REG>
-void launch_warp_rows(const SweepFactor<VT> &F, int gb, int ge, const XT *x, XT *y, cudaStream_t s, const int *gate)
-{
-    auto kern = k_sweep_warp<VT, XT, BS, UPPER, REG>;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(ceil_div(ge - gb, kSweepWarps));
-    cfg.blockDim = dim3(kSweepWarps * 32);
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    SENK_CUDA(cudaLaunchKernelEx(&cfg, kern, (const int4 *)F.wgroups.p, gb, ge, (const VT *)F.val.p,
-                                 (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate));
-}
-
-template <typename VT, typename XT, int BS, bool UPPER>
-void warp_rows_colour(const SweepFactor<VT> &F, int c, const XT *x, XT *y, cudaStream_t s, const int *gate)
-{
-    const int gb = F.colour_groups[c], ge = F.colour_groups[c + 1];
-    if (ge == gb) return;
-    if (F.colour_maxslots[c] <= kSweepRegSlots) launch_warp_rows<VT, XT, BS, UPPER, true>(F, gb, ge, x, y, s, gate);
-    else launch_warp_rows<VT, XT, BS, UPPER, false>(F, gb, ge, x, y, s, gate);
-}
-
 template <typename VT, typename XT, bool UPPER>
 void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
     const int nc = (int)F.colour_groups.size() - 1;
-    if (F.warp_rows) {
-        for (int c = 0; c < nc; c++) {
-            switch (F.bs) {
-            case 2: warp_rows_colour<VT, XT, 2, UPPER>(F, c, x, y, s, gate); break;
-            case 4: warp_rows_colour<VT, XT, 4, UPPER>(F, c, x, y, s, gate); break;
-            case 8: warp_rows_colour<VT, XT, 8, UPPER>(F, c, x, y, s, gate); break;
-            case 16: warp_rows_colour<VT, XT, 16, UPPER>(F, c, x, y, s, gate); break;
-            case 32: warp_rows_colour<VT, XT, 32, UPPER>(F, c, x, y, s, gate); break;
-            default: throw ArgError("unsupported chain length");
-            }
-        }
-        return;
-    }
     for (int c = 0; c < nc; c++) {
         if (F.mapped) {
             launch_colour<VT, XT, 1, UPPER, true>(F, status, c, x, y, s, gate);
             continue;
         }
-        SENK_REQUIRE(F.bs == 1, "chains of more than one row use the warp-row layout");
-        launch_colour<VT, XT, 1, UPPER, false>(F, status, c, x, y, s, gate);
+        switch (F.bs) {
+        case 1: launch_colour<VT, XT, 1, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 2: launch_colour<VT, XT, 2, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 4: launch_colour<VT, XT, 4, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 8: launch_colour<VT, XT, 8, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 16: launch_colour<VT, XT, 16, UPPER, false>(F, status, c, x, y, s, gate); break;
+        case 32: launch_colour<VT, XT, 32, UPPER, false>(F, status, c, x, y, s, gate); break;
+        default: throw ArgError("unsupported chain length");
+        }
     }
 }
 
@@ -387,6 +270,11 @@ void allow_all_smem()
 {
     allow_smem<VT, XT, 1, false, true>(); allow_smem<VT, XT, 1, true, true>();
     allow_smem<VT, XT, 1, false, false>(); allow_smem<VT, XT, 1, true, false>();
+    allow_smem<VT, XT, 2, false, false>(); allow_smem<VT, XT, 2, true, false>();
+    allow_smem<VT, XT, 4, false, false>(); allow_smem<VT, XT, 4, true, false>();
+    allow_smem<VT, XT, 8, false, false>(); allow_smem<VT, XT, 8, true, false>();
+    allow_smem<VT, XT, 16, false, false>(); allow_smem<VT, XT, 16, true, false>();
+    allow_smem<VT, XT, 32, false, false>(); allow_smem<VT, XT, 32, true, false>();
 }
 
 }  // namespace
