@@ -542,7 +542,6 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
         const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
         const int *__restrict__ rowmap, const XT *x, XT *y, const int *gate, int *status)
 {
-    static_assert(BS == 1 || !MAPPED, "chains are stored in schedule order");
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) unsigned long long bar;
     __shared__ XT tsh[BS][32];    // row l of chain q
@@ -550,9 +549,8 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     __shared__ int wsh[2 * BS];   // we[BS], wi[BS]
     const int g = g_begin + blockIdx.x;
     const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
-    // the widths sit at a fixed stride per group: both loads issue together
-    if (threadIdx.x < 2 * BS) wsh[threadIdx.x] = widths[(size_t)g * 2 * BS + threadIdx.x];
     const GroupDesc d = groups[g];
+    if (threadIdx.x < 2 * BS) wsh[threadIdx.x] = widths[d.widx + threadIdx.x];
     __syncthreads();
     int eo = 0, etot = 0;
 #pragma unroll
@@ -600,25 +598,13 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     const int pos = d.pos0 + q * BS + l;
     const int row = live ? (MAPPED ? __ldg(rowmap + pos) : pos) : 0;
     XT t = live ? x[row] : XT(0);
-    // Phase 1: row l's external entries, four at a time (all gathers of a
-    // batch in flight together; subtraction in slot order).
+    // Phase 1: row l's external entries.
     const int we = wsh[l];
-    for (int k0 = 0; k0 < we; k0 += 4) {
-        int c[4];
-        VT v[4];
-        XT yv[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const bool in = k0 + u < we;
-            const int at = (eo + k0 + u) * 32 + q;
-            c[u] = in ? (STAGED ? cb[at] : ld_stream(cb + at)) : -1;
-            v[u] = in ? (STAGED ? vb[at] : ld_stream(vb + at)) : VT(0);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) yv[u] = c[u] >= 0 ? y[c[u]] : XT(0);
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-            if (c[u] >= 0) t -= (XT)v[u] * yv[u];
+    for (int k = 0; k < we; k++) {
+        const int at = (eo + k) * 32 + q;
+        const int c = STAGED ? cb[at] : ld_stream(cb + at);
+        const VT v = STAGED ? vb[at] : ld_stream(vb + at);
+        if (c >= 0) t -= (XT)v * y[c];
     }
     if (BS == 1) {
         if (UPPER && live) t *= (XT)__ldg(dinv + pos);
@@ -628,8 +614,7 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     tsh[l][q] = t;
     if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
     __syncthreads();
-    // Phase 2: one lane per chain, rows in solve order; warp 0 also writes the
-    // chains' results (the other warps are done).
+    // Phase 2: one lane per chain, rows in solve order.
     if (l == 0) {
         int io = etot;
         int ioff[BS];
@@ -643,31 +628,18 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
             const int r = UPPER ? BS - 1 - s : s;
             XT tt = tsh[r][q];
             const int wi = wsh[BS + r];
-            for (int k0 = 0; k0 < wi; k0 += 4) {
-                int c[4];
-                VT v[4];
-                XT tv[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const bool in = k0 + u < wi;
-                    const int at = (ioff[r] + k0 + u) * 32 + q;
-                    c[u] = in ? cb[at] : -1;
-                    v[u] = in ? vb[at] : VT(0);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; u++) tv[u] = c[u] >= 0 ? tsh[c[u]][q] : XT(0);
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-                    if (c[u] >= 0) tt -= (XT)v[u] * tv[u];
+            for (int k = 0; k < wi; k++) {
+                const int at = (ioff[r] + k) * 32 + q;
+                const int c = cb[at];
+                const VT v = vb[at];
+                if (c >= 0) tt -= (XT)v * tsh[c][q];
             }
             if (UPPER) tt *= dsh[r][q];
             tsh[r][q] = tt;
         }
-        if (live) {
-#pragma unroll
-            for (int r = 0; r < BS; r++) y[d.pos0 + q * BS + r] = tsh[r][q];
-        }
     }
+    __syncthreads();
+    if (live) y[row] = tsh[l][q];
 }
 
 }  // namespace senkgpu
