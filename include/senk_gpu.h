@@ -243,7 +243,9 @@ typedef struct {
     const int *cptr; int cnum; int bsize;                 /* colour schedule */
     int m_max;                 /* largest restart length to be used (<= 63) */
     int mixed;                 /* 1 (SENK_F64 systems): also build the FP32 copies
-                                  (A, factors, Krylov basis) used by GMRES-IR */
+                                  (A, factors, Krylov basis) used by GMRES-IR;
+                                  2: GMRES-IR only: the FP64 part keeps A (SELL)
+                                  for residuals and no preconditioner or basis */
     int bnl, bnw;              /* SENK_PC_ILUB*: block shape; l* and u* then hold
                                   the BCSR factors (bval, bcind, brptr) */
 } senk_system_desc;

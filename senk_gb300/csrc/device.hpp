@@ -114,7 +114,9 @@ struct SpmvOp {
     DevBuf<T> sval;
     DevBuf<int> scol, soff;
 
-    void upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s);
+    // keep_csr = false (with a SELL format): only the SELL copy goes to the device
+    void upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s, bool keep_csr = true);
+    bool has_csr = false;
     // y = A x (MODE 0) or y = b - A x (MODE 1)
     void apply(const T *x, T *y, cudaStream_t s, const int *gate) const;
     // y = b - A x, ||y|| -> *norm_out, 1/||y|| -> *inv_out
@@ -255,7 +257,10 @@ struct System {
     System(const System &) = delete;
     ~System();
     // `shared` (optional): run on this stream instead of creating one.
-    void create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared = nullptr);
+    // sell_only: keep A on the device as SELL only (no CSR copy).
+    void create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared = nullptr,
+                bool sell_only = false);
+    bool ir_only = false;  // desc.mixed == 2: the FP64 part serves GMRES-IR's outer loop only
     int gmres_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
                  senk_result *res);
     void ensure_gmres(int m);

@@ -38,10 +38,12 @@ System<T>::~System()
 }
 
 template <typename T>
-void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared)
+void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared, bool sell_only)
 {
     SENK_REQUIRE(d.N > 0, "N must be positive");
+    SENK_REQUIRE(d.mixed >= 0 && d.mixed <= 2, "mixed must be 0, 1 or 2");
     n = d.N;
+    ir_only = d.mixed == 2;
     if (o) opt = *o;
     if (shared) {
         stream = shared;
@@ -52,8 +54,12 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     SENK_CUDA(cudaEventCreate(&ev0));
     SENK_CUDA(cudaEventCreate(&ev1));
     SENK_CUDA(cudaMallocHost((void **)&st_host, sizeof(KrylovState)));
-    A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream);
-    if (d.precond == SENK_PC_ILUB || d.precond == SENK_PC_ILUB_ABMC) {
+    // GMRES-IR only: the FP64 system computes residuals and updates x; the
+    // preconditioner and the Krylov basis live in the FP32 copy.
+    A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream, !(sell_only || ir_only));
+    if (ir_only) {
+        // nothing to build here for the preconditioner
+    } else if (d.precond == SENK_PC_ILUB || d.precond == SENK_PC_ILUB_ABMC) {
         SENK_REQUIRE(sizeof(T) == sizeof(double) && !d.mixed, "ILUB systems are FP64 only");
         SENK_REQUIRE((d.precond == SENK_PC_ILUB_ABMC) == (d.cptr != nullptr),
                      "SENK_PC_ILUB_ABMC needs cptr; SENK_PC_ILUB takes none");
@@ -72,7 +78,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     SENK_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), stream));
     st.alloc(1);
     red.ensure(stream);
-    if (d.m_max > 0) ensure_gmres(d.m_max);
+    if (d.m_max > 0 && !ir_only) ensure_gmres(d.m_max);
     SENK_CUDA(cudaStreamSynchronize(stream));
     h2d_bytes = (long long)(A.val.bytes() + A.cind.bytes() + A.rptr.bytes() + A.sval.bytes() + A.scol.bytes() +
                             A.soff.bytes());
@@ -105,7 +111,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
             di.uval = u32.data();
         }
         inner = std::make_unique<System<float>>();
-        inner->create(di, &opt, stream);
+        inner->create(di, &opt, stream, ir_only);
         h2d_bytes += inner->h2d_bytes;
         irs.alloc(2);
         SENK_CUDA(cudaMallocHost((void **)&ir_host, 2 * sizeof(double)));
@@ -211,6 +217,7 @@ void System<T>::enqueue_gmres_cycle(int m)
 template <typename T>
 int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *res)
 {
+    SENK_REQUIRE(!ir_only, "this system was created for GMRES-IR only (mixed = 2)");
     SENK_REQUIRE(outer >= 0, "outer must be non-negative");
     ensure_gmres(m);
     const int orth = opt.orth;
@@ -591,7 +598,7 @@ int senk_abmc_ilu_gmres_ir_d(const double *val, const int *cind, const int *rptr
         d.lval = lval; d.lcind = lcind; d.lrptr = lrptr;
         d.uval = uval; d.ucind = ucind; d.urptr = urptr;
         d.cptr = cptr; d.cnum = cnum; d.bsize = bsize;
-        d.mixed = 1;
+        d.mixed = 2;  // the FP64 part only computes residuals and updates
         senk_options o{};
         if (opt) o = *opt;
         System<double> S;

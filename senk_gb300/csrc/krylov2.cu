@@ -211,6 +211,7 @@ cudaGraphExec_t capture(System<T> &S, long long *nodes, const std::function<void
 template <typename T>
 int System<T>::gcr(double nrm_b, int outer, int m, double eps, senk_result *res)
 {
+    SENK_REQUIRE(!ir_only, "this system was created for GMRES-IR only (mixed = 2)");
     SENK_REQUIRE(outer >= 0 && m >= 1 && m <= 62, "GCR restart length m must be in [1, 62]");
     if (gcr_m != m) {
         if (gcr_cycle) cudaGraphExecDestroy(gcr_cycle);
@@ -306,6 +307,7 @@ int System<T>::gcr(double nrm_b, int outer, int m, double eps, senk_result *res)
 template <typename T>
 int System<T>::bicgstab(double nrm_b, int max_iter, double eps, senk_result *res)
 {
+    SENK_REQUIRE(!ir_only, "this system was created for GMRES-IR only (mixed = 2)");
     SENK_REQUIRE(max_iter >= 0, "max_iter must be non-negative");
     const long long ld = n;
     if (!BW.p) {

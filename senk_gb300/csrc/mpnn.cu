@@ -567,6 +567,7 @@ int senk_mpnn_bind(senk_mpnn *net, senk_system *sys)
         SENK_REQUIRE(net && sys && sys->d, "needs an FP64 system");
         System<double> &S = *sys->d;
         SENK_REQUIRE(S.has_pc(), "the learned correction needs the system's ILU preconditioner");
+        SENK_REQUIRE(S.A.has_csr, "the system keeps no CSR copy of A");
         const int N = S.n, nnz = S.A.nnz;
         std::vector<double> v(nnz);
         std::vector<int> c(nnz), r(N + 1);

@@ -51,23 +51,26 @@ void launch_spmv_csr_s(const float *v, const int *c, const int *r, const float *
 }
 
 template <typename T>
-void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s)
+void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s, bool keep_csr)
 {
     SENK_REQUIRE(N > 0 && v && c && r, "empty or null matrix");
     n = N;
     nnz = r[N];
     SENK_REQUIRE(r[0] == 0 && nnz >= 0, "rptr must start at 0");
     lanes = csr_lanes(nnz, N);
-    val.alloc(std::max(nnz, 1));
-    cind.alloc(std::max(nnz, 1));
-    rptr.alloc(N + 1);
-    val.upload(v, nnz, s);
-    cind.upload(c, nnz, s);
-    rptr.upload(r, N + 1, s);
     // The inner SpMV defaults to SELL-32: one thread per row keeps every lane of
     // every FP64 instruction useful (GB300's FP64 pipe, not HBM, limits the
     // CSR-vector kernel).
     use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_AUTO;
+    has_csr = keep_csr || !use_sell;
+    if (has_csr) {
+        val.alloc(std::max(nnz, 1));
+        cind.alloc(std::max(nnz, 1));
+        rptr.alloc(N + 1);
+        val.upload(v, nnz, s);
+        cind.upload(c, nnz, s);
+        rptr.upload(r, N + 1, s);
+    }
     if (use_sell) {
         // SELL-32 (no row sorting): slice i = rows [32i, 32i+32), width = longest row.
         const int ns = (N + 31) / 32;

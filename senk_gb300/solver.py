@@ -199,7 +199,7 @@ class System:
     once; b and x live on the device between solves."""
 
     def __init__(self, A: Csr, L: Csr = None, U: Csr = None, precond: int = PC_NONE, cptr=None, cnum: int = 0,
-                 bsize: int = 1, dtype=np.float64, m_max: int = 30, mixed: bool = False, **opt):
+                 bsize: int = 1, dtype=np.float64, m_max: int = 30, mixed: int = 0, **opt):
         self.dtype = np.dtype(dtype)
         T = self.dtype
         self.n = A.n

@@ -62,3 +62,29 @@ def test_gmres_ir_needs_mixed_system():
     with pytest.raises(L.SenkError):
         sysm.gmres_ir(1.0, 5, 10, 1e-8)
     sysm.close()
+
+
+def test_ir_only_system_solves_and_refuses_plain_solvers():
+    """desc.mixed = 2 (what the drop-in GMRES-IR entry uses): no FP64
+    preconditioner or basis; GMRES-IR works, the FP64 solvers refuse."""
+    import numpy as np
+    from senk_gb300 import lib as L
+    from senk_gb300 import problems as P
+    from senk_gb300 import setup as S
+    from senk_gb300 import solver as SV
+    A = P.convdiff3d(24, 0.5)
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    Lf, Uf, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
+    b = Ar.matvec(P.uniform_solution(A.n, 0)[LP])
+    nb = float(np.linalg.norm(b))
+    sy = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=30, mixed=2)
+    try:
+        sy.set_rhs(b)
+        r = sy.gmres_ir(nb, 20, 30, 1e-8)
+        x = sy.get_x()
+        assert r.converged and np.linalg.norm(b - Ar.matvec(x)) / nb < 1e-8
+        with pytest.raises(L.SenkError):
+            sy.gmres(nb, 10, 30, 1e-8)
+    finally:
+        sy.close()
