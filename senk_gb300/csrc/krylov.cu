@@ -6,9 +6,31 @@
 #include <cmath>
 #include <cstdio>
 
+#include <chrono>
+
 #include "device.hpp"
 
 namespace senkgpu {
+
+namespace {
+
+// Wall-clock trace of host-side phases, printed to stderr when verbose >= 2.
+struct PhaseClock {
+    bool on;
+    const char *who;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void lap(const char *what)
+    {
+        if (!on) return;
+        const auto n = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "# setup %s %s %.2f ms\n", who, what,
+                     std::chrono::duration<double, std::milli>(n - t).count());
+        t = n;
+    }
+};
+
+}  // namespace
+
 
 namespace {
 
@@ -45,6 +67,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     n = d.N;
     ir_only = d.mixed == 2;
     if (o) opt = *o;
+    PhaseClock clk{opt.verbose >= 2, sizeof(T) == 8 ? "fp64" : "fp32"};
     if (shared) {
         stream = shared;
         own_stream = false;
@@ -54,9 +77,11 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     SENK_CUDA(cudaEventCreate(&ev0));
     SENK_CUDA(cudaEventCreate(&ev1));
     SENK_CUDA(cudaMallocHost((void **)&st_host, sizeof(KrylovState)));
+    clk.lap("stream+events");
     // GMRES-IR only: the FP64 system computes residuals and updates x; the
     // preconditioner and the Krylov basis live in the FP32 copy.
     A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream, !(sell_only || ir_only));
+    clk.lap("A upload (+SELL build)");
     if (ir_only) {
         // nothing to build here for the preconditioner
     } else if (d.precond == SENK_PC_ILUB || d.precond == SENK_PC_ILUB_ABMC) {
@@ -71,6 +96,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
         pc->build(n, (const T *)d.lval, d.lcind, d.lrptr, (const T *)d.uval, d.ucind, d.urptr, d.precond, d.cptr,
                   d.cnum, d.bsize, stream);
     }
+    clk.lap("preconditioner plan");
     b.alloc(n);
     x.alloc(n);
     t.alloc(n);
@@ -80,6 +106,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     red.ensure(stream);
     if (d.m_max > 0 && !ir_only) ensure_gmres(d.m_max);
     SENK_CUDA(cudaStreamSynchronize(stream));
+    clk.lap("vectors + Krylov workspace");
     h2d_bytes = (long long)(A.val.bytes() + A.cind.bytes() + A.rptr.bytes() + A.sval.bytes() + A.scol.bytes() +
                             A.soff.bytes());
     if (pcb) h2d_bytes += pcb->h2d_bytes();
@@ -100,6 +127,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
             return v;
         };
         std::vector<float> a32 = demote(d.val, d.rptr[n]), l32, u32;
+        clk.lap("demote A");
         senk_system_desc di = d;
         di.dtype = SENK_F32;
         di.mixed = 0;
@@ -110,8 +138,10 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
             di.lval = l32.data();
             di.uval = u32.data();
         }
+        clk.lap("demote factors");
         inner = std::make_unique<System<float>>();
         inner->create(di, &opt, stream, ir_only);
+        clk.lap("FP32 system");
         h2d_bytes += inner->h2d_bytes;
         irs.alloc(2);
         SENK_CUDA(cudaMallocHost((void **)&ir_host, 2 * sizeof(double)));
@@ -223,6 +253,7 @@ int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *re
     const int orth = opt.orth;
     SENK_REQUIRE(orth == SENK_ORTH_CGS2 || orth == SENK_ORTH_CGS || orth == SENK_ORTH_MGS, "unknown orthogonalisation");
     if (!cycle || cycle_m != m || cycle_orth != orth) {
+        PhaseClock clk{opt.verbose >= 2, sizeof(T) == 8 ? "fp64" : "fp32"};
         if (cycle) cudaGraphExecDestroy(cycle);
         cycle = nullptr;
         cudaGraph_t g;
@@ -235,12 +266,14 @@ int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *re
             throw;
         }
         SENK_CUDA(cudaStreamEndCapture(stream, &g));
+        clk.lap("GMRES cycle capture");
         size_t nodes = 0;
         SENK_CUDA(cudaGraphGetNodes(g, nullptr, &nodes));
         cycle_nodes = (long long)nodes;
         cudaError_t ie = cudaGraphInstantiate(&cycle, g, 0);
         cudaGraphDestroy(g);
         SENK_CUDA(ie);
+        clk.lap("GMRES cycle instantiate");
         cycle_m = m;
         cycle_orth = orth;
     }
