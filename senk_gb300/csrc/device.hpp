@@ -114,9 +114,16 @@ struct SpmvOp {
     DevBuf<T> sval;
     DevBuf<int> scol, soff;
 
-    // keep_csr = false (with a SELL format): only the SELL copy goes to the device
+    // keep_csr = false (with a SELL format): only the SELL copy stays on the device
     void upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s, bool keep_csr = true);
+    template <typename S>
+    void convert_from(const SpmvOp<S> &src, int format, cudaStream_t s, bool keep_csr);
+    template <typename S>
+    void sell_from_device(const S *dv, const int *dc, const int *dr, const std::vector<int> &off, cudaStream_t s);
+    void drop_csr(cudaStream_t s);
     bool has_csr = false;
+    std::vector<int> sell_off;  // host copy of the SELL slice offsets
+    long long h2d = 0;          // bytes copied from the host
     // y = A x (MODE 0) or y = b - A x (MODE 1)
     void apply(const T *x, T *y, cudaStream_t s, const int *gate) const;
     // y = b - A x, ||y|| -> *norm_out, 1/||y|| -> *inv_out
@@ -258,8 +265,10 @@ struct System {
     ~System();
     // `shared` (optional): run on this stream instead of creating one.
     // sell_only: keep A on the device as SELL only (no CSR copy).
+    // csr_src: an FP64 operator holding the same matrix (CSR on the device) to
+    // convert A from, instead of desc.val.
     void create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared = nullptr,
-                bool sell_only = false);
+                bool sell_only = false, const SpmvOp<double> *csr_src = nullptr);
     bool ir_only = false;  // desc.mixed == 2: the FP64 part serves GMRES-IR's outer loop only
     int gmres_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
                  senk_result *res);

@@ -60,7 +60,8 @@ System<T>::~System()
 }
 
 template <typename T>
-void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared, bool sell_only)
+void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStream_t shared, bool sell_only,
+                       const SpmvOp<double> *csr_src)
 {
     SENK_REQUIRE(d.N > 0, "N must be positive");
     SENK_REQUIRE(d.mixed >= 0 && d.mixed <= 2, "mixed must be 0, 1 or 2");
@@ -80,7 +81,13 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     clk.lap("stream+events");
     // GMRES-IR only: the FP64 system computes residuals and updates x; the
     // preconditioner and the Krylov basis live in the FP32 copy.
-    A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream, !(sell_only || ir_only));
+    if (csr_src) {
+        // FP32 copy of an FP64 system: converted on the device
+        A.convert_from(*csr_src, opt.spmv, stream, !sell_only);
+    } else {
+        // an FP32 copy still needs the CSR arrays (dropped once it is built)
+        A.upload((const T *)d.val, d.cind, d.rptr, n, opt.spmv, stream, !(sell_only || ir_only) || d.mixed);
+    }
     clk.lap("A upload (+SELL build)");
     if (ir_only) {
         // nothing to build here for the preconditioner
@@ -107,8 +114,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     if (d.m_max > 0 && !ir_only) ensure_gmres(d.m_max);
     SENK_CUDA(cudaStreamSynchronize(stream));
     clk.lap("vectors + Krylov workspace");
-    h2d_bytes = (long long)(A.val.bytes() + A.cind.bytes() + A.rptr.bytes() + A.sval.bytes() + A.scol.bytes() +
-                            A.soff.bytes());
+    h2d_bytes = A.h2d;
     if (pcb) h2d_bytes += pcb->h2d_bytes();
     if (pc) {
         for (const SweepFactor<T> *F : {&pc->L, &pc->U})
@@ -126,12 +132,11 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
             for (int i = 0; i < cnt; i++) v[i] = (float)p[i];
             return v;
         };
-        std::vector<float> a32 = demote(d.val, d.rptr[n]), l32, u32;
-        clk.lap("demote A");
+        std::vector<float> l32, u32;
         senk_system_desc di = d;
         di.dtype = SENK_F32;
         di.mixed = 0;
-        di.val = a32.data();
+        di.val = nullptr;  // A comes from this system's device copy
         if (d.precond != SENK_PC_NONE) {
             l32 = demote(d.lval, d.lrptr[n]);
             u32 = demote(d.uval, d.urptr[n]);
@@ -140,7 +145,8 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
         }
         clk.lap("demote factors");
         inner = std::make_unique<System<float>>();
-        inner->create(di, &opt, stream, ir_only);
+        if constexpr (std::is_same<T, double>::value) inner->create(di, &opt, stream, ir_only, &A);
+        if (ir_only) A.drop_csr(stream);
         clk.lap("FP32 system");
         h2d_bytes += inner->h2d_bytes;
         irs.alloc(2);

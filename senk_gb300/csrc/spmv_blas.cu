@@ -50,6 +50,72 @@ void launch_spmv_csr_s(const float *v, const int *c, const int *r, const float *
     else spmv_csr_dispatch<float, float, 0>(v, c, r, x, b, y, n, lanes, s, gate);
 }
 
+// CSR -> SELL-32 on the device: one warp per slice of 32 rows, lane = row;
+// slot k of the slice's row is element off[slice] + 32 k + lane. Padding reads
+// a valid x entry (the row itself) times 0. Values are converted to TD.
+template <typename TS, typename TD>
+__global__ void __launch_bounds__(kThreads)
+k_csr_to_sell(const TS *__restrict__ v, const int *__restrict__ c, const int *__restrict__ r,
+              const int *__restrict__ off, TD *__restrict__ sv, int *__restrict__ sc, int n)
+{
+    const long long slice = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long q = slice * 32 + lane;
+    if (slice * 32 >= n) return;
+    const int o = off[slice], w = (off[slice + 1] - o) / 32;
+    const int b = q < n ? r[q] : 0, len = q < n ? r[q + 1] - b : 0;
+    for (int k = 0; k < w; k++) {
+        const long long at = o + (long long)k * 32 + lane;
+        if (k < len) {
+            sv[at] = (TD)v[b + k];
+            sc[at] = c[b + k];
+        } else {
+            sv[at] = TD(0);
+            sc[at] = q < n ? (int)q : 0;
+        }
+    }
+}
+
+template <typename TS, typename TD>
+__global__ void __launch_bounds__(kThreads) k_cast(const TS *__restrict__ a, TD *__restrict__ b, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (TD)a[i];
+}
+
+// Slice offsets of SELL-32 from a host row pointer: slice width = longest row.
+static std::vector<int> sell_offsets(const int *r, int N)
+{
+    const int ns = (N + 31) / 32;
+    std::vector<int> off(ns + 1, 0);
+    long long acc = 0;
+    for (int i = 0; i < ns; i++) {
+        int w = 0;
+        const int e = std::min(N, i * 32 + 32);
+        for (int q = i * 32; q < e; q++) w = std::max(w, r[q + 1] - r[q]);
+        acc += 32LL * w;
+        SENK_REQUIRE(acc < INT_MAX, "matrix too large for SELL-32 offsets");
+        off[i + 1] = (int)acc;
+    }
+    return off;
+}
+
+template <typename T>
+template <typename S>
+void SpmvOp<T>::sell_from_device(const S *dv, const int *dc, const int *dr, const std::vector<int> &off, cudaStream_t s)
+{
+    sell_off = off;
+    h2d += (long long)sizeof(int) * off.size();
+    const int ns = (int)off.size() - 1;
+    sval.alloc(std::max(off[ns], 1));
+    scol.alloc(std::max(off[ns], 1));
+    soff.alloc(off.size());
+    soff.upload(off.data(), off.size(), s);
+    k_csr_to_sell<S, T><<<ceil_div((long long)ns * 32, kThreads), kThreads, 0, s>>>(dv, dc, dr, soff.p, sval.p, scol.p,
+                                                                                   n);
+    SENK_LAUNCH_CHECK();
+}
+
 template <typename T>
 void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s, bool keep_csr)
 {
@@ -60,55 +126,68 @@ void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format
     lanes = csr_lanes(nnz, N);
     // The inner SpMV defaults to SELL-32: one thread per row keeps every lane of
     // every FP64 instruction useful (GB300's FP64 pipe, not HBM, limits the
-    // CSR-vector kernel).
+    // CSR-vector kernel). The CSR arrays go up as they are and the SELL copy is
+    // built from them on the device.
     use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_AUTO;
+    val.alloc(std::max(nnz, 1));
+    cind.alloc(std::max(nnz, 1));
+    rptr.alloc(N + 1);
+    val.upload(v, nnz, s);
+    cind.upload(c, nnz, s);
+    rptr.upload(r, N + 1, s);
+    has_csr = true;
+    h2d = (long long)(sizeof(T) + sizeof(int)) * nnz + sizeof(int) * (N + 1LL);
+    if (use_sell) sell_from_device<T>(val.p, cind.p, rptr.p, sell_offsets(r, N), s);
+    if (!keep_csr) drop_csr(s);
+}
+
+// The same matrix in another precision, converted on the device from `src`,
+// which must still hold its CSR arrays.
+template <typename T>
+template <typename S>
+void SpmvOp<T>::convert_from(const SpmvOp<S> &src, int format, cudaStream_t s, bool keep_csr)
+{
+    SENK_REQUIRE(src.has_csr, "the source operator keeps no CSR copy");
+    n = src.n;
+    nnz = src.nnz;
+    lanes = src.lanes;
+    use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_AUTO;
+    if (use_sell) {
+        SENK_REQUIRE(!src.sell_off.empty() || !src.use_sell, "source SELL offsets missing");
+        std::vector<int> off = src.sell_off;
+        if (off.empty()) {
+            std::vector<int> hr(n + 1);
+            SENK_CUDA(cudaMemcpyAsync(hr.data(), src.rptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+            SENK_CUDA(cudaStreamSynchronize(s));
+            off = sell_offsets(hr.data(), n);
+        }
+        sell_from_device<S>(src.val.p, src.cind.p, src.rptr.p, off, s);
+    }
     has_csr = keep_csr || !use_sell;
     if (has_csr) {
         val.alloc(std::max(nnz, 1));
         cind.alloc(std::max(nnz, 1));
-        rptr.alloc(N + 1);
-        val.upload(v, nnz, s);
-        cind.upload(c, nnz, s);
-        rptr.upload(r, N + 1, s);
-    }
-    if (use_sell) {
-        // SELL-32 (no row sorting): slice i = rows [32i, 32i+32), width = longest row.
-        const int ns = (N + 31) / 32;
-        std::vector<int> off(ns + 1, 0);
-        for (int i = 0; i < ns; i++) {
-            int w = 0;
-            for (int q = i * 32; q < std::min(N, i * 32 + 32); q++) w = std::max(w, r[q + 1] - r[q]);
-            SENK_REQUIRE((long long)off[i] + 32LL * w < INT_MAX, "matrix too large for SELL-32 offsets");
-            off[i + 1] = off[i] + 32 * w;
-        }
-        std::vector<T> hv(std::max(off[ns], 1), T(0));
-        std::vector<int> hc(std::max(off[ns], 1), 0);
-#pragma omp parallel for schedule(static)
-        for (int i = 0; i < ns; i++) {
-            const int w = (off[i + 1] - off[i]) / 32;
-            for (int l = 0; l < 32; l++) {
-                const int q = i * 32 + l;
-                const int len = q < N ? r[q + 1] - r[q] : 0;
-                for (int k = 0; k < w; k++) {
-                    const long long at = off[i] + (long long)k * 32 + l;
-                    if (k < len) {
-                        hv[at] = v[r[q] + k];
-                        hc[at] = c[r[q] + k];
-                    } else {
-                        hc[at] = q < N ? q : 0;  // padding reads a valid x entry, times 0
-                    }
-                }
-            }
-        }
-        sval.alloc(hv.size());
-        scol.alloc(hc.size());
-        soff.alloc(off.size());
-        sval.upload(hv.data(), hv.size(), s);
-        scol.upload(hc.data(), hc.size(), s);
-        soff.upload(off.data(), off.size(), s);
-        SENK_CUDA(cudaStreamSynchronize(s));
+        rptr.alloc(n + 1);
+        k_cast<S, T><<<stream_grid(nnz, kThreads, 8), kThreads, 0, s>>>(src.val.p, val.p, nnz);
+        SENK_CUDA(cudaMemcpyAsync(cind.p, src.cind.p, sizeof(int) * nnz, cudaMemcpyDeviceToDevice, s));
+        SENK_CUDA(cudaMemcpyAsync(rptr.p, src.rptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToDevice, s));
+        SENK_LAUNCH_CHECK();
     }
 }
+
+template <typename T>
+void SpmvOp<T>::drop_csr(cudaStream_t s)
+{
+    if (!use_sell || !has_csr) return;
+    SENK_CUDA(cudaStreamSynchronize(s));  // the SELL build may still read them
+    val.release();
+    cind.release();
+    rptr.release();
+    has_csr = false;
+}
+
+template void SpmvOp<float>::convert_from<double>(const SpmvOp<double> &, int, cudaStream_t, bool);
+template void SpmvOp<double>::convert_from<double>(const SpmvOp<double> &, int, cudaStream_t, bool);
 
 template <typename T>
 void SpmvOp<T>::apply(const T *x, T *y, cudaStream_t s, const int *gate) const

@@ -13,6 +13,7 @@
 // 32-wide column across the group's chains, so a warp's loads coalesce.
 #include <algorithm>
 #include <climits>
+#include <memory>
 
 #include "device.hpp"
 
@@ -108,8 +109,15 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
         for (int i = F.colour_groups[c]; i < F.colour_groups[c + 1]; i++)
             F.colour_smem[c] = std::max(F.colour_smem[c], (size_t)slots[i] * 32 * (sizeof(VT) + sizeof(int)));
     F.elems = off;
-    std::vector<VT> hv((size_t)std::max<long long>(off, 1), VT(0));
-    std::vector<int> hc((size_t)std::max<long long>(off, 1), -1);
+    // padding is (0, column -1); filled in parallel (the arrays run to 100s of MB)
+    const long long ne = std::max<long long>(off, 1);
+    std::unique_ptr<VT[]> hv(new VT[ne]);
+    std::unique_ptr<int[]> hc(new int[ne]);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < ne; i++) {
+        hv[i] = VT(0);
+        hc[i] = -1;
+    }
     std::vector<VT> hd(upper ? N : 0);
     long long stored = 0;
 #pragma omp parallel for schedule(static) reduction(+ : stored)
@@ -149,10 +157,10 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
         }
     }
     F.nnz = stored + (upper ? N : 0);
-    F.val.alloc(hv.size());
-    F.val.upload(hv.data(), hv.size(), s);
-    F.col.alloc(hc.size());
-    F.col.upload(hc.data(), hc.size(), s);
+    F.val.alloc(ne);
+    F.val.upload(hv.get(), ne, s);
+    F.col.alloc(ne);
+    F.col.upload(hc.get(), ne, s);
     if (upper) {
         F.dinv.alloc(N);
         F.dinv.upload(hd.data(), N, s);
