@@ -15,6 +15,12 @@ Workloads:
     exp((g_p+g_q)/2) of a Gaussian random field g (FFT spectral synthesis,
     Gaussian covariance with correlation length ``corr`` cells, std ``sigma``);
     boundary faces use the cell's own exp(g_p) (zero Dirichlet ghost).
+  * ``block27(96, ...)``      block-3x3 system on an n^3 grid with a 27-point
+    stencil: dense 3x3 off-diagonal blocks with entries U(-1, 0) * scale, SPD
+    diagonal blocks S S^T + c I with c chosen so that the smallest eigenvalue of
+    each diagonal block is at least 1.1 times the sum of the spectral norms of
+    its row's off-diagonal blocks (block diagonal dominance 1.1). N = 3 n^3 rows,
+    nnz = 9 * (number of nonzero blocks), as generated (no "71M" rounding).
 """
 from __future__ import annotations
 
@@ -138,3 +144,64 @@ def uniform_solution(n: int, seed: int = 0) -> np.ndarray:
 def normal_solution(n: int, seed: int = 1) -> np.ndarray:
     """x_true ~ N(0, 1) from numpy.random.default_rng(seed)."""
     return np.random.default_rng(seed).standard_normal(n)
+
+
+def block27(n: int = 96, scale: float = 1.0, dominance: float = 1.1, seed: int = 0) -> Csr:
+    """Block-3x3 27-point system on an n^3 grid (3 unknowns per node, node-major:
+    row 3*node + k), seeded."""
+    rng = np.random.default_rng([seed, 27])
+    nn = n ** 3
+    node = np.arange(nn, dtype=np.int64)
+    i, j, k = node % n, (node // n) % n, node // (n * n)
+    nbrs, keep = [], []
+    for dk in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            for di in (-1, 0, 1):
+                ii, jj, kk = i + di, j + dj, k + dk
+                ok = (ii >= 0) & (ii < n) & (jj >= 0) & (jj < n) & (kk >= 0) & (kk < n)
+                nbrs.append(ii + n * jj + n * n * kk)
+                keep.append(ok)
+    nbrs = np.stack(nbrs, axis=1)        # nn x 27, ascending node index (dk, dj, di order)
+    keep = np.stack(keep, axis=1)
+    blocks = -rng.uniform(0.0, 1.0, (nn, 27, 3, 3)) * scale
+    blocks[~keep] = 0.0
+    centre = 13                           # (0, 0, 0)
+    offn = np.linalg.norm(blocks, ord=2, axis=(2, 3))
+    offn[:, centre] = 0.0
+    offsum = offn.sum(axis=1)
+    S = rng.uniform(-1.0, 1.0, (nn, 3, 3))
+    D = S @ np.transpose(S, (0, 2, 1))
+    lam = np.linalg.eigvalsh(D)[:, 0]
+    c = np.maximum(dominance * offsum - lam, 0.0) + 1e-3
+    blocks[:, centre] = D + c[:, None, None] * np.eye(3)
+    # scalar CSR: row 3*node + a, columns 3*nbr + b for each kept neighbour
+    cnt = keep.sum(axis=1) * 3
+    rptr = np.zeros(3 * nn + 1, np.int64)
+    rptr[1:] = np.cumsum(np.repeat(cnt, 3))
+    cols = (3 * nbrs[:, :, None] + np.arange(3)[None, None, :])       # nn x 27 x 3
+    cols = np.broadcast_to(cols[:, None, :, :], (nn, 3, 27, 3))       # node, a, nbr, b
+    vals = np.transpose(blocks, (0, 2, 1, 3))                          # node, a, nbr, b
+    mask = np.broadcast_to(keep[:, None, :, None], (nn, 3, 27, 3))
+    return Csr(np.ascontiguousarray(vals[mask], np.float64), np.ascontiguousarray(cols[mask], np.int32),
+               rptr.astype(np.int32))
+
+
+def expand_node_permutation(LP_nodes: np.ndarray, bs: int = 3) -> tuple:
+    """Scalar-row permutations (LP, RP) of a node permutation, bs rows per node:
+    new scalar row bs*i + a is old row bs*LP_nodes[i] + a."""
+    LP = (bs * np.asarray(LP_nodes, np.int64)[:, None] + np.arange(bs)[None, :]).reshape(-1)
+    RP = np.empty_like(LP)
+    RP[LP] = np.arange(LP.size)
+    return LP.astype(np.int32), RP.astype(np.int32)
+
+
+def node_graph(A: Csr, bs: int = 3) -> Csr:
+    """Pattern of the node graph of a block matrix (one entry per nonzero block)."""
+    nrows = A.n // bs
+    rows = np.repeat(np.arange(A.n), np.diff(A.rptr)) // bs
+    cols = A.cind.astype(np.int64) // bs
+    key = np.unique(rows * nrows + cols)
+    r, c = key // nrows, key % nrows
+    rptr = np.zeros(nrows + 1, np.int64)
+    np.add.at(rptr, r + 1, 1)
+    return Csr(np.ones(key.size), c.astype(np.int32), np.cumsum(rptr).astype(np.int32))

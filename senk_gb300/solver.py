@@ -198,8 +198,10 @@ class System:
     """A device-resident system: A (+ split ILU factors and their schedule) uploaded
     once; b and x live on the device between solves."""
 
-    def __init__(self, A: Csr, L: Csr = None, U: Csr = None, precond: int = PC_NONE, cptr=None, cnum: int = 0,
-                 bsize: int = 1, dtype=np.float64, m_max: int = 30, mixed: int = 0, **opt):
+    def __init__(self, A: Csr, L=None, U=None, precond: int = PC_NONE, cptr=None, cnum: int = 0,
+                 bsize: int = 1, dtype=np.float64, m_max: int = 30, mixed: int = 0, block=(1, 1), **opt):
+        """L, U: split ILU factors (Csr), or for PC_ILUB / PC_ILUB_ABMC the BCSR
+        factors as (bval, bcind, brptr) tuples with `block` = (bnl, bnw)."""
         self.dtype = np.dtype(dtype)
         T = self.dtype
         self.n = A.n
@@ -209,8 +211,11 @@ class System:
         d.val, d.cind, d.rptr = [ptr(a) for a in self._keep]
         d.precond = precond
         if precond != PC_NONE:
-            fac = [_arr(L.val, T), _arr(L.cind, np.int32), _arr(L.rptr, np.int32), _arr(U.val, T),
-                   _arr(U.cind, np.int32), _arr(U.rptr, np.int32)]
+            lv, lc, lr = (L.val, L.cind, L.rptr) if isinstance(L, Csr) else L
+            uv, uc, ur = (U.val, U.cind, U.rptr) if isinstance(U, Csr) else U
+            fac = [_arr(lv, T), _arr(lc, np.int32), _arr(lr, np.int32), _arr(uv, T), _arr(uc, np.int32),
+                   _arr(ur, np.int32)]
+            d.bnl, d.bnw = block
             self._keep += fac
             d.lval, d.lcind, d.lrptr, d.uval, d.ucind, d.urptr = [ptr(a) for a in fac]
             if cptr is not None:

@@ -271,3 +271,17 @@ def test_live_solvers_match_reference(port, ref):
     x, it, res, _ = port.solve("gcr", Ar, b, L=L, U=U, pc=oracle.PC_ILU, outer=100, m=20, eps=1e-8, nrm_b=nb)
     assert it == oracle.parse_solver_stdout(t)["iters"]
     np.testing.assert_allclose(x, xr, rtol=0, atol=1e-11)
+
+
+def test_block27_generator_and_live_ilub33_gcr(port, ref):
+    A = P.block27(4, seed=3)
+    assert A.n == 192 and np.all(np.diff(A.rptr) % 3 == 0)
+    Lf, Uf, _ = port.split(port.ilu0(port.alloc_block_zero(A, 3, 3)), "L-DU", True)
+    bl, bu = port.csr2bcsr(Lf, 3, 3), port.csr2bcsr(Uf, 3, 3)
+    assert all(np.array_equal(p, q) for p, q in zip(bl, ref.csr2bcsr(Lf, 3, 3)))
+    b = A.matvec(np.ones(A.n))
+    nb = float(np.linalg.norm(b))
+    _, it, _, _ = port.solve("gcr", A, b, L=bl, U=bu, pc=oracle.PC_ILUB, bnl=3, bnw=3, outer=100, m=20, eps=1e-8)
+    txt = ref.solve_text("ilub_gcr_d", A.val, A.cind, A.rptr, *bl, *bu, b, np.zeros(A.n), nb, 100, 20, A.n, 1e-8,
+                         3, 3)
+    assert it == oracle.parse_solver_stdout(txt)["iters"]
