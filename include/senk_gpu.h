@@ -401,8 +401,11 @@ int senk_mpnn_set_params(senk_mpnn *net, const float *params, int nparams);
 /* Graph data (row-normalised |A| off-diagonal, its transpose, diagonal and row
  * sums) and activations for the system's matrix. */
 int senk_mpnn_bind(senk_mpnn *net, senk_system *sys);
-/* Loss of one residual/error pair: t = (e - ILU(r)) mean(a_ii) / ||r||_rms,
- * loss = sum (net(r) - t)^2 / sum t^2; gradient to grad (host, may be NULL). */
+/* Training objective: 1 (default) residual space, q = (r - A ILU(r)) / ||r||_rms,
+ * loss = |A c / mean(a_ii) - q|^2 / |q|^2 with c = net(r); 0 error space,
+ * t = (e - ILU(r)) mean(a_ii) / ||r||_rms, loss = |c - t|^2 / |t|^2. */
+int senk_mpnn_set_loss(senk_mpnn *net, int mode);
+/* Loss of one residual/error pair; gradient to grad (host, may be NULL). */
 int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const double *e, double *loss,
                         float *grad);
 /* loss_grad, then one Adam step (beta 0.9 / 0.999, eps 1e-8) with rate lr. */

@@ -70,6 +70,9 @@ class Graph:
         Woff = absA - sp.diags(np.abs(diag))
         Woff.eliminate_zeros()
         inv = np.divide(1.0, off, out=np.zeros_like(off), where=off > 0)
+        self.A = A
+        self.A32 = sp.csr_matrix((A.data.astype(np.float32).astype(np.float64), A.indices, A.indptr), shape=A.shape)
+        self.A32T = self.A32.T.tocsr()
         self.W = (sp.diags(inv) @ Woff).tocsr()
         # the GPU keeps W in FP32
         self.W.data = self.W.data.astype(np.float32).astype(np.float64)
@@ -118,18 +121,29 @@ def apply(P, g: Graph, r, ilu, rounding=True):
     return np.asarray(ilu, np.float64) + cache["rms"] / g.d * c
 
 
-def loss_grad(P, g: Graph, r, ilu, e, rounding=True):
-    """(loss, gradient) for one residual/error pair, as senk_mpnn_loss_grad."""
+def loss_grad(P, g: Graph, r, ilu, e, rounding=True, mode=1):
+    """(loss, gradient) for one residual/error pair, as senk_mpnn_loss_grad.
+    mode 1 (residual space): q = (r - A ILU(r)) / rms, loss = |A c / d - q|^2 / |q|^2;
+    mode 0 (error space): t = (e - ILU(r)) d / rms, loss = |c - t|^2 / |t|^2."""
     Win, bin_, layers, wout, bout = unpack(P)
     c, ch = forward(P, g, r, rounding)
-    t = (np.asarray(e, np.float64) - np.asarray(ilu, np.float64)) * g.d * ch["inv"]
-    if rounding:
-        t = t.astype(np.float32).astype(np.float64)
-    S = float(np.dot(t, t))
-    diff = c - t
-    loss = float(np.dot(diff, diff)) / S
+    if mode == 0:
+        t = (np.asarray(e, np.float64) - np.asarray(ilu, np.float64)) * g.d * ch["inv"]
+        if rounding:
+            t = t.astype(np.float32).astype(np.float64)
+        S = float(np.dot(t, t))
+        diff = c - t
+        loss = float(np.dot(diff, diff)) / S
+        dc = 2.0 * diff / S
+    else:
+        q = (np.asarray(r, np.float64) - g.A @ np.asarray(ilu, np.float64)) * ch["inv"]
+        if rounding:
+            q = q.astype(np.float32).astype(np.float64)
+        S = float(np.dot(q, q))
+        res = g.A32 @ c / g.d - q
+        loss = float(np.dot(res, res)) / S
+        dc = 2.0 / (g.d * S) * (g.A32T @ res)
     G = np.zeros(NPARAMS)
-    dc = 2.0 * diff / S
     H = ch["H"]
     G[OFF_WOUT:OFF_BOUT] = H[LAYERS].T @ dc
     G[OFF_BOUT] = dc.sum()

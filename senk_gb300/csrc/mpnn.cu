@@ -10,9 +10,11 @@
 //                   z = [h, m] Theta_l + beta_l                     (128 -> 64, tcgen05)
 //                   h <- h + relu(z)
 //   c = h w_out + b_out                                            (64 -> 1)
-// Training target for a residual/error pair (r, e): t = (e - ILU(r)) d / ||r||_rms,
-// loss = sum (c - t)^2 / sum t^2. GEMM operands are BF16 with FP32 accumulation;
-// the residual stream, gradients and the Adam state are FP32.
+// Training objective for a residual/error pair (r, e), by default in residual
+// space: q = (r - A ILU(r)) / ||r||_rms, loss = |A c / d - q|^2 / |q|^2 (what the
+// correction leaves of the ILU residual); or in error space:
+// t = (e - ILU(r)) d / ||r||_rms, loss = |c - t|^2 / |t|^2. GEMM operands are BF16
+// with FP32 accumulation; the residual stream, gradients and Adam state are FP32.
 #include <cmath>
 #include <vector>
 
@@ -161,56 +163,6 @@ k_target(const T *e, const T *ilu, const float *rms, float d, float *t, long lon
     }
 }
 
-// Training decoder: c_i = h_i . w_out + b_out; loss = sum (c - t)^2 / sum t^2;
-// dc = 2 (c - t) / sum t^2; dH4 = dc w_out; grad w_out += dc h; grad b_out += dc.
-// Warp per node; per-CTA partial sums, then atomics. acc[0] = sum t^2, acc[1] += sum (c-t)^2.
-__global__ void __launch_bounds__(kThreads)
-k_decode_train(const float *H, const float *P, const float *t, float *dH, float *G, double *acc, long long n)
-{
-    __shared__ float gw[kThreads / 32][kHid];
-    __shared__ float gb[kThreads / 32];
-    __shared__ double gl[kThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const float inv = acc[0] > 0 ? (float)(1.0 / acc[0]) : 0.f;
-    const float w0 = P[kOffWout + 2 * lane], w1 = P[kOffWout + 2 * lane + 1];
-    float g0 = 0.f, g1 = 0.f, gbs = 0.f;
-    double ls = 0;
-    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-        const float2 h = *reinterpret_cast<const float2 *>(H + i * 64 + 2 * lane);
-        float c = warp_sum(h.x * w0 + h.y * w1) + P[kOffBout];
-        const float diff = c - t[i];
-        const float dc = 2.f * diff * inv;
-        ls += (double)diff * diff;
-        *reinterpret_cast<float2 *>(dH + i * 64 + 2 * lane) = make_float2(dc * w0, dc * w1);
-        g0 += dc * h.x;
-        g1 += dc * h.y;
-        gbs += dc;
-    }
-    gw[wid][2 * lane] = g0;
-    gw[wid][2 * lane + 1] = g1;
-    if (lane == 0) {
-        gb[wid] = gbs;
-        gl[wid] = ls;
-    }
-    __syncthreads();
-    if (threadIdx.x < kHid) {
-        float s = 0;
-        for (int w = 0; w < kThreads / 32; w++) s += gw[w][threadIdx.x];
-        atomicAdd(G + kOffWout + threadIdx.x, s);
-    }
-    if (threadIdx.x == 0) {
-        float s = 0;
-        double l = 0;
-        for (int w = 0; w < kThreads / 32; w++) {
-            s += gb[w];
-            l += gl[w];
-        }
-        atomicAdd(G + kOffBout, s);
-        atomicAdd(acc + 1, l);
-    }
-}
-
 // dZ = bf16(dH (.) [z > 0]); grad beta += column sums of the FP32 product.
 // Block of 256 threads = 4 nodes x 64 features, grid-stride over nodes.
 __global__ void __launch_bounds__(kThreads)
@@ -289,6 +241,114 @@ __global__ void __launch_bounds__(kThreads) k_weights_bf16(const float *P, bf16 
     WTb[(long long)l * 128 * 64 + j * 128 + i] = v;  // Theta_l^T[j][i]
 }
 
+// c_i = h_i . w_out + b_out, warp per node
+__global__ void __launch_bounds__(kThreads) k_decode_c(const float *H, const float *P, float *c, long long n)
+{
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const float2 h = *reinterpret_cast<const float2 *>(H + i * 64 + 2 * lane);
+    const float v = warp_sum(h.x * P[kOffWout + 2 * lane] + h.y * P[kOffWout + 2 * lane + 1]);
+    if (lane == 0) c[i] = v + P[kOffBout];
+}
+
+// Error-space loss: dc = 2 (c - t) / acc[0]; acc[1] += sum (c - t)^2
+__global__ void __launch_bounds__(kThreads) k_loss_error(const float *c, const float *t, float *dc, double *acc, long long n)
+{
+    const float inv = acc[0] > 0 ? (float)(1.0 / acc[0]) : 0.f;
+    double ls = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float diff = c[i] - t[i];
+        dc[i] = 2.f * diff * inv;
+        ls += (double)diff * diff;
+    }
+    __shared__ double sh[32];
+    ls = block_sum(ls, sh);
+    if (threadIdx.x == 0) atomicAdd(acc + 1, ls);
+}
+
+// Residual-space target: qh = (r - A ILU(r)) / rms; acc[0] += sum qh^2
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_resid_target(const T *r, const T *ailu, const float *rms, float *qh, double *acc, long long n)
+{
+    double s = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float v = (float)(((double)r[i] - (double)ailu[i]) * (double)rms[1]);
+        qh[i] = v;
+        s += (double)v * v;
+    }
+    __shared__ double sh[32];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) atomicAdd(acc, s);
+}
+
+// y = alpha * (B x) with B in CSR (FP32 values), thread per row; with qh: the
+// residual e = (B x) / d - qh, acc[1] += sum e^2.
+__global__ void __launch_bounds__(kThreads)
+k_spmv_loss(const int *rp, const int *ci, const float *bv, const float *x, float *y, long long n, float inv_d,
+            const float *qh, double *acc)
+{
+    double ls = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float a = 0.f;
+        for (int p = rp[i]; p < rp[i + 1]; p++) a += bv[p] * x[ci[p]];
+        const float e = a * inv_d - qh[i];
+        y[i] = e;
+        ls += (double)e * e;
+    }
+    __shared__ double sh[32];
+    ls = block_sum(ls, sh);
+    if (threadIdx.x == 0) atomicAdd(acc + 1, ls);
+}
+
+// dc = 2 / (d acc[0]) * (B^T e), thread per row of B^T
+__global__ void __launch_bounds__(kThreads)
+k_spmv_grad(const int *rp, const int *ci, const float *bv, const float *e, float *dc, long long n, float inv_d,
+            const double *acc)
+{
+    const float sc = acc[0] > 0 ? (float)(2.0 * inv_d / acc[0]) : 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float a = 0.f;
+        for (int p = rp[i]; p < rp[i + 1]; p++) a += bv[p] * e[ci[p]];
+        dc[i] = sc * a;
+    }
+}
+
+// Decoder backward: dH4 = dc w_out; grad w_out += dc h; grad b_out += dc (warp per node)
+__global__ void __launch_bounds__(kThreads)
+k_decode_back(const float *H, const float *P, const float *dc, float *dH, float *G, long long n)
+{
+    __shared__ float gw[kThreads / 32][kHid];
+    __shared__ float gb[kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const float w0 = P[kOffWout + 2 * lane], w1 = P[kOffWout + 2 * lane + 1];
+    float g0 = 0.f, g1 = 0.f, gbs = 0.f;
+    const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const float2 h = *reinterpret_cast<const float2 *>(H + i * 64 + 2 * lane);
+        const float g = dc[i];
+        *reinterpret_cast<float2 *>(dH + i * 64 + 2 * lane) = make_float2(g * w0, g * w1);
+        g0 += g * h.x;
+        g1 += g * h.y;
+        gbs += g;
+    }
+    gw[wid][2 * lane] = g0;
+    gw[wid][2 * lane + 1] = g1;
+    if (lane == 0) gb[wid] = gbs;
+    __syncthreads();
+    if (threadIdx.x < kHid) {
+        float s = 0;
+        for (int w = 0; w < kThreads / 32; w++) s += gw[w][threadIdx.x];
+        atomicAdd(G + kOffWout + threadIdx.x, s);
+    }
+    if (threadIdx.x == 0) {
+        float s = 0;
+        for (int w = 0; w < kThreads / 32; w++) s += gb[w];
+        atomicAdd(G + kOffBout, s);
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ the network
@@ -304,6 +364,10 @@ struct Mpnn {
     float d = 1.f;                // mean diagonal
     DevBuf<int> wr, wc, tr, tcol; // W and W^T (CSR)
     DevBuf<float> wv, tv, fd, fs;
+    DevBuf<int> ar, ac, atr, atc; // A and A^T (CSR, FP32 values) for the residual-space loss
+    DevBuf<float> av, atv, cbuf, dcb, ebuf;
+    DevBuf<double> ailu;          // A ILU(r)
+    int loss_mode = 1;            // 0: error space, 1: residual space
     // activations
     DevBuf<bf16> X[kLayers], Z[kLayers], dZ;
     DevBuf<float> H[kLayers + 1], dH, dH2, dM, t;
@@ -379,10 +443,31 @@ struct Mpnn {
                 tc_[q] = i;
                 tw[q] = w[p];
             }
+        // A and A^T with FP32 values
+        std::vector<int> atr_(N + 1, 0), atc_(rptr[N]), fill2;
+        std::vector<float> av_(rptr[N]), atv_(rptr[N]);
+        for (int p = 0; p < rptr[N]; p++) {
+            av_[p] = (float)val[p];
+            atr_[cind[p] + 1]++;
+        }
+        for (int i = 0; i < N; i++) atr_[i + 1] += atr_[i];
+        fill2.assign(atr_.begin(), atr_.end() - 1);
+        for (int i = 0; i < N; i++)
+            for (int p = rptr[i]; p < rptr[i + 1]; p++) {
+                const int q = fill2[cind[p]]++;
+                atc_[q] = i;
+                atv_[q] = av_[p];
+            }
         auto put = [s](auto &buf, const auto &h) {
             buf.alloc(h.size());
             buf.upload(h.data(), h.size(), s);
         };
+        put(ar, std::vector<int>(rptr, rptr + N + 1));
+        put(ac, std::vector<int>(cind, cind + rptr[N]));
+        put(av, av_);
+        put(atr, atr_);
+        put(atc, atc_);
+        put(atv, atv_);
         put(wr, r);
         put(wc, c);
         put(wv, w);
@@ -403,6 +488,10 @@ struct Mpnn {
             dH2.alloc((size_t)N * 64);
             dM.alloc((size_t)N * 64);
             t.alloc(N);
+            cbuf.alloc(N);
+            dcb.alloc(N);
+            ebuf.alloc(N);
+            ailu.alloc(N);
         }
         SENK_CUDA(cudaStreamSynchronize(s));
     }
@@ -438,16 +527,28 @@ struct Mpnn {
         SENK_LAUNCH_CHECK();
     }
 
-    // Loss and gradient of one (r, ILU(r), e) triple into G (zeroed first).
+    // Loss and gradient of one residual/error pair into G (zeroed first).
+    //  loss_mode 0 (error space):    t = (e - ILU(r)) d / rms, loss = |c - t|^2 / |t|^2
+    //  loss_mode 1 (residual space): q = (r - A ILU(r)) / rms,
+    //                                loss = |A c / d - q|^2 / |q|^2
+    // `ailu_dev` holds A ILU(r) (mode 1).
     template <typename T>
-    void loss_grad(const T *r, const T *ilu, const T *e, cudaStream_t s)
+    void loss_grad(const T *r, const T *ilu, const T *e, const T *ailu_dev, cudaStream_t s)
     {
         SENK_CUDA(cudaMemsetAsync(G.p, 0, G.bytes(), s));
         SENK_CUDA(cudaMemsetAsync(acc.p, 0, acc.bytes(), s));
         forward<T>(r, s, true);
         const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
-        k_target<T><<<rg, kThreads, 0, s>>>(e, ilu, rms.p, d, t.p, n, red.p, ticket.p, acc.p);
-        k_decode_train<<<kNumSMs * 4, kThreads, 0, s>>>(H[kLayers].p, P.p, t.p, dH.p, G.p, acc.p, n);
+        k_decode_c<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(H[kLayers].p, P.p, cbuf.p, n);
+        if (loss_mode == 0) {
+            k_target<T><<<rg, kThreads, 0, s>>>(e, ilu, rms.p, d, t.p, n, red.p, ticket.p, acc.p);
+            k_loss_error<<<rg, kThreads, 0, s>>>(cbuf.p, t.p, dcb.p, acc.p, n);
+        } else {
+            k_resid_target<T><<<rg, kThreads, 0, s>>>(r, ailu_dev, rms.p, t.p, acc.p, n);
+            k_spmv_loss<<<rg, kThreads, 0, s>>>(ar.p, ac.p, av.p, cbuf.p, ebuf.p, n, 1.f / d, t.p, acc.p);
+            k_spmv_grad<<<rg, kThreads, 0, s>>>(atr.p, atc.p, atv.p, ebuf.p, dcb.p, n, 1.f / d, acc.p);
+        }
+        k_decode_back<<<kNumSMs * 4, kThreads, 0, s>>>(H[kLayers].p, P.p, dcb.p, dH.p, G.p, n);
         float *dh = dH.p, *dh2 = dH2.p;
         const int tiles = ceil_div(n, 128);
         for (int l = kLayers - 1; l >= 0; l--) {
@@ -561,6 +662,16 @@ int senk_mpnn_set_params(senk_mpnn *net, const float *host, int nparams)
     });
 }
 
+// Training objective: 0 = error space, 1 = residual space (default).
+int senk_mpnn_set_loss(senk_mpnn *net, int mode)
+{
+    return guarded("senk_mpnn_set_loss", [&] {
+        SENK_REQUIRE(net && (mode == 0 || mode == 1), "mode must be 0 or 1");
+        net->net.loss_mode = mode;
+        return (int)kOk;
+    });
+}
+
 int senk_mpnn_bind(senk_mpnn *net, senk_system *sys)
 {
     return guarded("senk_mpnn_bind", [&] {
@@ -592,7 +703,8 @@ int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const
         Mpnn &m = net->net;
         SENK_REQUIRE(m.bound == &S, "bind the network to this system first");
         S.precondition_base(r, S.t.p, nullptr);  // ILU(r) alone
-        m.loss_grad<double>(r, S.t.p, e, S.stream);
+        if (m.loss_mode == 1) S.A.apply(S.t.p, m.ailu.p, S.stream, nullptr);
+        m.loss_grad<double>(r, S.t.p, e, m.ailu.p, S.stream);
         double a[2];
         SENK_CUDA(cudaMemcpyAsync(a, m.acc.p, sizeof(a), cudaMemcpyDeviceToHost, S.stream));
         if (grad) SENK_CUDA(cudaMemcpyAsync(grad, m.G.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost, S.stream));

@@ -61,6 +61,10 @@ class Net:
         p = np.ascontiguousarray(p, np.float32)
         check("senk_mpnn_set_params", lib().senk_mpnn_set_params(self._h, p.ctypes.data_as(C.c_void_p), NPARAMS))
 
+    def set_loss(self, mode: int):
+        """Training objective: 1 = residual space (default), 0 = error space."""
+        check("senk_mpnn_set_loss", lib().senk_mpnn_set_loss(self._h, mode))
+
     def bind(self, sysm: System):
         check("senk_mpnn_bind", lib().senk_mpnn_bind(self._h, sysm._h))
 
@@ -212,3 +216,51 @@ def compare_gcr(net: Net, mb: Member, m: int = 20, eps: float = 1e-8, max_outer:
     Net.detach(sysm)
     sysm.close()
     return out
+
+
+def main(argv=None):
+    """Train on the seeded family and compare flexible GCR(m) with K = ILU + net
+    against plain ILU(0)-GCR(m) on held-out seeds; prints one JSON line.
+
+        python -m senk_gb300.learned --n 32 --train 64 --epochs 2 --test 4
+    """
+    import argparse
+    import json
+
+    import torch
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=32, help="grid points per dimension")
+    ap.add_argument("--train", type=int, default=64, help="training systems (seeds 1000..)")
+    ap.add_argument("--epochs", type=int, default=2)
+    ap.add_argument("--test", type=int, default=4, help="held-out systems (seeds 900000..)")
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--m", type=int, default=20)
+    ap.add_argument("--loss", type=int, default=1, help="1 residual space, 0 error space")
+    ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
+    args = ap.parse_args(argv)
+    net = Net(seed=0)
+    net.set_loss(args.loss)
+    t0 = time.perf_counter()
+    losses = train(torch, net, args.n, range(1000, 1000 + args.train), args.epochs, args.lr)
+    train_s = time.perf_counter() - t0
+    results = []
+    for s in range(900000, 900000 + args.test):
+        results.append(dict(seed=s, **compare_gcr(net, family_member(args.n, s), m=args.m)))
+    if args.save:
+        np.save(args.save, net.params)
+    plain = [r["plain"]["iters"] for r in results]
+    learned = [r["learned"]["iters"] for r in results]
+    out = dict(n=args.n, train_systems=args.train, epochs=args.epochs, pairs=len(losses), train_s=round(train_s, 1),
+               loss_first=float(np.mean(losses[:8])), loss_last=float(np.mean(losses[-8:])),
+               plain_iters=plain, learned_iters=learned,
+               plain_ms=[round(r["plain"]["ms"], 2) for r in results],
+               learned_ms=[round(r["learned"]["ms"], 2) for r in results],
+               learned_true_res=[r["learned"]["true_res"] for r in results],
+               fallback=[r["learned"]["fallback_cycle"] for r in results])
+    print(json.dumps(out))
+    net.close()
+
+
+if __name__ == "__main__":
+    main()

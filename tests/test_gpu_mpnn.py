@@ -89,13 +89,15 @@ def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
         corr_got, corr_want = got - ilu_h, want - ilu_h
         assert rel(corr_got, corr_want) <= 1e-2
         assert rel(got, want) <= 1e-3
-        loss, grad = net.loss_grad(sysm, rd.data_ptr(), ed.data_ptr())
-        lw, gw = M.loss_grad(params, g, r, ilu_h, e, rounding=True)
-        assert abs(loss - lw) <= 1e-3 * lw
-        for lo, hi in [(M.OFF_WIN, M.OFF_LAYER)] + [
-                (M.OFF_LAYER + l * M.LAYER_SIZE, M.OFF_LAYER + (l + 1) * M.LAYER_SIZE) for l in range(M.LAYERS)] + [
-                (M.OFF_WOUT, M.NPARAMS)]:
-            assert rel(grad[lo:hi], gw[lo:hi]) <= 2e-2, (lo, hi, rel(grad[lo:hi], gw[lo:hi]))
+        for mode in (1, 0):
+            net.set_loss(mode)
+            loss, grad = net.loss_grad(sysm, rd.data_ptr(), ed.data_ptr())
+            lw, gw = M.loss_grad(params, g, r, ilu_h, e, rounding=True, mode=mode)
+            assert abs(loss - lw) <= 1e-3 * lw, (mode, loss, lw)
+            for lo, hi in [(M.OFF_WIN, M.OFF_LAYER)] + [
+                    (M.OFF_LAYER + l * M.LAYER_SIZE, M.OFF_LAYER + (l + 1) * M.LAYER_SIZE)
+                    for l in range(M.LAYERS)] + [(M.OFF_WOUT, M.NPARAMS)]:
+                assert rel(grad[lo:hi], gw[lo:hi]) <= 2e-2, (mode, lo, hi, rel(grad[lo:hi], gw[lo:hi]))
     finally:
         net.close()
         sysm.close()
@@ -104,9 +106,9 @@ def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
 def test_training_lowers_the_loss_and_flexible_gcr_converges(torch):
     net = LN.Net(seed=0)
     try:
-        losses = LN.train(torch, net, 16, seeds=range(100, 116), epochs=3, lr=2e-3)
+        losses = LN.train(torch, net, 16, seeds=range(100, 116), epochs=3, lr=1e-3)
         first, last = np.mean(losses[:8]), np.mean(losses[-8:])
-        assert np.isfinite(last) and last < first
+        assert np.isfinite(last) and last < first and last < 1.0
         res = {}
         for s in (900, 901):
             mb = LN.family_member(16, s)

@@ -2,6 +2,7 @@
 pass agrees with finite differences of its forward pass (plain float64), and the
 BF16-rounded variant stays close to the plain one."""
 import numpy as np
+import pytest
 
 from oracle import mpnn as M
 from senk_gb300 import problems as P
@@ -20,16 +21,17 @@ def _case(seed=0):
     return g, r, ilu, e, params
 
 
-def test_backward_matches_finite_differences():
+@pytest.mark.parametrize("mode", [0, 1])
+def test_backward_matches_finite_differences(mode):
     g, r, ilu, e, params = _case()
-    loss, G = M.loss_grad(params, g, r, ilu, e, rounding=False)
+    loss, G = M.loss_grad(params, g, r, ilu, e, rounding=False, mode=mode)
     rng = np.random.default_rng(7)
     eps = 1e-6
     for _ in range(4):
         v = rng.standard_normal(M.NPARAMS)
         v /= np.linalg.norm(v)
-        lp, _ = M.loss_grad(params + eps * v, g, r, ilu, e, rounding=False)
-        lm, _ = M.loss_grad(params - eps * v, g, r, ilu, e, rounding=False)
+        lp, _ = M.loss_grad(params + eps * v, g, r, ilu, e, rounding=False, mode=mode)
+        lm, _ = M.loss_grad(params - eps * v, g, r, ilu, e, rounding=False, mode=mode)
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - G @ v) <= 1e-5 * max(1.0, abs(fd))
     # every parameter block receives gradient
