@@ -405,6 +405,8 @@ int senk_mpnn_bind(senk_mpnn *net, senk_system *sys);
  * loss = |A c / mean(a_ii) - q|^2 / |q|^2 with c = net(r); 0 error space,
  * t = (e - ILU(r)) mean(a_ii) / ||r||_rms, loss = |c - t|^2 / |t|^2. */
 int senk_mpnn_set_loss(senk_mpnn *net, int mode);
+/* Global gradient-norm clip of the Adam steps (default 1; <= 0: off). */
+int senk_mpnn_set_clip(senk_mpnn *net, float clip);
 /* Loss of one residual/error pair; gradient to grad (host, may be NULL). */
 int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const double *e, double *loss,
                         float *grad);

@@ -217,13 +217,26 @@ k_encode_back(const float *fd, const float *fs, const T *r, const float *rms, co
 
 // Adam (decoupled moments, bias-corrected), then the BF16 weight copies:
 // Theta_l (128 x 64) and its transpose (64 x 128).
+// ||G||^2 into *out (one CTA)
+__global__ void __launch_bounds__(1024) k_grad_norm2(const float *G, int np, float *out)
+{
+    float s = 0.f;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += G[i] * G[i];
+    __shared__ float sh[32];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) *out = s;
+}
+
+// Adam with the gradient scaled to global norm at most `clip` (clip <= 0: off).
 __global__ void __launch_bounds__(kThreads)
 k_adam(float *P, const float *G, float *M, float *V, int np, float lr, float b1, float b2, float eps, float c1,
-       float c2)
+       float c2, const float *norm2, float clip)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    const float g = G[i];
+    const float gn = sqrtf(*norm2);
+    const float gs = (clip > 0.f && gn > clip) ? clip / gn : 1.f;
+    const float g = G[i] * gs;
     const float m = b1 * M[i] + (1.f - b1) * g;
     const float v = b2 * V[i] + (1.f - b2) * g * g;
     M[i] = m;
@@ -368,6 +381,8 @@ struct Mpnn {
     DevBuf<float> av, atv, cbuf, dcb, ebuf;
     DevBuf<double> ailu;          // A ILU(r)
     int loss_mode = 1;            // 0: error space, 1: residual space
+    float clip = 1.0f;            // global gradient-norm clip of the Adam step (<= 0: off)
+    DevBuf<float> gnorm;
     // activations
     DevBuf<bf16> X[kLayers], Z[kLayers], dZ;
     DevBuf<float> H[kLayers + 1], dH, dH2, dM, t;
@@ -389,6 +404,7 @@ struct Mpnn {
         SENK_CUDA(cudaMemset(V.p, 0, V.bytes()));
         status.alloc(1);
         SENK_CUDA(cudaMemset(status.p, 0, sizeof(int)));
+        gnorm.alloc(1);
         rms.alloc(2);
         red.alloc(kNumSMs * 4);
         acc.alloc(2);
@@ -573,7 +589,9 @@ struct Mpnn {
         step++;
         const float b1 = 0.9f, b2 = 0.999f;
         const float c1 = 1.f / (1.f - std::pow(b1, (float)step)), c2 = 1.f / (1.f - std::pow(b2, (float)step));
-        k_adam<<<ceil_div(kParams, kThreads), kThreads, 0, s>>>(P.p, G.p, M.p, V.p, kParams, lr, b1, b2, 1e-8f, c1, c2);
+        k_grad_norm2<<<1, 1024, 0, s>>>(G.p, kParams, gnorm.p);
+        k_adam<<<ceil_div(kParams, kThreads), kThreads, 0, s>>>(P.p, G.p, M.p, V.p, kParams, lr, b1, b2, 1e-8f, c1, c2,
+                                                                gnorm.p, clip);
         refresh_weights(s);
     }
 
@@ -668,6 +686,16 @@ int senk_mpnn_set_loss(senk_mpnn *net, int mode)
     return guarded("senk_mpnn_set_loss", [&] {
         SENK_REQUIRE(net && (mode == 0 || mode == 1), "mode must be 0 or 1");
         net->net.loss_mode = mode;
+        return (int)kOk;
+    });
+}
+
+// Global gradient-norm clip of the Adam steps (default 1; <= 0 turns it off).
+int senk_mpnn_set_clip(senk_mpnn *net, float clip)
+{
+    return guarded("senk_mpnn_set_clip", [&] {
+        SENK_REQUIRE(net, "null network");
+        net->net.clip = clip;
         return (int)kOk;
     });
 }

@@ -234,13 +234,15 @@ def main(argv=None):
     ap.add_argument("--train", type=int, default=64, help="training systems (seeds 1000..)")
     ap.add_argument("--epochs", type=int, default=2)
     ap.add_argument("--test", type=int, default=4, help="held-out systems (seeds 900000..)")
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=3e-4)
+    ap.add_argument("--clip", type=float, default=1.0)
     ap.add_argument("--m", type=int, default=20)
     ap.add_argument("--loss", type=int, default=1, help="1 residual space, 0 error space")
     ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
     args = ap.parse_args(argv)
     net = Net(seed=0)
     net.set_loss(args.loss)
+    check("senk_mpnn_set_clip", lib().senk_mpnn_set_clip(net._h, args.clip))
     t0 = time.perf_counter()
     losses = train(torch, net, args.n, range(1000, 1000 + args.train), args.epochs, args.lr)
     train_s = time.perf_counter() - t0
