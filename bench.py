@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "solve ms to 1e-8 FP64 true rel. residual (ABMC-ILU(0) GMRES(30), mixed-precision GMRES-IR)"
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ilu_apply_traffic_convdiff128.md")
 
 
 def parse():
@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
     ap.add_argument("--no-kernels", action="store_true", help="skip the per-kernel timings (profiling runs)")
     ap.add_argument("--only", default="both", choices=["both", "mixed", "plain"], help="which solves to time")
     ap.add_argument("--inner-tol", type=float, default=1e-4)
@@ -154,12 +155,41 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def learned_leg(n=16, train_seeds=range(100, 116), test_seeds=(900, 901, 902), epochs=3):
+    """Plain ILU(0)-GCR(20) against flexible GCR(20) with K = ILU + net on held-out
+    systems of the variable-coefficient family (n^3), the network trained on the
+    GPU first (residual-space objective, Adam 3e-4, clipped)."""
+    import torch
+
+    from senk_gb300 import learned as LN
+    net = LN.Net(seed=0)
+    t0 = time.perf_counter()
+    losses = LN.train(torch, net, n, train_seeds, epochs, 3e-4)
+    train_s = time.perf_counter() - t0
+    rows = [LN.compare_gcr(net, LN.family_member(n, s), m=20) for s in test_seeds]
+    net.close()
+    return {"family": f"vardiff3d {n}^3, sigma~U[0.5,2], corr~U[4,16], ABMC 16, ILU(0), GCR(20), 1e-8",
+            "train_systems": len(train_seeds), "epochs": epochs, "pairs": len(losses), "train_s": round(train_s, 2),
+            "loss_first": float(np.mean(losses[:8])), "loss_last": float(np.mean(losses[-8:])),
+            "plain_iters": [r["plain"]["iters"] for r in rows], "learned_iters": [r["learned"]["iters"] for r in rows],
+            "plain_ms": [round(r["plain"]["ms"], 3) for r in rows],
+            "learned_ms": [round(r["learned"]["ms"], 3) for r in rows],
+            "learned_true_res": [r["learned"]["true_res"] for r in rows],
+            "fallback_cycle": [r["learned"]["fallback_cycle"] for r in rows]}
+
+
 def traffic_for(kernel):
+    """DRAM bytes (read + write) of one launch of `kernel`, from the ncu summary's
+    `traffic <kernel> <bytes>` lines."""
     try:
         with open(PROFILE_TRAFFIC) as f:
-            return json.load(f).get(kernel)
+            for ln in f:
+                parts = ln.strip().strip("`").split()
+                if len(parts) == 3 and parts[0] == "traffic" and parts[1] == kernel:
+                    return int(parts[2])
     except (OSError, ValueError):
-        return None
+        pass
+    return None
 
 
 def cpu_solve(port, Ar, Lf, Uf, nc, sc, b, eps, m, threads):
@@ -273,6 +303,9 @@ def run_gpu(args, rank, world):
                "h2d_bytes_per_step": int(rr.h2d_bytes), "d2h_bytes_per_step": int(rr.d2h_bytes),
                "steps": len(e2e_ms), "iterations": rr.iters,
                "note": "drop-in C ABI call senk_abmc_ilu_gmres_ir_d with host arrays; wall clock"}
+    learned = None
+    if not args.no_learned and rank == 0:
+        learned = learned_leg()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -312,6 +345,7 @@ def run_gpu(args, rank, world):
                      "bytes_per_launch": kern[dom + "_bytes"], "ms_per_launch": kern[dom + "_ms"]},
         "kernels": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in kern.items()},
         "cpu_baseline": cpu,
+        "learned": learned,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
