@@ -67,8 +67,14 @@ typedef struct {
 typedef struct {
     int orth;         /* SENK_ORTH_* */
     int spmv;         /* SENK_SPMV_* */
-    int verbose;      /* print the reference's stdout lines */
+    int verbose;      /* print the reference's stdout lines (2: also setup timings) */
+    int sweep;        /* SENK_SWEEP_* */
 } senk_options;
+
+/* How the ILU sweeps of ABMC chains (bsize >= 2) are scheduled. */
+#define SENK_SWEEP_AUTO 0     /* one dataflow launch per sweep: groups of chains wait
+                                 on per-group flags of the groups they read */
+#define SENK_SWEEP_COLOURS 1  /* one launch per colour */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0

@@ -158,6 +158,10 @@ struct SweepFactor {
     std::vector<size_t> colour_smem; // bytes to stage the largest group of each colour
     long long elems = 0;           // padded slots
     long long nnz = 0;             // stored off-diagonal entries (+N for U's diagonal)
+    // dataflow sweep (chains of bs >= 2 rows): the groups each group reads from
+    bool dataflow = false;
+    DevBuf<int> dep_ptr, dep_idx, flags, ctrl;
+    int df_grid = 0;
 };
 
 // A split ILU factorisation with its sweep schedule.
@@ -168,8 +172,11 @@ struct IluPlan {
     SweepFactor<VT> L, U;
     DevBuf<int> status;  // set to 1 by a sweep whose TMA wait ran out
 
+    // sweep_mode: SENK_SWEEP_AUTO (dataflow sweeps for chains of 2+ rows) or
+    // SENK_SWEEP_COLOURS (one launch per colour)
     void build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
-               const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s);
+               const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s,
+               int sweep_mode = 0);
     template <typename XT>
     void sweep(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate) const;
     template <typename XT>

@@ -642,4 +642,123 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     if (live) y[row] = tsh[l][q];
 }
 
+// ------------------------------------------------------ dataflow sweeps
+// One launch per triangular sweep: CTAs take groups in processing order from a
+// counter, wait until every group their rows read from has published its flag
+// for this sweep, solve the group as k_sweep does, and publish their own flag.
+// A group only reads groups of earlier colours, which were taken earlier by
+// running CTAs, so every wait ends. ctrl = {counter, epoch, abort}: the epoch
+// numbers the sweeps (flags hold the epoch of the sweep that set them), a wait
+// that runs out of polls sets abort and *status, and every later wait gives up
+// at once.
+constexpr unsigned kFlagPolls = 1u << 20;
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Starts a sweep: new epoch, counter back to 0 (one thread).
+static __global__ void k_df_begin(int *ctrl)
+{
+    ctrl[0] = 0;
+    ctrl[1] += 1;
+}
+
+template <typename VT, typename XT, int BS, bool UPPER>
+__global__ void __launch_bounds__(BS * 32)
+k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__restrict__ widths,
+           const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
+           const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl, const XT *x,
+           XT *y, const int *gate, int *status)
+{
+    static_assert(BS >= 2, "dataflow sweeps are for chains of two or more rows");
+    __shared__ XT tsh[BS][32];
+    __shared__ XT dsh[UPPER ? BS : 1][32];
+    __shared__ int wsh[2 * BS];
+    __shared__ int item;
+    if (gated(gate)) return;
+    const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
+    const int epoch = *(volatile const int *)(ctrl + 1);
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(ctrl, 1);
+        __syncthreads();
+        const int g = item;
+        if (g >= ng) return;
+        if (threadIdx.x < 2 * BS) wsh[threadIdx.x] = widths[(size_t)g * 2 * BS + threadIdx.x];
+        const GroupDesc d = groups[g];
+        // wait for the groups this one reads from
+        bool bad = false;
+        for (int i = dep_ptr[g] + threadIdx.x; i < dep_ptr[g + 1] && !bad; i += blockDim.x) {
+            const int *f = flags + dep_idx[i];
+            unsigned k = 0;
+            while (ld_acquire(f) != epoch) {
+                if (++k > kFlagPolls || *(volatile const int *)(ctrl + 2)) {
+                    atomicExch(ctrl + 2, 1);
+                    atomicExch(status, 1);
+                    bad = true;
+                    break;
+                }
+            }
+        }
+        if (__syncthreads_or(bad)) return;
+        int eo = 0, etot = 0;
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+            if (r < l) eo += wsh[r];
+            etot += wsh[r];
+        }
+        const VT *vb = val + d.off;
+        const int *cb = col + d.off;
+        const bool live = q < d.nchains;
+        const int pos = d.pos0 + q * BS + l;
+        XT t = live ? x[pos] : XT(0);
+        const int we = wsh[l];
+        for (int k = 0; k < we; k++) {
+            const int at = (eo + k) * 32 + q;
+            const int c = ld_stream(cb + at);
+            const VT v = ld_stream(vb + at);
+            if (c >= 0) t -= (XT)v * __ldcg(y + c);  // L2: written by other SMs in this launch
+        }
+        tsh[l][q] = t;
+        if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
+        __syncthreads();
+        if (l == 0) {
+            int io = etot;
+            int ioff[BS];
+#pragma unroll
+            for (int r = 0; r < BS; r++) {
+                ioff[r] = io;
+                io += wsh[BS + r];
+            }
+#pragma unroll
+            for (int st = 0; st < BS; st++) {
+                const int r = UPPER ? BS - 1 - st : st;
+                XT tt = tsh[r][q];
+                const int wi = wsh[BS + r];
+                for (int k = 0; k < wi; k++) {
+                    const int at = (ioff[r] + k) * 32 + q;
+                    const int c = ld_stream(cb + at);
+                    const VT v = ld_stream(vb + at);
+                    if (c >= 0) tt -= (XT)v * tsh[c][q];
+                }
+                if (UPPER) tt *= dsh[r][q];
+                tsh[r][q] = tt;
+            }
+        }
+        __syncthreads();
+        if (live) y[pos] = tsh[l][q];
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) st_release(flags + g, epoch);
+    }
+}
+
 }  // namespace senkgpu

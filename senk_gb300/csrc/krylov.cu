@@ -101,7 +101,7 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     } else if (d.precond != SENK_PC_NONE) {
         pc = std::make_unique<IluPlan<T>>();
         pc->build(n, (const T *)d.lval, d.lcind, d.lrptr, (const T *)d.uval, d.ucind, d.urptr, d.precond, d.cptr,
-                  d.cnum, d.bsize, stream);
+                  d.cnum, d.bsize, stream, opt.sweep);
     }
     clk.lap("preconditioner plan");
     b.alloc(n);

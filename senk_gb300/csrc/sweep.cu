@@ -25,10 +25,15 @@ struct Group {
     int p0, p1;  // schedule positions [p0, p1)
 };
 
+// The groups each group reads from (dataflow sweeps), and the launch size.
+template <typename VT>
+void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> &gd, int bs, const int *cind,
+                        const int *rptr, bool upper, cudaStream_t s);
+
 template <typename VT>
 void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
                   const std::vector<Group> &groups, const std::vector<int> *rowmap, int bs,
-                  const std::vector<int> *group_of_row, cudaStream_t s)
+                  const std::vector<int> *group_of_row, cudaStream_t s, int sweep_mode = SENK_SWEEP_AUTO)
 {
     F.upper = upper;
     F.mapped = rowmap != nullptr;
@@ -173,7 +178,54 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.groups.upload(gd.data(), ng, s);
     F.widths.alloc(wd.size());
     F.widths.upload(wd.data(), wd.size(), s);
+    F.dataflow = chains && sweep_mode == SENK_SWEEP_AUTO;
+    if (F.dataflow) build_dependencies(F, N, gd, bs, cind, rptr, upper, s);
     // Host vectors are released on return: finish the copies first.
+    SENK_CUDA(cudaStreamSynchronize(s));
+}
+
+template <typename VT>
+void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> &gd, int bs, const int *cind,
+                        const int *rptr, bool upper, cudaStream_t s)
+{
+    const int ng = (int)gd.size();
+    std::vector<int> owner(N, -1);
+    for (int i = 0; i < ng; i++)
+        for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) owner[p] = i;
+    std::vector<std::vector<int>> deps(ng);
+    int bad = -1;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < ng; i++) {
+        std::vector<int> &dv = deps[i];
+        for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) {
+            const int cs = p - p % bs, ce = cs + bs;
+            for (int j = rptr[p] + (upper ? 1 : 0); j < rptr[p + 1]; j++) {
+                const int c = cind[j];
+                if (c >= cs && c < ce) continue;  // in-chain
+                const int o = owner[c];
+                if (o < 0 || o >= i) {
+#pragma omp atomic write
+                    bad = i;
+                }
+                dv.push_back(o);
+            }
+        }
+        std::sort(dv.begin(), dv.end());
+        dv.erase(std::unique(dv.begin(), dv.end()), dv.end());
+    }
+    SENK_REQUIRE(bad < 0, "group " + std::to_string(bad) + " reads a group that is not solved before it");
+    std::vector<int> ptr(ng + 1, 0), idx;
+    for (int i = 0; i < ng; i++) ptr[i + 1] = ptr[i] + (int)deps[i].size();
+    idx.reserve(ptr[ng]);
+    for (int i = 0; i < ng; i++) idx.insert(idx.end(), deps[i].begin(), deps[i].end());
+    F.dep_ptr.alloc(ptr.size());
+    F.dep_ptr.upload(ptr.data(), ptr.size(), s);
+    F.dep_idx.alloc(std::max<size_t>(idx.size(), 1));
+    F.dep_idx.upload(idx.data(), idx.size(), s);
+    F.flags.alloc(std::max(ng, 1));
+    SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
+    F.ctrl.alloc(4);
+    SENK_CUDA(cudaMemsetAsync(F.ctrl.p, 0, F.ctrl.bytes(), s));
     SENK_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -252,10 +304,37 @@ void allow_smem()
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStagedBytes));
 }
 
+template <typename VT, typename XT, int BS, bool UPPER>
+void launch_dataflow(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
+{
+    const int ng = F.colour_groups.back();
+    if (ng == 0) return;
+    auto kern = k_sweep_df<VT, XT, BS, UPPER>;
+    static int per_sm = -1;  // resident CTAs per SM (the same for every factor of this shape)
+    if (per_sm < 0) SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 0));
+    const int grid = std::max(1, std::min(ng, per_sm * kNumSMs));
+    k_df_begin<<<1, 1, 0, s>>>(F.ctrl.p);
+    kern<<<grid, BS * 32, 0, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
+                                  (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, F.dep_ptr.p,
+                                  F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status);
+    SENK_LAUNCH_CHECK();
+}
+
 template <typename VT, typename XT, bool UPPER>
 void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
     const int nc = (int)F.colour_groups.size() - 1;
+    if (F.dataflow) {
+        switch (F.bs) {
+        case 2: launch_dataflow<VT, XT, 2, UPPER>(F, status, x, y, s, gate); break;
+        case 4: launch_dataflow<VT, XT, 4, UPPER>(F, status, x, y, s, gate); break;
+        case 8: launch_dataflow<VT, XT, 8, UPPER>(F, status, x, y, s, gate); break;
+        case 16: launch_dataflow<VT, XT, 16, UPPER>(F, status, x, y, s, gate); break;
+        case 32: launch_dataflow<VT, XT, 32, UPPER>(F, status, x, y, s, gate); break;
+        default: throw ArgError("unsupported chain length");
+        }
+        return;
+    }
     for (int c = 0; c < nc; c++) {
         if (F.mapped) {
             launch_colour<VT, XT, 1, UPPER, true>(F, status, c, x, y, s, gate);
@@ -290,8 +369,9 @@ void allow_all_smem()
 template <typename VT>
 void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval,
                         const int *ucind, const int *urptr, int pckind, const int *cptr, int cnum, int bsize,
-                        cudaStream_t s)
+                        cudaStream_t s, int sweep_mode)
 {
+    SENK_REQUIRE(sweep_mode == SENK_SWEEP_AUTO || sweep_mode == SENK_SWEEP_COLOURS, "unknown sweep mode");
     SENK_REQUIRE(N > 0, "N must be positive");
     SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
     n = N;
@@ -322,10 +402,10 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
+    build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s, sweep_mode);
     // For U, "earlier" means a later colour: flip the colour numbers.
     for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
-    build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
+    build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s, sweep_mode);
 }
 
 template <typename VT>

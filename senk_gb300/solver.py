@@ -17,8 +17,8 @@ from .lib import (F32, F64, PC_ILU, PC_ILU_ABMC, PC_ILU_AMC, PC_NONE, Options, R
 from .problems import Csr
 
 
-def _opts(orth=0, spmv=0, verbose=False):
-    return Options(orth, spmv, int(verbose))
+def _opts(orth=0, spmv=0, verbose=False, sweep=0):
+    return Options(orth, spmv, int(verbose), sweep)
 
 
 def _T(x):
