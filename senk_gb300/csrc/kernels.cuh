@@ -680,6 +680,7 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
            XT *y, const int *gate, int *status)
 {
     static_assert(BS >= 2, "dataflow sweeps are for chains of two or more rows");
+    extern __shared__ __align__(16) unsigned char dfs[];  // the group's values, then its columns
     __shared__ XT tsh[BS][32];
     __shared__ XT dsh[UPPER ? BS : 1][32];
     __shared__ int wsh[2 * BS];
@@ -694,12 +695,26 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
         if (g >= ng) return;
         if (threadIdx.x < 2 * BS) wsh[threadIdx.x] = widths[(size_t)g * 2 * BS + threadIdx.x];
         const GroupDesc d = groups[g];
+        __syncthreads();
+        int slots = 0;
+#pragma unroll
+        for (int r = 0; r < 2 * BS; r++) slots += wsh[r];
+        // stage the group's block (contiguous values and columns, 16-byte
+        // chunks) while the dependencies are being waited for
+        const int vchunks = slots * 32 * (int)sizeof(VT) / 16, cchunks = slots * 32 * 4 / 16;
+        const uint4 *gv = reinterpret_cast<const uint4 *>(val + d.off);
+        const uint4 *gc = reinterpret_cast<const uint4 *>(col + d.off);
+        uint4 *sv4 = reinterpret_cast<uint4 *>(dfs);
+        uint4 *sc4 = reinterpret_cast<uint4 *>(dfs + (size_t)slots * 32 * sizeof(VT));
+        for (int i = threadIdx.x; i < vchunks; i += blockDim.x) sv4[i] = ld_stream(gv + i);
+        for (int i = threadIdx.x; i < cchunks; i += blockDim.x) sc4[i] = ld_stream(gc + i);
         // wait for the groups this one reads from
         bool bad = false;
         for (int i = dep_ptr[g] + threadIdx.x; i < dep_ptr[g + 1] && !bad; i += blockDim.x) {
             const int *f = flags + dep_idx[i];
             unsigned k = 0;
             while (ld_acquire(f) != epoch) {
+                __nanosleep(128);  // back off: spinning CTAs must not crowd out the producers' traffic
                 if (++k > kFlagPolls || *(volatile const int *)(ctrl + 2)) {
                     atomicExch(ctrl + 2, 1);
                     atomicExch(status, 1);
@@ -715,16 +730,16 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
             if (r < l) eo += wsh[r];
             etot += wsh[r];
         }
-        const VT *vb = val + d.off;
-        const int *cb = col + d.off;
+        const VT *vb = reinterpret_cast<const VT *>(dfs);
+        const int *cb = reinterpret_cast<const int *>(dfs + (size_t)slots * 32 * sizeof(VT));
         const bool live = q < d.nchains;
         const int pos = d.pos0 + q * BS + l;
         XT t = live ? x[pos] : XT(0);
         const int we = wsh[l];
         for (int k = 0; k < we; k++) {
             const int at = (eo + k) * 32 + q;
-            const int c = ld_stream(cb + at);
-            const VT v = ld_stream(vb + at);
+            const int c = cb[at];
+            const VT v = vb[at];
             if (c >= 0) t -= (XT)v * __ldcg(y + c);  // L2: written by other SMs in this launch
         }
         tsh[l][q] = t;
@@ -745,8 +760,8 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
                 const int wi = wsh[BS + r];
                 for (int k = 0; k < wi; k++) {
                     const int at = (ioff[r] + k) * 32 + q;
-                    const int c = ld_stream(cb + at);
-                    const VT v = ld_stream(vb + at);
+                    const int c = cb[at];
+                    const VT v = vb[at];
                     if (c >= 0) tt -= (XT)v * tsh[c][q];
                 }
                 if (UPPER) tt *= dsh[r][q];

@@ -310,11 +310,14 @@ void launch_dataflow(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, 
     const int ng = F.colour_groups.back();
     if (ng == 0) return;
     auto kern = k_sweep_df<VT, XT, BS, UPPER>;
-    static int per_sm = -1;  // resident CTAs per SM (the same for every factor of this shape)
-    if (per_sm < 0) SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 0));
-    const int grid = std::max(1, std::min(ng, per_sm * kNumSMs));
+    size_t smem = 0;  // the widest group's block
+    for (size_t b : F.colour_smem) smem = std::max(smem, b);
+    SENK_REQUIRE(smem <= kMaxStagedBytes, "a group's factor block exceeds the shared memory of the dataflow sweep");
+    int per_sm = 0;
+    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, smem));
+    const int grid = std::max(1, std::min(ng, std::max(per_sm, 1) * kNumSMs));
     k_df_begin<<<1, 1, 0, s>>>(F.ctrl.p);
-    kern<<<grid, BS * 32, 0, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
+    kern<<<grid, BS * 32, smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
                                   (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, F.dep_ptr.p,
                                   F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status);
     SENK_LAUNCH_CHECK();
@@ -352,9 +355,20 @@ void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cud
     }
 }
 
+template <typename VT, typename XT, int BS>
+void allow_df_smem()
+{
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kMaxStagedBytes));
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kMaxStagedBytes));
+}
+
 template <typename VT, typename XT>
 void allow_all_smem()
 {
+    allow_df_smem<VT, XT, 2>(); allow_df_smem<VT, XT, 4>(); allow_df_smem<VT, XT, 8>();
+    allow_df_smem<VT, XT, 16>(); allow_df_smem<VT, XT, 32>();
     allow_smem<VT, XT, 1, false, true>(); allow_smem<VT, XT, 1, true, true>();
     allow_smem<VT, XT, 1, false, false>(); allow_smem<VT, XT, 1, true, false>();
     allow_smem<VT, XT, 2, false, false>(); allow_smem<VT, XT, 2, true, false>();
