@@ -128,3 +128,29 @@ def test_nonconvergence_reports_outer_times_m(c1):
     x = np.zeros(A.n)
     r = SV.Gmresm(A.val, A.cind, A.rptr, b, x, nb, 2, 10, A.n, 1e-8)
     assert not r.converged and r.iters == 20 and r.cycles == 2
+
+
+@pytest.mark.parametrize("sweep", [L.SWEEP_COLOURS, L.SWEEP_DATAFLOW])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_c1_abmc_sweep_schedules(port, golden, c1, sweep, dtype):
+    """Both schedules of the ABMC sweeps (one launch per colour, one dataflow
+    launch per sweep) in both precisions give the reference's iteration count."""
+    A, b, nb = c1
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    L_, U_, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
+    br = b[LP]
+    sy = SV.System(Ar, L_, U_, L.PC_ILU_ABMC, sc, nc, 16, dtype=dtype, m_max=30, sweep=sweep)
+    try:
+        sy.set_rhs(br)
+        eps = 1e-8 if dtype == np.float64 else 1e-5
+        r = sy.gmres(nb, 10000 // 30, 30, eps)
+        x = sy.get_x().astype(np.float64)
+        assert r.converged
+        if dtype == np.float64:
+            assert abs(r.iters - golden["c1"]["AbmcIluGmresm_m30"]["iters"]) <= 2
+            assert port.relative_residual(Ar, br, x) < 2e-8
+        else:
+            assert port.relative_residual(Ar, br, x) < 1e-4
+    finally:
+        sy.close()
