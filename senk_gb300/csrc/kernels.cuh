@@ -677,37 +677,47 @@ __global__ void __launch_bounds__(BS * 32)
 k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__restrict__ widths,
            const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
            const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl, const XT *x,
-           XT *y, const int *gate, int *status)
+           XT *y, const int *gate, int *status, unsigned buf_bytes)
 {
     static_assert(BS >= 2, "dataflow sweeps are for chains of two or more rows");
-    extern __shared__ __align__(16) unsigned char dfs[];  // the group's values, then its columns
+    // Two staging buffers of buf_bytes (values, then columns, of one group):
+    // while warp 0 solves the current group's chains, warps 1.. fetch the next
+    // group and stage its block into the other buffer.
+    extern __shared__ __align__(16) unsigned char dfs[];
     __shared__ XT tsh[BS][32];
     __shared__ XT dsh[UPPER ? BS : 1][32];
-    __shared__ int wsh[2 * BS];
-    __shared__ int item;
+    __shared__ int wsh[2][2 * BS];
+    __shared__ GroupDesc dd[2];
+    __shared__ int item[2];
     if (gated(gate)) return;
     const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
     const int epoch = *(volatile const int *)(ctrl + 1);
-    for (;;) {
-        if (threadIdx.x == 0) item = atomicAdd(ctrl, 1);
-        __syncthreads();
-        const int g = item;
-        if (g >= ng) return;
-        if (threadIdx.x < 2 * BS) wsh[threadIdx.x] = widths[(size_t)g * 2 * BS + threadIdx.x];
-        const GroupDesc d = groups[g];
-        __syncthreads();
+    // stage group g into buffer b (threads [t0, t0 + nt) of the CTA)
+    auto stage = [&](int g, int b, int t0, int nt) {
         int slots = 0;
 #pragma unroll
-        for (int r = 0; r < 2 * BS; r++) slots += wsh[r];
-        // stage the group's block (contiguous values and columns, 16-byte
-        // chunks) while the dependencies are being waited for
+        for (int r = 0; r < 2 * BS; r++) slots += wsh[b][r];
         const int vchunks = slots * 32 * (int)sizeof(VT) / 16, cchunks = slots * 32 * 4 / 16;
-        const uint4 *gv = reinterpret_cast<const uint4 *>(val + d.off);
-        const uint4 *gc = reinterpret_cast<const uint4 *>(col + d.off);
-        uint4 *sv4 = reinterpret_cast<uint4 *>(dfs);
-        uint4 *sc4 = reinterpret_cast<uint4 *>(dfs + (size_t)slots * 32 * sizeof(VT));
-        for (int i = threadIdx.x; i < vchunks; i += blockDim.x) sv4[i] = ld_stream(gv + i);
-        for (int i = threadIdx.x; i < cchunks; i += blockDim.x) sc4[i] = ld_stream(gc + i);
+        const uint4 *gv = reinterpret_cast<const uint4 *>(val + dd[b].off);
+        const uint4 *gc = reinterpret_cast<const uint4 *>(col + dd[b].off);
+        unsigned char *base = dfs + (size_t)b * buf_bytes;
+        uint4 *sv4 = reinterpret_cast<uint4 *>(base);
+        uint4 *sc4 = reinterpret_cast<uint4 *>(base + (size_t)slots * 32 * sizeof(VT));
+        for (int i = threadIdx.x - t0; i < vchunks; i += nt) sv4[i] = ld_stream(gv + i);
+        for (int i = threadIdx.x - t0; i < cchunks; i += nt) sc4[i] = ld_stream(gc + i);
+    };
+    // prologue: the first group
+    if (threadIdx.x == 0) item[0] = atomicAdd(ctrl, 1);
+    __syncthreads();
+    if (item[0] >= ng) return;
+    if (threadIdx.x < 2 * BS) wsh[0][threadIdx.x] = widths[(size_t)item[0] * 2 * BS + threadIdx.x];
+    if (threadIdx.x == 0) dd[0] = groups[item[0]];
+    __syncthreads();
+    stage(item[0], 0, 0, blockDim.x);
+    int cur = 0;
+    for (;;) {
+        const int g = item[cur];
+        const GroupDesc d = dd[cur];
         // wait for the groups this one reads from
         bool bad = false;
         for (int i = dep_ptr[g] + threadIdx.x; i < dep_ptr[g + 1] && !bad; i += blockDim.x) {
@@ -723,19 +733,23 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
                 }
             }
         }
-        if (__syncthreads_or(bad)) return;
-        int eo = 0, etot = 0;
+        if (threadIdx.x == 0) item[cur ^ 1] = atomicAdd(ctrl, 1);  // the next group
+        if (__syncthreads_or(bad)) return;  // (also: the staged block and item[cur ^ 1] are visible)
+        int eo = 0, etot = 0, slots = 0;
 #pragma unroll
         for (int r = 0; r < BS; r++) {
-            if (r < l) eo += wsh[r];
-            etot += wsh[r];
+            if (r < l) eo += wsh[cur][r];
+            etot += wsh[cur][r];
         }
-        const VT *vb = reinterpret_cast<const VT *>(dfs);
-        const int *cb = reinterpret_cast<const int *>(dfs + (size_t)slots * 32 * sizeof(VT));
+#pragma unroll
+        for (int r = 0; r < 2 * BS; r++) slots += wsh[cur][r];
+        const unsigned char *base = dfs + (size_t)cur * buf_bytes;
+        const VT *vb = reinterpret_cast<const VT *>(base);
+        const int *cb = reinterpret_cast<const int *>(base + (size_t)slots * 32 * sizeof(VT));
         const bool live = q < d.nchains;
         const int pos = d.pos0 + q * BS + l;
         XT t = live ? x[pos] : XT(0);
-        const int we = wsh[l];
+        const int we = wsh[cur][l];
         for (int k = 0; k < we; k++) {
             const int at = (eo + k) * 32 + q;
             const int c = cb[at];
@@ -745,19 +759,20 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
         tsh[l][q] = t;
         if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
         __syncthreads();
+        const int gn = item[cur ^ 1];
         if (l == 0) {
             int io = etot;
             int ioff[BS];
 #pragma unroll
             for (int r = 0; r < BS; r++) {
                 ioff[r] = io;
-                io += wsh[BS + r];
+                io += wsh[cur][BS + r];
             }
 #pragma unroll
             for (int st = 0; st < BS; st++) {
                 const int r = UPPER ? BS - 1 - st : st;
                 XT tt = tsh[r][q];
-                const int wi = wsh[BS + r];
+                const int wi = wsh[cur][BS + r];
                 for (int k = 0; k < wi; k++) {
                     const int at = (ioff[r] + k) * 32 + q;
                     const int c = cb[at];
@@ -767,12 +782,21 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
                 if (UPPER) tt *= dsh[r][q];
                 tsh[r][q] = tt;
             }
+        } else if (gn < ng) {
+            // warps 1..BS-1: describe and stage the next group
+            const int t = threadIdx.x - 32;
+            if (t < 2 * BS) wsh[cur ^ 1][t] = widths[(size_t)gn * 2 * BS + t];
+            if (t == 0) dd[cur ^ 1] = groups[gn];
+            asm volatile("bar.sync 1, %0;" ::"r"((BS - 1) * 32) : "memory");
+            stage(gn, cur ^ 1, 32, (BS - 1) * 32);
         }
         __syncthreads();
         if (live) y[pos] = tsh[l][q];
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) st_release(flags + g, epoch);
+        if (gn >= ng) return;
+        cur ^= 1;
     }
 }
 

@@ -316,14 +316,17 @@ void launch_dataflow(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, 
     auto kern = k_sweep_df<VT, XT, BS, UPPER>;
     size_t smem = 0;  // the widest group's block
     for (size_t b : F.colour_smem) smem = std::max(smem, b);
-    SENK_REQUIRE(smem <= kMaxStagedBytes, "a group's factor block exceeds the shared memory of the dataflow sweep");
+    smem = (smem + 15) / 16 * 16;
+    SENK_REQUIRE(2 * smem <= kMaxStagedBytes,
+                 "a group's factor block exceeds the shared memory of the dataflow sweep");
     int per_sm = 0;
-    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, smem));
+    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 2 * smem));
     const int grid = std::max(1, std::min(ng, std::max(per_sm, 1) * kNumSMs));
     k_df_begin<<<1, 1, 0, s>>>(F.ctrl.p);
-    kern<<<grid, BS * 32, smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
-                                  (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, F.dep_ptr.p,
-                                  F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status);
+    kern<<<grid, BS * 32, 2 * smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
+                                      (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p,
+                                      F.dep_ptr.p, F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status,
+                                      (unsigned)smem);
     SENK_LAUNCH_CHECK();
 }
 
