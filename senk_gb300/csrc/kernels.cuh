@@ -672,18 +672,14 @@ static __global__ void k_df_begin(int *ctrl)
     ctrl[1] += 1;
 }
 
-// WARPS warps per CTA, each taking BS / WARPS rows of the 32 chains in phase 1
-// (fewer threads per group than k_sweep: more groups resident per SM).
-template <typename VT, typename XT, int BS, int WARPS, bool UPPER>
-__global__ void __launch_bounds__(WARPS * 32)
+template <typename VT, typename XT, int BS, bool UPPER>
+__global__ void __launch_bounds__(BS * 32)
 k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__restrict__ widths,
            const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
            const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl, const XT *x,
            XT *y, const int *gate, int *status, unsigned buf_bytes)
 {
     static_assert(BS >= 2, "dataflow sweeps are for chains of two or more rows");
-    static_assert(WARPS >= 2 && BS % WARPS == 0, "WARPS must divide BS and be at least 2");
-    constexpr int RPW = BS / WARPS;  // rows of each chain per warp
     // Two staging buffers of buf_bytes (values, then columns, of one group):
     // while warp 0 solves the current group's chains, warps 1.. fetch the next
     // group and stage its block into the other buffer.
@@ -739,35 +735,29 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
         }
         if (threadIdx.x == 0) item[cur ^ 1] = atomicAdd(ctrl, 1);  // the next group
         if (__syncthreads_or(bad)) return;  // (also: the staged block and item[cur ^ 1] are visible)
-        int etot = 0, slots = 0;
+        int eo = 0, etot = 0, slots = 0;
 #pragma unroll
-        for (int r = 0; r < BS; r++) etot += wsh[cur][r];
+        for (int r = 0; r < BS; r++) {
+            if (r < l) eo += wsh[cur][r];
+            etot += wsh[cur][r];
+        }
 #pragma unroll
         for (int r = 0; r < 2 * BS; r++) slots += wsh[cur][r];
         const unsigned char *base = dfs + (size_t)cur * buf_bytes;
         const VT *vb = reinterpret_cast<const VT *>(base);
         const int *cb = reinterpret_cast<const int *>(base + (size_t)slots * 32 * sizeof(VT));
         const bool live = q < d.nchains;
-        // phase 1: rows l = warp + WARPS * rr of every chain
-#pragma unroll
-        for (int rr = 0; rr < RPW; rr++) {
-            const int lr = l + WARPS * rr;
-            int eo = 0;
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-                if (r < lr) eo += wsh[cur][r];
-            const int pos = d.pos0 + q * BS + lr;
-            XT t = live ? x[pos] : XT(0);
-            const int we = wsh[cur][lr];
-            for (int k = 0; k < we; k++) {
-                const int at = (eo + k) * 32 + q;
-                const int c = cb[at];
-                const VT v = vb[at];
-                if (c >= 0) t -= (XT)v * __ldcg(y + c);  // L2: written by other SMs in this launch
-            }
-            tsh[lr][q] = t;
-            if (UPPER) dsh[lr][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
+        const int pos = d.pos0 + q * BS + l;
+        XT t = live ? x[pos] : XT(0);
+        const int we = wsh[cur][l];
+        for (int k = 0; k < we; k++) {
+            const int at = (eo + k) * 32 + q;
+            const int c = cb[at];
+            const VT v = vb[at];
+            if (c >= 0) t -= (XT)v * __ldcg(y + c);  // L2: written by other SMs in this launch
         }
+        tsh[l][q] = t;
+        if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
         __syncthreads();
         const int gn = item[cur ^ 1];
         if (l == 0) {
@@ -797,17 +787,11 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
             const int t = threadIdx.x - 32;
             if (t < 2 * BS) wsh[cur ^ 1][t] = widths[(size_t)gn * 2 * BS + t];
             if (t == 0) dd[cur ^ 1] = groups[gn];
-            asm volatile("bar.sync 1, %0;" ::"r"((WARPS - 1) * 32) : "memory");
-            stage(gn, cur ^ 1, 32, (WARPS - 1) * 32);
+            asm volatile("bar.sync 1, %0;" ::"r"((BS - 1) * 32) : "memory");
+            stage(gn, cur ^ 1, 32, (BS - 1) * 32);
         }
         __syncthreads();
-        if (live) {
-#pragma unroll
-            for (int rr = 0; rr < RPW; rr++) {
-                const int lr = l + WARPS * rr;
-                y[d.pos0 + q * BS + lr] = tsh[lr][q];
-            }
-        }
+        if (live) y[pos] = tsh[l][q];
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) st_release(flags + g, epoch);

@@ -270,9 +270,6 @@ void level_schedule(int N, const int *cind, const int *rptr, bool upper, std::ve
 // from global memory instead.
 constexpr size_t kMaxStagedBytes = 160 * 1024;
 
-// Warps per CTA of the dataflow sweep: two rows of each chain per warp.
-constexpr int df_warps(int bs) { return bs >= 4 ? bs / 2 : 2; }
-
 template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED, bool STAGED>
 void launch_group(const SweepFactor<VT> &F, int *status, int gb, int ge, size_t smem, const XT *x, XT *y,
                   cudaStream_t s, const int *gate)
@@ -316,18 +313,17 @@ void launch_dataflow(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, 
 {
     const int ng = F.colour_groups.back();
     if (ng == 0) return;
-    constexpr int W = df_warps(BS);
-    auto kern = k_sweep_df<VT, XT, BS, W, UPPER>;
+    auto kern = k_sweep_df<VT, XT, BS, UPPER>;
     size_t smem = 0;  // the widest group's block
     for (size_t b : F.colour_smem) smem = std::max(smem, b);
     smem = (smem + 15) / 16 * 16;
     SENK_REQUIRE(2 * smem <= kMaxStagedBytes,
                  "a group's factor block exceeds the shared memory of the dataflow sweep");
     int per_sm = 0;
-    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, W * 32, 2 * smem));
+    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 2 * smem));
     const int grid = std::max(1, std::min(ng, std::max(per_sm, 1) * kNumSMs));
     k_df_begin<<<1, 1, 0, s>>>(F.ctrl.p);
-    kern<<<grid, W * 32, 2 * smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
+    kern<<<grid, BS * 32, 2 * smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
                                       (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p,
                                       F.dep_ptr.p, F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status,
                                       (unsigned)smem);
@@ -369,10 +365,9 @@ void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cud
 template <typename VT, typename XT, int BS>
 void allow_df_smem()
 {
-    constexpr int W = df_warps(BS);
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kMaxStagedBytes));
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kMaxStagedBytes));
 }
 
