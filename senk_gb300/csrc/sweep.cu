@@ -198,24 +198,30 @@ void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> 
         for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) owner[p] = i;
     std::vector<std::vector<int>> deps(ng);
     int bad = -1;
-#pragma omp parallel for schedule(dynamic, 16)
-    for (int i = 0; i < ng; i++) {
-        std::vector<int> &dv = deps[i];
-        for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) {
-            const int cs = p - p % bs, ce = cs + bs;
-            for (int j = rptr[p] + (upper ? 1 : 0); j < rptr[p + 1]; j++) {
-                const int c = cind[j];
-                if (c >= cs && c < ce) continue;  // in-chain
-                const int o = owner[c];
-                if (o < 0 || o >= i) {
+#pragma omp parallel
+    {
+        std::vector<int> seen(ng, -1);  // per thread: the group that last listed each group
+#pragma omp for schedule(dynamic, 16)
+        for (int i = 0; i < ng; i++) {
+            std::vector<int> &dv = deps[i];
+            for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) {
+                const int cs = p - p % bs, ce = cs + bs;
+                for (int j = rptr[p] + (upper ? 1 : 0); j < rptr[p + 1]; j++) {
+                    const int c = cind[j];
+                    if (c >= cs && c < ce) continue;  // in-chain
+                    const int o = owner[c];
+                    if (o < 0 || o >= i) {
 #pragma omp atomic write
-                    bad = i;
+                        bad = i;
+                        continue;
+                    }
+                    if (seen[o] != i) {
+                        seen[o] = i;
+                        dv.push_back(o);
+                    }
                 }
-                dv.push_back(o);
             }
         }
-        std::sort(dv.begin(), dv.end());
-        dv.erase(std::unique(dv.begin(), dv.end()), dv.end());
     }
     SENK_REQUIRE(bad < 0, "group " + std::to_string(bad) + " reads a group that is not solved before it");
     std::vector<int> ptr(ng + 1, 0), idx;
