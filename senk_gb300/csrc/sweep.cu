@@ -13,8 +13,6 @@
 // 32-wide column across the group's chains, so a warp's loads coalesce.
 #include <algorithm>
 #include <climits>
-#include <exception>
-#include <future>
 #include <memory>
 
 #include "device.hpp"
@@ -433,24 +431,10 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    // For U, "earlier" means a later colour: flip the colour numbers. The two
-    // layouts are independent: U's is built on a second host thread.
-    std::vector<int> colour_of_u(N);
-    for (int p = 0; p < N; p++) colour_of_u[p] = cnum - 1 - colour_of[p];
-    int dev = 0;
-    SENK_CUDA(cudaGetDevice(&dev));
-    auto u_build = std::async(std::launch::async, [&] {
-        SENK_CUDA(cudaSetDevice(dev));  // the current device is per host thread
-        build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of_u, s, sweep_mode);
-    });
-    std::exception_ptr err;
-    try {
-        build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s, sweep_mode);
-    } catch (...) {
-        err = std::current_exception();
-    }
-    u_build.get();  // rethrows U's error, if any
-    if (err) std::rethrow_exception(err);
+    build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s, sweep_mode);
+    // For U, "earlier" means a later colour: flip the colour numbers.
+    for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
+    build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s, sweep_mode);
 }
 
 template <typename VT>
