@@ -292,13 +292,14 @@ def run_gpu(args, rank, world):
     e2e = None
     if not args.no_e2e and do_mixed:
         e2e_ms, rr = [], None
-        for i in range(max(1, min(args.steps, 3))):
+        for i in range(max(1, min(args.steps, 3)) + 1):  # the first call is an untimed warm-up
             xh = np.zeros(Ar.n)
             t0 = time.perf_counter()
             rr = SV.AbmcIluGmresIr(Ar.val, Ar.cind, Ar.rptr, Lf.val, Lf.cind, Lf.rptr, Uf.val, Uf.cind, Uf.rptr, sc,
                                    nc, 16, b, xh, nb, ir_outer, args.m, Ar.n, args.eps, args.inner_tol,
                                    args.inner_cycles, orth=orth, spmv=spmv)
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            if i > 0:
+                e2e_ms.append((time.perf_counter() - t0) * 1e3)
         e2e = {"value": allmax(world, sum(e2e_ms) / len(e2e_ms)), "unit": "ms",
                "h2d_bytes_per_step": int(rr.h2d_bytes), "d2h_bytes_per_step": int(rr.d2h_bytes),
                "steps": len(e2e_ms), "iterations": rr.iters,
