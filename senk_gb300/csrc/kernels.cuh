@@ -616,20 +616,22 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     __syncthreads();
     // Phase 2: one lane per chain, rows in solve order.
     if (l == 0) {
+        // slot offset of row r's in-chain entries: etot + sum of wi over rows < r,
+        // walked upwards for L and downwards for U
         int io = etot;
-        int ioff[BS];
-#pragma unroll
-        for (int r = 0; r < BS; r++) {
-            ioff[r] = io;
-            io += wsh[BS + r];
+        if (UPPER) {
+            for (int r = 0; r < BS; r++) io += wsh[BS + r];
         }
-#pragma unroll
+#pragma unroll 4
         for (int s = 0; s < BS; s++) {
             const int r = UPPER ? BS - 1 - s : s;
             XT tt = tsh[r][q];
             const int wi = wsh[BS + r];
+            if (UPPER) io -= wi;
+            const int ro = io;
+            if (!UPPER) io += wi;
             for (int k = 0; k < wi; k++) {
-                const int at = (ioff[r] + k) * 32 + q;
+                const int at = (ro + k) * 32 + q;
                 const int c = cb[at];
                 const VT v = vb[at];
                 if (c >= 0) tt -= (XT)v * tsh[c][q];
@@ -761,20 +763,20 @@ k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__
         __syncthreads();
         const int gn = item[cur ^ 1];
         if (l == 0) {
-            int io = etot;
-            int ioff[BS];
-#pragma unroll
-            for (int r = 0; r < BS; r++) {
-                ioff[r] = io;
-                io += wsh[cur][BS + r];
+            int io = etot;  // as in k_sweep: walked upwards for L, downwards for U
+            if (UPPER) {
+                for (int r = 0; r < BS; r++) io += wsh[cur][BS + r];
             }
-#pragma unroll
+#pragma unroll 4
             for (int st = 0; st < BS; st++) {
                 const int r = UPPER ? BS - 1 - st : st;
                 XT tt = tsh[r][q];
                 const int wi = wsh[cur][BS + r];
+                if (UPPER) io -= wi;
+                const int ro = io;
+                if (!UPPER) io += wi;
                 for (int k = 0; k < wi; k++) {
-                    const int at = (ioff[r] + k) * 32 + q;
+                    const int at = (ro + k) * 32 + q;
                     const int c = cb[at];
                     const VT v = vb[at];
                     if (c >= 0) tt -= (XT)v * tsh[c][q];

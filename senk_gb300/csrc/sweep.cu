@@ -1,473 +1,10 @@
-// ILU sweep plans: the split factors re-laid out for colour-by-colour triangular
-// sweeps on the GPU (replaces include/senk_sparse.hpp:132-315, SptrsvCsr_l/_u in
-// their sequential, AMC and ABMC forms).
-//
-// Layout ("chain-major"): the schedule is a list of colours (or level sets for
-// the natural order) in processing order. A chain is `bs` consecutive schedule
-// positions (one ABMC block) solved in order; 32 chains of a colour form a
-// group, solved by one CTA of bs warps. Per row, entries referencing other
-// chains are stored first (they are final before the colour starts, so the
-// thread gathers all of them at once) and entries inside the chain after all of
-// them, as chain-local row numbers; each part keeps the reference's subtraction
-// order (ascending columns for L, descending for U). Slot k of a row is a
-// 32-wide column across the group's chains, so a warp's loads coalesce.
-#include <algorithm>
-#include <climits>
+// C ABI of the ILU sweep plans (senk_ilu_plan_*, senk_ilub_plan_create); the
+// plans themselves are in sweep_impl.cuh, sweep_f32.cu and sweep_f64.cu.
 #include <memory>
 
 #include "device.hpp"
 
 namespace senkgpu {
-
-namespace {
-
-struct Group {
-    int p0, p1;  // schedule positions [p0, p1)
-};
-
-// The groups each group reads from (dataflow sweeps), and the launch size.
-template <typename VT>
-void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> &gd, int bs, const int *cind,
-                        const int *rptr, bool upper, cudaStream_t s);
-
-template <typename VT>
-void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
-                  const std::vector<Group> &groups, const std::vector<int> *rowmap, int bs,
-                  const std::vector<int> *group_of_row, cudaStream_t s, int sweep_mode = SENK_SWEEP_AUTO)
-{
-    F.upper = upper;
-    F.mapped = rowmap != nullptr;
-    F.bs = bs;
-    const bool chains = !F.mapped && bs > 1;
-    std::vector<int> next(N), nint(N);
-    int bad = -1;
-#pragma omp parallel for schedule(static)
-    for (int p = 0; p < N; p++) {
-        const int row = rowmap ? (*rowmap)[p] : p;
-        int b = rptr[row], e = rptr[row + 1];
-        bool ok = true;
-        if (upper) {
-            ok = e > b && cind[b] == row;  // U row must start with its diagonal
-            b++;
-        }
-        const int cs = row - row % bs, ce = cs + bs;
-        int ni = 0;
-        for (int j = b; j < e && ok; j++) {
-            const int c = cind[j];
-            if (c < 0 || c >= N || (upper ? c <= row : c >= row)) { ok = false; break; }
-            if (chains && c >= cs && c < ce) ni++;
-            else if (group_of_row && (*group_of_row)[c] >= (*group_of_row)[row])
-                ok = false;  // a column outside the chain must belong to a group solved earlier
-        }
-        if (!ok || e - b - ni > 255 || ni > 255) {
-#pragma omp atomic write
-            bad = row;
-        }
-        next[p] = (e - b) - ni;
-        nint[p] = ni;
-    }
-    SENK_REQUIRE(bad < 0, std::string(upper ? "U" : "L") + " factor row " + std::to_string(bad) +
-                              " does not fit the schedule (diagonal first in U, strictly triangular, "
-                              "columns of other chains in earlier colours, at most 255 entries)");
-    // Groups of up to 32 chains inside each colour, in processing order.
-    std::vector<GroupDesc> gd;
-    F.colour_groups.assign(1, 0);
-    for (const Group &g : groups) {
-        const int nch = (g.p1 - g.p0) / bs;
-        for (int q = 0; q < nch; q += 32) {
-            GroupDesc d{};
-            d.pos0 = g.p0 + q * bs;
-            d.nchains = std::min(32, nch - q);
-            d.widx = (int)gd.size() * 2 * bs;
-            gd.push_back(d);
-        }
-        F.colour_groups.push_back((int)gd.size());
-    }
-    const int ng = (int)gd.size();
-    std::vector<unsigned char> wd((size_t)std::max(ng, 1) * 2 * bs, 0);
-    std::vector<long long> slots(ng, 0);
-#pragma omp parallel for schedule(static)
-    for (int i = 0; i < ng; i++) {
-        long long tot = 0;
-        for (int l = 0; l < bs; l++) {
-            int we = 0, wi = 0;
-            for (int q = 0; q < gd[i].nchains; q++) {
-                const int p = gd[i].pos0 + q * bs + l;
-                we = std::max(we, next[p]);
-                wi = std::max(wi, nint[p]);
-            }
-            wd[(size_t)gd[i].widx + l] = (unsigned char)we;
-            wd[(size_t)gd[i].widx + bs + l] = (unsigned char)wi;
-            tot += we + wi;
-        }
-        slots[i] = tot;
-    }
-    long long off = 0;
-    for (int i = 0; i < ng; i++) {
-        gd[i].off = (int)off;
-        off += slots[i] * 32;
-        SENK_REQUIRE(off < INT_MAX, "factor too large for 32-bit slot offsets");
-    }
-    // Shared memory a colour's CTAs need to stage their group's block.
-    F.colour_smem.assign(F.colour_groups.size() - 1, 0);
-    for (size_t c = 0; c + 1 < F.colour_groups.size(); c++)
-        for (int i = F.colour_groups[c]; i < F.colour_groups[c + 1]; i++)
-            F.colour_smem[c] = std::max(F.colour_smem[c], (size_t)slots[i] * 32 * (sizeof(VT) + sizeof(int)));
-    F.elems = off;
-    // padding is (0, column -1); filled in parallel (the arrays run to 100s of MB)
-    const long long ne = std::max<long long>(off, 1);
-    std::unique_ptr<VT[]> hv(new VT[ne]);
-    std::unique_ptr<int[]> hc(new int[ne]);
-#pragma omp parallel for schedule(static)
-    for (long long i = 0; i < ne; i++) {
-        hv[i] = VT(0);
-        hc[i] = -1;
-    }
-    std::vector<VT> hd(upper ? N : 0);
-    long long stored = 0;
-#pragma omp parallel for schedule(static) reduction(+ : stored)
-    for (int i = 0; i < ng; i++) {
-        const GroupDesc d = gd[i];
-        const unsigned char *w = wd.data() + d.widx;
-        int eoff[32], ioff[32];
-        int acc = 0;
-        for (int l = 0; l < bs; l++) { eoff[l] = acc; acc += w[l]; }
-        for (int l = 0; l < bs; l++) { ioff[l] = acc; acc += w[bs + l]; }
-        for (int q = 0; q < d.nchains; q++) {
-            for (int l = 0; l < bs; l++) {
-                const int p = d.pos0 + q * bs + l;
-                const int row = rowmap ? (*rowmap)[p] : p;
-                const int cs = row - row % bs, ce = cs + bs;
-                int ke = 0, ki = 0;
-                auto put = [&](int j) {
-                    const int c = cind[j];
-                    long long at;
-                    if (chains && c >= cs && c < ce) {
-                        at = d.off + (long long)(ioff[l] + ki++) * 32 + q;
-                        hc[at] = c - cs;
-                    } else {
-                        at = d.off + (long long)(eoff[l] + ke++) * 32 + q;
-                        hc[at] = c;
-                    }
-                    hv[at] = val[j];
-                    stored++;
-                };
-                if (upper) {
-                    hd[p] = val[rptr[row]];
-                    for (int j = rptr[row + 1] - 1; j >= rptr[row] + 1; j--) put(j);
-                } else {
-                    for (int j = rptr[row]; j < rptr[row + 1]; j++) put(j);
-                }
-            }
-        }
-    }
-    F.nnz = stored + (upper ? N : 0);
-    F.val.alloc(ne);
-    F.val.upload(hv.get(), ne, s);
-    F.col.alloc(ne);
-    F.col.upload(hc.get(), ne, s);
-    if (upper) {
-        F.dinv.alloc(N);
-        F.dinv.upload(hd.data(), N, s);
-    }
-    if (rowmap) {
-        F.rowmap.alloc(N);
-        F.rowmap.upload(rowmap->data(), N, s);
-    }
-    F.groups.alloc(std::max(ng, 1));
-    F.groups.upload(gd.data(), ng, s);
-    F.widths.alloc(wd.size());
-    F.widths.upload(wd.data(), wd.size(), s);
-    // Measured on the 128^3 convection-diffusion system (ILU application):
-    // dataflow FP32 274 us vs 291 us per colour launch; FP64 389 us vs 372 us.
-    // SENK_SWEEP_AUTO takes the faster of the two for the factor's type.
-    F.dataflow = chains && (sweep_mode == SENK_SWEEP_DATAFLOW ||
-                            (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == sizeof(float)));
-    if (F.dataflow) build_dependencies(F, N, gd, bs, cind, rptr, upper, s);
-    // Host vectors are released on return: finish the copies first.
-    SENK_CUDA(cudaStreamSynchronize(s));
-}
-
-template <typename VT>
-void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> &gd, int bs, const int *cind,
-                        const int *rptr, bool upper, cudaStream_t s)
-{
-    const int ng = (int)gd.size();
-    std::vector<int> owner(N, -1);
-    for (int i = 0; i < ng; i++)
-        for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) owner[p] = i;
-    std::vector<std::vector<int>> deps(ng);
-    int bad = -1;
-#pragma omp parallel
-    {
-        std::vector<int> seen(ng, -1);  // per thread: the group that last listed each group
-#pragma omp for schedule(dynamic, 16)
-        for (int i = 0; i < ng; i++) {
-            std::vector<int> &dv = deps[i];
-            for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) {
-                const int cs = p - p % bs, ce = cs + bs;
-                for (int j = rptr[p] + (upper ? 1 : 0); j < rptr[p + 1]; j++) {
-                    const int c = cind[j];
-                    if (c >= cs && c < ce) continue;  // in-chain
-                    const int o = owner[c];
-                    if (o < 0 || o >= i) {
-#pragma omp atomic write
-                        bad = i;
-                        continue;
-                    }
-                    if (seen[o] != i) {
-                        seen[o] = i;
-                        dv.push_back(o);
-                    }
-                }
-            }
-        }
-    }
-    SENK_REQUIRE(bad < 0, "group " + std::to_string(bad) + " reads a group that is not solved before it");
-    std::vector<int> ptr(ng + 1, 0), idx;
-    for (int i = 0; i < ng; i++) ptr[i + 1] = ptr[i] + (int)deps[i].size();
-    idx.reserve(ptr[ng]);
-    for (int i = 0; i < ng; i++) idx.insert(idx.end(), deps[i].begin(), deps[i].end());
-    F.dep_ptr.alloc(ptr.size());
-    F.dep_ptr.upload(ptr.data(), ptr.size(), s);
-    F.dep_idx.alloc(std::max<size_t>(idx.size(), 1));
-    F.dep_idx.upload(idx.data(), idx.size(), s);
-    F.flags.alloc(std::max(ng, 1));
-    SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
-    F.ctrl.alloc(4);
-    SENK_CUDA(cudaMemsetAsync(F.ctrl.p, 0, F.ctrl.bytes(), s));
-    SENK_CUDA(cudaStreamSynchronize(s));
-}
-
-// Level sets of a triangular factor for the natural order: level(i) = 1 + max
-// level of the rows it reads. Rows of one level are independent, and each row's
-// arithmetic is the sequential sweep's, so the result equals the sequential one.
-void level_schedule(int N, const int *cind, const int *rptr, bool upper, std::vector<int> &rowmap,
-                    std::vector<Group> &groups)
-{
-    std::vector<int> lev(N, 0);
-    int maxlev = 0;
-    if (!upper) {
-        for (int i = 0; i < N; i++) {
-            int l = 0;
-            for (int j = rptr[i]; j < rptr[i + 1]; j++) l = std::max(l, lev[cind[j]] + 1);
-            lev[i] = l;
-            maxlev = std::max(maxlev, l);
-        }
-    } else {
-        for (int i = N - 1; i >= 0; i--) {
-            int l = 0;
-            for (int j = rptr[i] + 1; j < rptr[i + 1]; j++) l = std::max(l, lev[cind[j]] + 1);
-            lev[i] = l;
-            maxlev = std::max(maxlev, l);
-        }
-    }
-    std::vector<int> cnt(maxlev + 2, 0);
-    for (int i = 0; i < N; i++) cnt[lev[i] + 1]++;
-    for (int l = 0; l <= maxlev; l++) cnt[l + 1] += cnt[l];
-    rowmap.assign(N, 0);
-    std::vector<int> at(cnt.begin(), cnt.end() - 1);
-    for (int i = 0; i < N; i++) rowmap[at[lev[i]]++] = i;
-    groups.clear();
-    for (int l = 0; l <= maxlev; l++) groups.push_back({cnt[l], cnt[l + 1]});
-}
-
-// Largest block staged through shared memory; bigger groups read the factor
-// from global memory instead.
-constexpr size_t kMaxStagedBytes = 160 * 1024;
-
-template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED, bool STAGED>
-void launch_group(const SweepFactor<VT> &F, int *status, int gb, int ge, size_t smem, const XT *x, XT *y,
-                  cudaStream_t s, const int *gate)
-{
-    auto kern = k_sweep<VT, XT, BS, UPPER, MAPPED, STAGED>;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(ge - gb);
-    cfg.blockDim = dim3(BS * 32);
-    cfg.dynamicSmemBytes = STAGED ? smem : 0;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    SENK_CUDA(cudaLaunchKernelEx(&cfg, kern, (const GroupDesc *)F.groups.p, gb, (const unsigned char *)F.widths.p,
-                                 (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p,
-                                 (const int *)F.rowmap.p, x, y, gate, status));
-}
-
-template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
-void launch_colour(const SweepFactor<VT> &F, int *status, int c, const XT *x, XT *y, cudaStream_t s,
-                   const int *gate)
-{
-    const int gb = F.colour_groups[c], ge = F.colour_groups[c + 1];
-    if (ge == gb) return;
-    const size_t smem = F.colour_smem[c];
-    if (smem <= kMaxStagedBytes) launch_group<VT, XT, BS, UPPER, MAPPED, true>(F, status, gb, ge, smem, x, y, s, gate);
-    else launch_group<VT, XT, BS, UPPER, MAPPED, false>(F, status, gb, ge, smem, x, y, s, gate);
-}
-
-template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED>
-void allow_smem()
-{
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep<VT, XT, BS, UPPER, MAPPED, true>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxStagedBytes));
-}
-
-template <typename VT, typename XT, int BS, bool UPPER>
-void launch_dataflow(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
-{
-    const int ng = F.colour_groups.back();
-    if (ng == 0) return;
-    auto kern = k_sweep_df<VT, XT, BS, UPPER>;
-    size_t smem = 0;  // the widest group's block
-    for (size_t b : F.colour_smem) smem = std::max(smem, b);
-    smem = (smem + 15) / 16 * 16;
-    SENK_REQUIRE(2 * smem <= kMaxStagedBytes,
-                 "a group's factor block exceeds the shared memory of the dataflow sweep");
-    int per_sm = 0;
-    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 2 * smem));
-    const int grid = std::max(1, std::min(ng, std::max(per_sm, 1) * kNumSMs));
-    k_df_begin<<<1, 1, 0, s>>>(F.ctrl.p);
-    kern<<<grid, BS * 32, 2 * smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
-                                      (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p,
-                                      F.dep_ptr.p, F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status,
-                                      (unsigned)smem);
-    SENK_LAUNCH_CHECK();
-}
-
-template <typename VT, typename XT, bool UPPER>
-void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
-{
-    const int nc = (int)F.colour_groups.size() - 1;
-    if (F.dataflow) {
-        switch (F.bs) {
-        case 2: launch_dataflow<VT, XT, 2, UPPER>(F, status, x, y, s, gate); break;
-        case 4: launch_dataflow<VT, XT, 4, UPPER>(F, status, x, y, s, gate); break;
-        case 8: launch_dataflow<VT, XT, 8, UPPER>(F, status, x, y, s, gate); break;
-        case 16: launch_dataflow<VT, XT, 16, UPPER>(F, status, x, y, s, gate); break;
-        case 32: launch_dataflow<VT, XT, 32, UPPER>(F, status, x, y, s, gate); break;
-        default: throw ArgError("unsupported chain length");
-        }
-        return;
-    }
-    for (int c = 0; c < nc; c++) {
-        if (F.mapped) {
-            launch_colour<VT, XT, 1, UPPER, true>(F, status, c, x, y, s, gate);
-            continue;
-        }
-        switch (F.bs) {
-        case 1: launch_colour<VT, XT, 1, UPPER, false>(F, status, c, x, y, s, gate); break;
-        case 2: launch_colour<VT, XT, 2, UPPER, false>(F, status, c, x, y, s, gate); break;
-        case 4: launch_colour<VT, XT, 4, UPPER, false>(F, status, c, x, y, s, gate); break;
-        case 8: launch_colour<VT, XT, 8, UPPER, false>(F, status, c, x, y, s, gate); break;
-        case 16: launch_colour<VT, XT, 16, UPPER, false>(F, status, c, x, y, s, gate); break;
-        case 32: launch_colour<VT, XT, 32, UPPER, false>(F, status, c, x, y, s, gate); break;
-        default: throw ArgError("unsupported chain length");
-        }
-    }
-}
-
-template <typename VT, typename XT, int BS>
-void allow_df_smem()
-{
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kMaxStagedBytes));
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kMaxStagedBytes));
-}
-
-template <typename VT, typename XT>
-void allow_all_smem()
-{
-    allow_df_smem<VT, XT, 2>(); allow_df_smem<VT, XT, 4>(); allow_df_smem<VT, XT, 8>();
-    allow_df_smem<VT, XT, 16>(); allow_df_smem<VT, XT, 32>();
-    allow_smem<VT, XT, 1, false, true>(); allow_smem<VT, XT, 1, true, true>();
-    allow_smem<VT, XT, 1, false, false>(); allow_smem<VT, XT, 1, true, false>();
-    allow_smem<VT, XT, 2, false, false>(); allow_smem<VT, XT, 2, true, false>();
-    allow_smem<VT, XT, 4, false, false>(); allow_smem<VT, XT, 4, true, false>();
-    allow_smem<VT, XT, 8, false, false>(); allow_smem<VT, XT, 8, true, false>();
-    allow_smem<VT, XT, 16, false, false>(); allow_smem<VT, XT, 16, true, false>();
-    allow_smem<VT, XT, 32, false, false>(); allow_smem<VT, XT, 32, true, false>();
-}
-
-}  // namespace
-
-template <typename VT>
-void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval,
-                        const int *ucind, const int *urptr, int pckind, const int *cptr, int cnum, int bsize,
-                        cudaStream_t s, int sweep_mode)
-{
-    SENK_REQUIRE(sweep_mode == SENK_SWEEP_AUTO || sweep_mode == SENK_SWEEP_COLOURS ||
-                     sweep_mode == SENK_SWEEP_DATAFLOW,
-                 "unknown sweep mode");
-    SENK_REQUIRE(N > 0, "N must be positive");
-    SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
-    n = N;
-    precond = pckind;
-    status.alloc(1);
-    SENK_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
-    allow_all_smem<VT, VT>();
-    if (pckind == SENK_PC_ILU) {
-        std::vector<int> rm;
-        std::vector<Group> gr;
-        level_schedule(N, lcind, lrptr, false, rm, gr);
-        build_factor(L, false, N, lval, lcind, lrptr, gr, &rm, 1, nullptr, s);
-        level_schedule(N, ucind, urptr, true, rm, gr);
-        build_factor(U, true, N, uval, ucind, urptr, gr, &rm, 1, nullptr, s);
-        return;
-    }
-    SENK_REQUIRE(pckind == SENK_PC_ILU_AMC || pckind == SENK_PC_ILU_ABMC, "unknown preconditioner kind");
-    const int bs = pckind == SENK_PC_ILU_AMC ? 1 : bsize;
-    SENK_REQUIRE(bs == 1 || bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32,
-                 "ABMC block size must be 1, 2, 4, 8, 16 or 32 on the GPU path (got " + std::to_string(bs) + ")");
-    SENK_REQUIRE(cptr && cnum > 0, "colour pointer missing");
-    SENK_REQUIRE(cptr[0] == 0 && (long long)cptr[cnum] * bs == N, "colour pointer does not cover N rows");
-    std::vector<Group> fwd, bwd;
-    std::vector<int> colour_of(N);
-    for (int k = 0; k < cnum; k++) {
-        SENK_REQUIRE(cptr[k + 1] >= cptr[k], "colour pointer not monotone");
-        fwd.push_back({cptr[k] * bs, cptr[k + 1] * bs});
-        for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
-    }
-    for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s, sweep_mode);
-    // For U, "earlier" means a later colour: flip the colour numbers.
-    for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
-    build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s, sweep_mode);
-}
-
-template <typename VT>
-template <typename XT>
-void IluPlan<VT>::sweep(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate) const
-{
-    if (F.upper) sweep_groups<VT, XT, true>(F, status.p, x, y, s, gate);
-    else sweep_groups<VT, XT, false>(F, status.p, x, y, s, gate);
-}
-
-template <typename VT>
-long long IluPlan<VT>::apply_bytes() const
-{
-    const long long vb = sizeof(VT);
-    // stored entries: value + column; U diagonal: value only; x read, t written,
-    // t read and written again by the in-place U sweep.
-    return (L.nnz + (U.nnz - n)) * (vb + 4) + (long long)n * vb + 4LL * n * vb;
-}
-
-template <typename VT>
-void IluPlan<VT>::check_status(cudaStream_t s) const
-{
-    int h = 0;
-    SENK_CUDA(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SENK_CUDA(cudaStreamSynchronize(s));
-    if (h) throw CudaError{cudaErrorLaunchTimeout, "ILU sweep: a TMA wait did not complete", __FILE__, __LINE__};
-}
-
-template struct IluPlan<double>;
-template struct IluPlan<float>;
-template void IluPlan<double>::sweep<double>(const SweepFactor<double> &, const double *, double *, cudaStream_t, const int *) const;
-template void IluPlan<float>::sweep<float>(const SweepFactor<float> &, const float *, float *, cudaStream_t, const int *) const;
-
 }  // namespace senkgpu
 
 using namespace senkgpu;
