@@ -72,8 +72,7 @@ typedef struct {
 } senk_options;
 
 /* How the ILU sweeps of ABMC chains (bsize >= 2) are scheduled. */
-#define SENK_SWEEP_AUTO 0     /* dataflow for FP32 factors, colours for FP64 (the
-                                 faster of the two for each type, as measured) */
+#define SENK_SWEEP_AUTO 0     /* the faster schedule as measured: one launch per colour */
 #define SENK_SWEEP_COLOURS 1  /* one launch per colour */
 #define SENK_SWEEP_DATAFLOW 2 /* one launch per sweep: groups of 32 chains wait on
                                  per-group flags of the groups they read */

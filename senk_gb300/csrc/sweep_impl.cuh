@@ -179,11 +179,10 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.groups.upload(gd.data(), ng, s);
     F.widths.alloc(wd.size());
     F.widths.upload(wd.data(), wd.size(), s);
-    // Measured on the 128^3 convection-diffusion system (ILU application):
-    // dataflow FP32 274 us vs 291 us per colour launch; FP64 389 us vs 372 us.
-    // SENK_SWEEP_AUTO takes the faster of the two for the factor's type.
-    F.dataflow = chains && (sweep_mode == SENK_SWEEP_DATAFLOW ||
-                            (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == sizeof(float)));
+    // Measured on the 128^3 convection-diffusion system (one ILU application):
+    // per-colour launches FP32 194 us, FP64 301 us; dataflow FP32 323 us,
+    // FP64 300 us. SENK_SWEEP_AUTO takes the per-colour launches.
+    F.dataflow = chains && sweep_mode == SENK_SWEEP_DATAFLOW;
     if (F.dataflow) build_dependencies(F, N, gd, bs, cind, rptr, upper, s);
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
