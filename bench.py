@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--eps", type=float, default=1e-8)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2", "mgs"])
     ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
+    ap.add_argument("--sweep", default="auto", choices=["auto", "colours", "dataflow"],
+                    help="schedule of the ABMC triangular sweeps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
@@ -243,9 +245,11 @@ def run_gpu(args, rank, world):
     nb = float(np.linalg.norm(b))
     orth = {"cgs2": L.ORTH_CGS2, "cgs": L.ORTH_CGS, "mgs": L.ORTH_MGS}[args.orth]
     spmv = {"auto": L.SPMV_AUTO, "csr": L.SPMV_CSR, "sell": L.SPMV_SELL}[args.spmv]
+    sweep = {"auto": L.SWEEP_AUTO, "colours": L.SWEEP_COLOURS, "dataflow": L.SWEEP_DATAFLOW}[args.sweep]
     outer = 10000 // args.m
     ir_outer = 20
-    sysm = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=args.m, mixed=True, orth=orth, spmv=spmv)
+    sysm = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=args.m, mixed=True, orth=orth, spmv=spmv,
+                     sweep=sweep)
     sysm.set_rhs(b)
     do_mixed, do_plain = args.only in ("both", "mixed"), args.only in ("both", "plain")
     mixed = lambda: sysm.gmres_ir(nb, ir_outer, args.m, args.eps, args.inner_tol, args.inner_cycles)
@@ -297,7 +301,7 @@ def run_gpu(args, rank, world):
             t0 = time.perf_counter()
             rr = SV.AbmcIluGmresIr(Ar.val, Ar.cind, Ar.rptr, Lf.val, Lf.cind, Lf.rptr, Uf.val, Uf.cind, Uf.rptr, sc,
                                    nc, 16, b, xh, nb, ir_outer, args.m, Ar.n, args.eps, args.inner_tol,
-                                   args.inner_cycles, orth=orth, spmv=spmv)
+                                   args.inner_cycles, orth=orth, spmv=spmv, sweep=sweep)
             if i > 0:
                 e2e_ms.append((time.perf_counter() - t0) * 1e3)
         e2e = {"value": allmax(world, sum(e2e_ms) / len(e2e_ms)), "unit": "ms",
@@ -327,7 +331,7 @@ def run_gpu(args, rank, world):
         "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if do_mixed else "f64", "data": "synthetic",
         "config": {"workload": workload_name(args.n), "N": Ar.n, "nnz": Ar.nnz, "colours": nc,
-                   "orth": args.orth, "spmv": args.spmv, "inner_tol": args.inner_tol,
+                   "orth": args.orth, "spmv": args.spmv, "sweep": args.sweep, "inner_tol": args.inner_tol,
                    "inner_cycles": args.inner_cycles,
                    "iterations": rm.iters if rm else rp.iters,
                    "outer_steps": rm.cycles if rm else None,
