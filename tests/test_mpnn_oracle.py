@@ -56,3 +56,27 @@ def test_bf16_rounding_is_nearest_even():
     y = M.bf16(x)
     assert y[0] == 1.0 and y[1] == 1.0 and y[2] == 1.0 + 2**-6 and y[3] == -2.5
     assert abs(y[4] - 3.0e-3) <= 3.0e-3 * 2**-8
+
+
+def test_learned_gcr_history_is_iluGcrm_between_restarts():
+    """oracle/learned_gcr.py's per-iteration GCR with K = ILU(0) is the oracle's
+    IluGcrm (senk_gcr.hpp:93-161) observed every iteration: its first iteration
+    below eps, rounded up to a restart, is IluGcrm's count; within a cycle the
+    residual never grows (GCR minimises it over the directions of the cycle)."""
+    import oracle
+    from oracle import learned_gcr as LG
+    from senk_gb300.learned import family_member
+
+    mb = family_member(8, 1234)
+    pt = oracle.port()
+    m, eps = 5, 1e-8
+    ilu = lambda r: pt.ilu_apply(mb.L, mb.U, r, mb.cptr, mb.cnum, 16)
+    h = LG.gcr_history(mb.A, mb.b, ilu, m, 80)
+    k = LG.first_below(h, eps)
+    assert k > 0
+    nb = float(np.linalg.norm(mb.b))
+    _, it, _, conv = pt.solve("gcr", mb.A, mb.b, L=mb.L, U=mb.U, pc=oracle.PC_ILU_ABMC, cptr=mb.cptr, cnum=mb.cnum,
+                              bsize=16, outer=80 // m, m=m, eps=eps, nrm_b=nb)
+    assert conv and it == -(-k // m) * m
+    for c in range(0, 80, m):
+        assert np.all(np.diff(h[c:c + m + 1]) <= 1e-12 * h[c])
