@@ -414,6 +414,10 @@ int senk_mpnn_bind(senk_mpnn *net, senk_system *sys);
 int senk_mpnn_set_loss(senk_mpnn *net, int mode);
 /* Global gradient-norm clip of the Adam steps (default 1; <= 0: off). */
 int senk_mpnn_set_clip(senk_mpnn *net, float clip);
+/* Step of the correction in the GCR hook: 0 (default) K(r) = ILU(r) + c;
+ * 1 K(r) = ILU(r) + alpha c, alpha = argmin |r - A(ILU(r) + alpha c)|, computed
+ * on the device (one extra SpMV pair and a reduction per application). */
+int senk_mpnn_set_step(senk_mpnn *net, int mode);
 /* Loss of one residual/error pair; gradient to grad (host, may be NULL). */
 int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const double *e, double *loss,
                         float *grad);

@@ -12,7 +12,7 @@ GCR here records the residual after every iteration. The reference's GCR
 iteration counts come in multiples of m and hide differences smaller than a
 restart cycle; this history shows them.
 
-    python -m oracle.learned_gcr --n 16 --train 16 --epochs 3 --lr 3e-4
+    python -m oracle.learned_gcr --n 16 --train 16 --epochs 3 --lr 3e-4 [--step 1]
 """
 from __future__ import annotations
 
@@ -97,8 +97,9 @@ def first_below(h, tol):
     return int(np.argmax(h < tol)) if (h < tol).any() else -1
 
 
-def compare(prm, mb, m=20, iters=60, eps=1e-8):
-    """Residual histories of GCR(m) with K = ILU and K = ILU + net on one system."""
+def compare(prm, mb, m=20, iters=60, eps=1e-8, step=0):
+    """Residual histories of GCR(m) with K = ILU and K = ILU + net on one system
+    (step 1: the correction scaled by its least-squares step, mpnn.apply_step)."""
     P = port()
     g = M.Graph(mb.A.val, mb.A.cind, mb.A.rptr)
 
@@ -106,7 +107,8 @@ def compare(prm, mb, m=20, iters=60, eps=1e-8):
         return P.ilu_apply(mb.L, mb.U, r, mb.cptr, mb.cnum, 16)
 
     h0 = gcr_history(mb.A, mb.b, ilu, m, iters)
-    h1 = gcr_history(mb.A, mb.b, lambda r: M.apply(prm, g, r, ilu(r), rounding=False), m, iters)
+    K = M.apply_step if step else M.apply
+    h1 = gcr_history(mb.A, mb.b, lambda r: K(prm, g, r, ilu(r), rounding=False), m, iters)
     return dict(plain_iters=first_below(h0, eps), learned_iters=first_below(h1, eps),
                 plain_res=[float(h0[i]) for i in range(0, iters + 1, 10)],
                 learned_res=[float(h1[i]) for i in range(0, iters + 1, 10)])
@@ -124,13 +126,14 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--test", type=int, default=3)
+    ap.add_argument("--step", type=int, default=0, help="1: least-squares step of the correction")
     args = ap.parse_args(argv)
     members = lambda: (family_member(args.n, s) for s in range(1000, 1000 + args.train))
     prm, losses = train(members, args.epochs, args.lr)
     out = dict(n=args.n, train_systems=args.train, epochs=args.epochs, lr=args.lr,
                loss_first=float(np.mean(losses[:8])), loss_last=float(np.mean(losses[-8:])), systems=[])
     for s in range(900000, 900000 + args.test):
-        out["systems"].append(dict(seed=s, **compare(prm, family_member(args.n, s))))
+        out["systems"].append(dict(seed=s, **compare(prm, family_member(args.n, s), step=args.step)))
     print(json.dumps(out))
 
 

@@ -121,6 +121,19 @@ def apply(P, g: Graph, r, ilu, rounding=True):
     return np.asarray(ilu, np.float64) + cache["rms"] / g.d * c
 
 
+def apply_step(P, g: Graph, r, ilu, rounding=True):
+    """K(r) = ILU(r) + alpha c with c = (rms / d) net(r) and
+    alpha = (q . A c) / (A c . A c), q = r - A ILU(r): the alpha minimising
+    |r - A K(r)| (senk_mpnn_set_step mode 1; 0 when A c = 0)."""
+    c, cache = forward(P, g, r, rounding)
+    ct = cache["rms"] / g.d * c
+    ilu = np.asarray(ilu, np.float64)
+    y = g.A @ ct
+    q = np.asarray(r, np.float64) - g.A @ ilu
+    den = float(y @ y)
+    return ilu + (float(q @ y) / den if den > 0 else 0.0) * ct
+
+
 def loss_grad(P, g: Graph, r, ilu, e, rounding=True, mode=1):
     """(loss, gradient) for one residual/error pair, as senk_mpnn_loss_grad.
     mode 1 (residual space): q = (r - A ILU(r)) / rms, loss = |A c / d - q|^2 / |q|^2;

@@ -265,6 +265,47 @@ __global__ void __launch_bounds__(kThreads) k_decode_c(const float *H, const flo
     if (lane == 0) c[i] = v + P[kOffBout];
 }
 
+// Least-squares step of the correction: alpha = (q . y) / (y . y) with
+// q = r - A u (u = ILU(r)) and y = A c (c the scaled correction), i.e. the alpha
+// that minimises |r - A (u + alpha c)|; 0 when y = 0. Last CTA finishes; part
+// holds 2 * gridDim.x partials.
+__global__ void __launch_bounds__(kThreads)
+k_step_alpha(const double *r, const double *au, const double *y, long long n, double *part, unsigned *ticket,
+             double *alpha)
+{
+    double a = 0, b = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double yi = y[i];
+        a += (r[i] - au[i]) * yi;
+        b += yi * yi;
+    }
+    __shared__ double sh[32];
+    a = block_sum(a, sh);
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+    if (last_cta_arrives(ticket, gridDim.x)) {
+        double ta = 0, tb = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+            ta += part[i];
+            tb += part[gridDim.x + i];
+        }
+        ta = block_sum(ta, sh);
+        tb = block_sum(tb, sh);
+        if (threadIdx.x == 0) *alpha = tb > 0 ? ta / tb : 0.0;
+    }
+}
+
+// out += alpha * c
+__global__ void __launch_bounds__(kThreads) k_add_step(double *out, const double *c, const double *alpha, long long n)
+{
+    const double a = *alpha;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] += a * c[i];
+}
+
 // Error-space loss: dc = 2 (c - t) / acc[0]; acc[1] += sum (c - t)^2
 __global__ void __launch_bounds__(kThreads) k_loss_error(const float *c, const float *t, float *dc, double *acc, long long n)
 {
@@ -380,8 +421,10 @@ struct Mpnn {
     DevBuf<int> ar, ac, atr, atc; // A and A^T (CSR, FP32 values) for the residual-space loss
     DevBuf<float> av, atv, cbuf, dcb, ebuf;
     DevBuf<double> ailu;          // A ILU(r)
+    DevBuf<double> cstep, acstep, alpha;  // scaled correction c, A c, and the step alpha
     int loss_mode = 1;            // 0: error space, 1: residual space
     float clip = 1.0f;            // global gradient-norm clip of the Adam step (<= 0: off)
+    int step_mode = 0;            // 0: K = ILU + c, 1: K = ILU + alpha c (least-squares alpha)
     DevBuf<float> gnorm;
     // activations
     DevBuf<bf16> X[kLayers], Z[kLayers], dZ;
@@ -406,7 +449,7 @@ struct Mpnn {
         SENK_CUDA(cudaMemset(status.p, 0, sizeof(int)));
         gnorm.alloc(1);
         rms.alloc(2);
-        red.alloc(kNumSMs * 4);
+        red.alloc(kNumSMs * 8);  // two partials per CTA for k_step_alpha
         acc.alloc(2);
         ticket.alloc(1);
         SENK_CUDA(cudaMemset(ticket.p, 0, sizeof(unsigned)));
@@ -508,6 +551,9 @@ struct Mpnn {
             dcb.alloc(N);
             ebuf.alloc(N);
             ailu.alloc(N);
+            cstep.alloc(N);
+            acstep.alloc(N);
+            alpha.alloc(1);
         }
         SENK_CUDA(cudaStreamSynchronize(s));
     }
@@ -540,6 +586,29 @@ struct Mpnn {
     {
         forward<T>(r, s, false);
         k_decode_apply<T><<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(H[kLayers].p, P.p, rms.p, 1.f / d, out, n);
+        SENK_LAUNCH_CHECK();
+    }
+
+    // The GCR hook: out holds u = ILU(r) on entry; with step_mode 1,
+    // out = u + alpha c where c = (rms / d) net(r) and alpha minimises
+    // |r - A(u + alpha c)| (two SpMVs with the system's A and one reduction, no
+    // host synchronisation, so it stays inside a captured graph).
+    void apply_step(const SpmvOp<double> &A, const double *r, double *out, cudaStream_t s)
+    {
+        if (step_mode == 0) {
+            apply<double>(r, out, s);
+            return;
+        }
+        forward<double>(r, s, false);
+        SENK_CUDA(cudaMemsetAsync(cstep.p, 0, sizeof(double) * n, s));
+        k_decode_apply<double><<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(H[kLayers].p, P.p, rms.p, 1.f / d,
+                                                                               cstep.p, n);
+        SENK_LAUNCH_CHECK();
+        A.apply(out, ailu.p, s, nullptr);
+        A.apply(cstep.p, acstep.p, s, nullptr);
+        const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
+        k_step_alpha<<<rg, kThreads, 0, s>>>(r, ailu.p, acstep.p, n, red.p, ticket.p, alpha.p);
+        k_add_step<<<rg, kThreads, 0, s>>>(out, cstep.p, alpha.p, n);
         SENK_LAUNCH_CHECK();
     }
 
@@ -623,7 +692,7 @@ void learned_apply(void *net, const void *sys, const double *v, double *out, cud
 {
     Mpnn *m = static_cast<Mpnn *>(net);
     SENK_REQUIRE(m->bound == sys, "the network is bound to another system");
-    m->apply<double>(v, out, s);
+    m->apply_step(static_cast<const System<double> *>(sys)->A, v, out, s);
 }
 
 }  // namespace senkgpu
@@ -696,6 +765,17 @@ int senk_mpnn_set_clip(senk_mpnn *net, float clip)
     return guarded("senk_mpnn_set_clip", [&] {
         SENK_REQUIRE(net, "null network");
         net->net.clip = clip;
+        return (int)kOk;
+    });
+}
+
+// Step of the correction inside the GCR: 0 = K(r) = ILU(r) + c (default),
+// 1 = K(r) = ILU(r) + alpha c with the least-squares alpha.
+int senk_mpnn_set_step(senk_mpnn *net, int mode)
+{
+    return guarded("senk_mpnn_set_step", [&] {
+        SENK_REQUIRE(net && (mode == 0 || mode == 1), "mode must be 0 or 1");
+        net->net.step_mode = mode;
         return (int)kOk;
     });
 }

@@ -65,6 +65,11 @@ class Net:
         """Training objective: 1 = residual space (default), 0 = error space."""
         check("senk_mpnn_set_loss", lib().senk_mpnn_set_loss(self._h, mode))
 
+    def set_step(self, mode: int):
+        """Step of the correction in the GCR: 0 = ILU + c, 1 = ILU + alpha c with
+        the least-squares alpha."""
+        check("senk_mpnn_set_step", lib().senk_mpnn_set_step(self._h, mode))
+
     def bind(self, sysm: System):
         check("senk_mpnn_bind", lib().senk_mpnn_bind(self._h, sysm._h))
 
@@ -242,9 +247,11 @@ def main(argv=None):
     ap.add_argument("--m", type=int, default=20)
     ap.add_argument("--loss", type=int, default=1, help="1 residual space, 0 error space")
     ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
+    ap.add_argument("--step", type=int, default=0, help="1: least-squares step of the correction in the GCR")
     args = ap.parse_args(argv)
     net = Net(seed=0)
     net.set_loss(args.loss)
+    net.set_step(args.step)
     check("senk_mpnn_set_clip", lib().senk_mpnn_set_clip(net._h, args.clip))
     t0 = time.perf_counter()
     losses = train(torch, net, args.n, range(1000, 1000 + args.train), args.epochs, args.lr)

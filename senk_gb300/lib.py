@@ -139,6 +139,7 @@ def _declare(L):
     d("senk_mpnn_bind", [_P, _P])
     d("senk_mpnn_set_loss", [_P, _I])
     d("senk_mpnn_set_clip", [_P, _Fl])
+    d("senk_mpnn_set_step", [_P, _I])
     d("senk_mpnn_loss_grad", [_P, _P, _P, _P, C.POINTER(_D), _P])
     d("senk_mpnn_train_step", [_P, _P, _P, _P, _Fl, C.POINTER(_D)])
     d("senk_mpnn_apply", [_P, _P, _P, _P])

@@ -80,3 +80,16 @@ def test_learned_gcr_history_is_iluGcrm_between_restarts():
     assert conv and it == -(-k // m) * m
     for c in range(0, 80, m):
         assert np.all(np.diff(h[c:c + m + 1]) <= 1e-12 * h[c])
+
+
+def test_least_squares_step_never_worsens_one_application():
+    """|r - A K(r)| with K = ILU + alpha c (alpha the least-squares step) is at
+    most |r - A ILU(r)|, whatever the network's output; the fixed step has no
+    such bound."""
+    g, r, ilu, e, params = _case(3)
+    params[M.OFF_WOUT:M.OFF_BOUT] = 50.0  # a large, useless correction
+    base = np.linalg.norm(r - g.A @ ilu)
+    ks = M.apply_step(params, g, r, ilu, rounding=False)
+    kf = M.apply(params, g, r, ilu, rounding=False)
+    assert np.linalg.norm(r - g.A @ ks) <= base * (1 + 1e-12)
+    assert np.linalg.norm(r - g.A @ kf) > base
