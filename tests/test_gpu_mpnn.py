@@ -115,6 +115,22 @@ def test_training_lowers_the_loss_and_flexible_gcr_converges(torch):
         net.close()
 
 
+def test_least_squares_step_gcr_converges(torch):
+    """K = ILU + alpha c with the least-squares alpha (senk_mpnn_set_step 1),
+    computed on the device inside the GCR cycle graph: the solve converges to
+    the FP64 true residual, in no more restart cycles than one over plain ILU."""
+    net = LN.Net(seed=0)
+    try:
+        LN.train(torch, net, 16, seeds=range(100, 116), epochs=3, lr=3e-4)
+        net.set_step(1)
+        for s in (900, 901):
+            c = LN.compare_gcr(net, LN.family_member(16, s), m=20)
+            assert c["learned"]["converged"] and c["learned"]["true_res"] < 1e-8
+            assert c["learned"]["iters"] <= c["plain"]["iters"] + 20
+    finally:
+        net.close()
+
+
 def test_stagnating_network_falls_back_to_plain_ilu(torch):
     mb = LN.family_member(16, 902)
     p = M.init_params(1)
