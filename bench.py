@@ -160,7 +160,8 @@ def peaks():
 def learned_leg(n=16, train_seeds=range(100, 116), test_seeds=(900, 901, 902), epochs=3):
     """Plain ILU(0)-GCR(20) against flexible GCR(20) with K = ILU + net on held-out
     systems of the variable-coefficient family (n^3), the network trained on the
-    GPU first (residual-space objective, Adam 3e-4, clipped)."""
+    GPU first (residual-space objective, Adam 3e-4, clipped); `lsq_step_*`: the
+    same network with its correction scaled by the least-squares step."""
     import torch
 
     from senk_gb300 import learned as LN
@@ -169,6 +170,8 @@ def learned_leg(n=16, train_seeds=range(100, 116), test_seeds=(900, 901, 902), e
     losses = LN.train(torch, net, n, train_seeds, epochs, 3e-4)
     train_s = time.perf_counter() - t0
     rows = [LN.compare_gcr(net, LN.family_member(n, s), m=20) for s in test_seeds]
+    net.set_step(1)  # the same network, its correction scaled by the least-squares step
+    rows_ls = [LN.compare_gcr(net, LN.family_member(n, s), m=20) for s in test_seeds]
     net.close()
     return {"family": f"vardiff3d {n}^3, sigma~U[0.5,2], corr~U[4,16], ABMC 16, ILU(0), GCR(20), 1e-8",
             "train_systems": len(train_seeds), "epochs": epochs, "pairs": len(losses), "train_s": round(train_s, 2),
@@ -177,7 +180,11 @@ def learned_leg(n=16, train_seeds=range(100, 116), test_seeds=(900, 901, 902), e
             "plain_ms": [round(r["plain"]["ms"], 3) for r in rows],
             "learned_ms": [round(r["learned"]["ms"], 3) for r in rows],
             "learned_true_res": [r["learned"]["true_res"] for r in rows],
-            "fallback_cycle": [r["learned"]["fallback_cycle"] for r in rows]}
+            "fallback_cycle": [r["learned"]["fallback_cycle"] for r in rows],
+            "plain_true_res": [r["plain"]["true_res"] for r in rows],
+            "lsq_step_iters": [r["learned"]["iters"] for r in rows_ls],
+            "lsq_step_ms": [round(r["learned"]["ms"], 3) for r in rows_ls],
+            "lsq_step_true_res": [r["learned"]["true_res"] for r in rows_ls]}
 
 
 def traffic_for(kernel):
