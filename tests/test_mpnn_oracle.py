@@ -93,3 +93,15 @@ def test_least_squares_step_never_worsens_one_application():
     kf = M.apply(params, g, r, ilu, rounding=False)
     assert np.linalg.norm(r - g.A @ ks) <= base * (1 + 1e-12)
     assert np.linalg.norm(r - g.A @ kf) > base
+
+
+@pytest.mark.parametrize("step", [0, 1])
+def test_untrained_network_leaves_gcr_as_plain_ilu(step):
+    """The initial parameters have a zero output layer, so K = ILU exactly under
+    either step and the GCR residual histories coincide."""
+    from oracle import learned_gcr as LG
+    from senk_gb300.learned import family_member
+
+    c = LG.compare(M.init_params(0).astype(np.float64), family_member(8, 4321), m=5, iters=40, step=step)
+    assert c["plain_iters"] == c["learned_iters"] > 0
+    assert np.allclose(c["plain_res"], c["learned_res"], rtol=1e-12, atol=0)
