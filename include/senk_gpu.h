@@ -71,11 +71,12 @@ typedef struct {
     int sweep;        /* SENK_SWEEP_* */
 } senk_options;
 
-/* How the ILU sweeps of ABMC chains (bsize >= 2) are scheduled. */
-#define SENK_SWEEP_AUTO 0     /* the faster schedule as measured: one launch per colour */
+/* How the ILU sweeps of AMC/ABMC factors are scheduled. */
+#define SENK_SWEEP_AUTO 0     /* the faster schedule as measured: dataflow */
 #define SENK_SWEEP_COLOURS 1  /* one launch per colour */
-#define SENK_SWEEP_DATAFLOW 2 /* one launch per sweep: groups of 32 chains wait on
-                                 per-group flags of the groups they read */
+#define SENK_SWEEP_DATAFLOW 2 /* one launch per sweep: each warp takes a group of 32
+                                 chains, waits on the flags of the groups it reads,
+                                 solves it and publishes its own flag */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0
@@ -288,9 +289,23 @@ int senk_system_gmres_ir(senk_system *sys, double nrm_b, int max_outer, int m, d
                          double inner_tol, int inner_cycles, senk_result *res);
 
 /* Restarted GCR(m) on the resident system (include/senk_gcr.hpp:30-91 /
- * 93-161): one CUDA graph per restart cycle. */
+ * 93-161, and IlubGcrm :163-231 for ILUB systems): one CUDA graph per restart
+ * cycle. */
 int senk_system_gcr(senk_system *sys, double nrm_b, int outer, int m, double epsilon,
                     senk_result *res);
+/* y = K x with the system's preconditioner (ILU or ILUB application, the
+ * reference's SptrsvCsr_l/_u or SptrsvBcsr_l/_u pair as its solvers apply it,
+ * e.g. include/senk_gcr.hpp:119-120); x and y are device vectors of the
+ * system's dtype. Synchronous; reports a sweep whose bounded wait ran out. */
+int senk_system_apply_pc(senk_system *sys, const void *x, void *y);
+/* Mixed-precision GCR iterative refinement on a system created with
+ * desc->mixed = 1 (new, like senk_system_gmres_ir): FP64 outer residual
+ * r = b - A x and update x += ||r|| d, stopping on the FP64 true residual
+ * (||r|| <= epsilon * nrm_b); d from FP32 GCR(m) (the reference's IluGcrm /
+ * IlubGcrm recurrence, include/senk_gcr.hpp:93-231, on FP32 A, factors and
+ * vectors) to inner_tol or inner_cycles restart cycles. res as for GMRES-IR. */
+int senk_system_gcr_ir(senk_system *sys, double nrm_b, int max_outer, int m, double epsilon,
+                       double inner_tol, int inner_cycles, senk_result *res);
 /* BiCGStab on the resident system (include/senk_bicgstab.hpp:29-105 / 107-196):
  * one CUDA graph per iteration, launched a few at a time; res->iters is exact. */
 int senk_system_bicgstab(senk_system *sys, double nrm_b, int max_iter, double epsilon,
@@ -346,14 +361,17 @@ int senk_dev_nrm2_d(const double *x, int N, double *result, void *stream);
  * No counterpart in the reference. It is for callers that cannot allocate at the
  * point of the call: applications that hand all GPU memory to their own pool at
  * start-up and forbid later cudaMalloc, and latency-critical loops where
- * cudaMalloc/cudaFree could synchronise the device. Same kernel and results as
- * senk_dev_dot_d per column, but its reduction scratch is a fixed 39,168-byte
+ * cudaMalloc/cudaFree could synchronise the device. Same kernel as
+ * senk_dev_dot_d per column; the CTA partition can differ, so results agree to
+ * rounding, not bit for bit. Its reduction scratch is a fixed 39,168-byte
  * array inside the library's device image, held by every GPU that loads the
  * library until the process exits. Limits: 1 <= nv <= 16 (other values return
- * SENK_ERR_ARG). The first call on each device looks up that array's device
- * address; make it before any stream capture. All calls share the one array
- * (each call clears what must start at zero), so calls that overlap on the GPU,
- * e.g. on two streams at once, race and give wrong results. */
+ * SENK_ERR_ARG); at most 304 CTAs per column block. The first call on each
+ * device looks up that array's device address and keeps it for the life of the
+ * process; make it before any stream capture, and do not call cudaDeviceReset
+ * between calls. All calls share the one array (each call clears what must
+ * start at zero), so calls that overlap on the GPU, e.g. on two streams at
+ * once, race and give wrong results. */
 int senk_dev_multidot_d_noalloc(const double *V, long long ldv, int nv, const double *w, int N,
                                 double *out, void *stream);
 /* senk::blas1::HadProd / HadDiv (include/senk_blas1.hpp:120-136): y *= x, y /= x */
@@ -383,10 +401,29 @@ int senk_ilub_plan_create(senk_ilu_plan **out, int N, int bnl, int bnw,
                           const double *blval, const int *blcind, const int *blrptr,
                           const double *buval, const int *bucind, const int *burptr,
                           const int *cptr, int cnum, int bsize);
-/* y = U^-1 L^-1 x (device vectors of the plan's dtype); x == y allowed. */
+/* senk_ilu_plan_create with the sweep schedule chosen (SENK_SWEEP_*): AUTO and
+ * DATAFLOW sweep AMC/ABMC factors in one launch per triangular sweep, COLOURS
+ * in one launch per colour. The natural order always runs level set by level
+ * set. */
+int senk_ilu_plan_create_sched(senk_ilu_plan **out, int dtype, int N,
+                               const void *lval, const int *lcind, const int *lrptr,
+                               const void *uval, const int *ucind, const int *urptr,
+                               int precond, const int *cptr, int cnum, int bsize, int sweep);
+/* y = U^-1 L^-1 x (device vectors of the plan's dtype); x == y allowed.
+ * Enqueued on `stream` without waiting: a sweep whose bounded wait ran out
+ * (it then leaves y incomplete) is reported by senk_ilu_plan_status. */
 int senk_ilu_plan_apply(senk_ilu_plan *plan, const void *x, void *y, void *stream);
 /* One triangular sweep: y = L^-1 x (upper=0) or y = U^-1 x (upper=1). */
 int senk_ilu_plan_sweep(senk_ilu_plan *plan, int upper, const void *x, void *y, void *stream);
+/* Waits for the device, then returns SENK_ERR_CUDA (with a message naming the
+ * wait) if a sweep of this plan gave up on a bounded wait since the last call,
+ * else SENK_OK; the report is cleared. */
+int senk_ilu_plan_status(senk_ilu_plan *plan, void *stream);
+/* For tests of the error path: makes `group` of the dataflow sweep (upper = 0:
+ * L, 1: U) wait on its own flag, which is never set before the group runs, so
+ * its bounded wait runs out (about a second) on the next sweep. The plan keeps
+ * this defect; destroy it afterwards. */
+int senk_ilu_plan_test_stall(senk_ilu_plan *plan, int upper, int group);
 int senk_ilu_plan_destroy(senk_ilu_plan *plan);
 
 /* ============================================= learned preconditioner ==

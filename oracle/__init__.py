@@ -25,7 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libsenk_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsenk_ref.so")
-REF_INCLUDE = "/root/reference/include"
+# The reference's include/ directory, for the live pins; given by the caller
+# (build(ref_include=...)) or the SENK_REF_INCLUDE environment variable.
+REF_INCLUDE = os.environ.get("SENK_REF_INCLUDE", "")
 
 PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC, PC_ILU_BJ, PC_ILUB, PC_ILUB_ABMC = range(7)
 OP_CSR, OP_BCSR = 0, 1
@@ -36,11 +38,15 @@ _D = C.c_double
 _F = C.c_float
 
 
-def build(ref: bool = True) -> None:
-    """Compile the C restatement, and the reference shim when its sources exist."""
+def build(ref: bool = True, ref_include: str | None = None) -> None:
+    """Compile the C restatement, and the reference shim when the reference's
+    include/ directory (ref_include, else SENK_REF_INCLUDE) exists."""
+    global REF_INCLUDE
+    if ref_include:
+        REF_INCLUDE = ref_include
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    if ref and os.path.isdir(REF_INCLUDE):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if ref and REF_INCLUDE and os.path.isdir(REF_INCLUDE):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_INCLUDE={REF_INCLUDE}"], check=True)
 
 
 def _ptr(a):
@@ -312,24 +318,25 @@ class Port(_Lib):
         t = self.sptrsv(L, x, False, cptr, cnum, bsize, amc, dtype)
         return self.sptrsv(U, t, True, cptr, cnum, bsize, amc, dtype)
 
-    def ilub_sweep(self, F, x, upper, bnl, bnw, cptr=None, cnum=0, bsize=0):
+    def ilub_sweep(self, F, x, upper, bnl, bnw, cptr=None, cnum=0, bsize=0, dtype=np.float64):
         """SptrsvBcsr_l/_u on a BCSR factor F = (bval, bcind, brptr); sequential or
-        ABMC (cptr counting blocks of bsize rows)."""
-        bv, bc, br = (np.ascontiguousarray(F[0], np.float64), _i32(F[1]), _i32(F[2]))
-        x = np.ascontiguousarray(x, np.float64)
-        y = np.zeros(x.size)
+        ABMC (cptr counting blocks of bsize rows); dtype float64 or float32."""
+        s = self._sfx(dtype)
+        bv, bc, br = (np.ascontiguousarray(F[0], dtype), _i32(F[1]), _i32(F[2]))
+        x = np.ascontiguousarray(x, dtype)
+        y = np.zeros(x.size, dtype)
         side = "u" if upper else "l"
         if cptr is None:
-            f = self.fn(f"sptrsv_bcsr_{side}_d", [_P, _P, _P, _P, _P, _I, _I, _I])
+            f = self.fn(f"sptrsv_bcsr_{side}{s}", [_P, _P, _P, _P, _P, _I, _I, _I])
             f(_ptr(bv), _ptr(bc), _ptr(br), _ptr(x), _ptr(y), x.size, bnl, bnw)
         else:
-            f = self.fn(f"sptrsv_bcsr_{side}_abmc_d", [_P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I])
+            f = self.fn(f"sptrsv_bcsr_{side}_abmc{s}", [_P, _P, _P, _P, _P, _I, _P, _I, _I, _I, _I])
             f(_ptr(bv), _ptr(bc), _ptr(br), _ptr(x), _ptr(y), x.size, _ptr(_i32(cptr)), cnum, bsize, bnl, bnw)
         return y
 
-    def ilub_apply(self, Lb, Ub, x, bnl, bnw, cptr=None, cnum=0, bsize=0):
-        t = self.ilub_sweep(Lb, x, False, bnl, bnw, cptr, cnum, bsize)
-        return self.ilub_sweep(Ub, t, True, bnl, bnw, cptr, cnum, bsize)
+    def ilub_apply(self, Lb, Ub, x, bnl, bnw, cptr=None, cnum=0, bsize=0, dtype=np.float64):
+        t = self.ilub_sweep(Lb, x, False, bnl, bnw, cptr, cnum, bsize, dtype)
+        return self.ilub_sweep(Ub, t, True, bnl, bnw, cptr, cnum, bsize, dtype)
 
     def dot(self, x, y):
         f = self.fn("dot_d", [_P, _P, _I], _D)
@@ -483,7 +490,7 @@ def ref(threads: int = 1):
     global _ref
     if _ref is None:
         if not os.path.exists(REF_SO):
-            if not os.path.isdir(REF_INCLUDE):
+            if not (REF_INCLUDE and os.path.isdir(REF_INCLUDE)):
                 return None
             build(ref=True)
         _ref = Ref()

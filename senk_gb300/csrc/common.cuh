@@ -38,17 +38,32 @@ struct CudaError {
 #define SENK_LAUNCH_CHECK() SENK_CUDA(cudaGetLastError())
 
 // ---------------------------------------------------------------- geometry
-constexpr int kNumSMs = 152;    // GB300: 2 dies x 76 SMs
+constexpr int kNumSMs = 152;    // GB300 (2 dies x 76 SMs): used only if the device query fails
 constexpr int kThreads = 256;   // default CTA size of the streaming kernels
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// SMs of the current device (cudaDevAttrMultiProcessorCount), looked up once per
+// device; kNumSMs if the query fails.
+inline int sm_count()
+{
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kNumSMs;
+    if (cache[dev] <= 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return kNumSMs;
+        cache[dev] = v;
+    }
+    return cache[dev];
+}
 
 // Grid size for a grid-stride streaming kernel: enough CTAs for every SM to hold
 // `per_sm` resident CTAs, but never more than the work needs.
 inline int stream_grid(long long n_items, int items_per_cta, int per_sm = 4)
 {
     long long need = (n_items + items_per_cta - 1) / items_per_cta;
-    long long cap = (long long)kNumSMs * per_sm;
+    long long cap = (long long)sm_count() * per_sm;
     if (need < 1) need = 1;
     return (int)(need < cap ? need : cap);
 }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -85,16 +86,19 @@ struct DevBuf {
 };
 
 // Partials + ticket for the last-CTA-finishes reductions. One per stream: the
-// reduction kernels of a stream run one after another and share it.
+// reduction kernels of a stream run one after another and share it. `ctas`
+// (4 per SM of the device) is the grid of the multi-dot and update kernels;
+// the partials hold kMaxCols columns of that many CTAs.
 struct ReduceScratch {
     static constexpr int kMaxCols = 64;
-    static constexpr int kMaxCtas = 4 * kNumSMs;
+    int ctas = 0;
     DevBuf<double> part;
     DevBuf<unsigned> ticket;
     void ensure(cudaStream_t s)
     {
         if (!part.p) {
-            part.alloc((size_t)kMaxCols * kMaxCtas);
+            ctas = 4 * sm_count();
+            part.alloc((size_t)kMaxCols * ctas);
             ticket.alloc(1);
             SENK_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
         }
@@ -158,10 +162,17 @@ struct SweepFactor {
     std::vector<size_t> colour_smem; // bytes to stage the largest group of each colour
     long long elems = 0;           // padded slots
     long long nnz = 0;             // stored off-diagonal entries (+N for U's diagonal)
-    // dataflow sweep (chains of bs >= 2 rows): the groups each group reads from
+    // dataflow sweep (compact chain layout, one warp per group): groups, chain
+    // descriptors, the groups each group reads from, per-group flags and the
+    // launch's control words
     bool dataflow = false;
+    DevBuf<WfGroup> wgroups;
+    DevBuf<int2> wchains;
     DevBuf<int> dep_ptr, dep_idx, flags, ctrl;
-    int df_grid = 0;
+    int ngroups = 0;
+    int slots_max = 0;             // widest group block (slots of 32 entries)
+    int wf_warps = 0, wf_grid = 0; // warps per CTA, CTAs
+    size_t wf_smem = 0;            // dynamic shared memory per CTA
 };
 
 // A split ILU factorisation with its sweep schedule.
@@ -170,10 +181,11 @@ struct IluPlan {
     int n = 0;
     int precond = SENK_PC_NONE;
     SweepFactor<VT> L, U;
-    DevBuf<int> status;  // set to 1 by a sweep whose TMA wait ran out
+    DevBuf<int> status;  // non-zero after a sweep whose bounded wait ran out (1: flag, 2: TMA)
 
-    // sweep_mode: SENK_SWEEP_AUTO (dataflow sweeps for chains of 2+ rows) or
-    // SENK_SWEEP_COLOURS (one launch per colour)
+    // sweep_mode: SENK_SWEEP_AUTO / SENK_SWEEP_DATAFLOW (one dataflow launch per
+    // sweep where the schedule is colours of chains) or SENK_SWEEP_COLOURS (one
+    // launch per colour)
     void build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
                const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s,
                int sweep_mode = 0);
@@ -188,7 +200,8 @@ struct IluPlan {
     // Algorithmic bytes of one application (values + indices once, x read once,
     // y written once per sweep and re-read by the U sweep), for roofline figures.
     long long apply_bytes() const;
-    // Throws if a sweep reported a failed wait (synchronises the stream).
+    // Throws if a sweep reported a failed wait, and clears the report
+    // (synchronises the stream).
     void check_status(cudaStream_t s) const;
 };
 
@@ -279,6 +292,14 @@ struct System {
     bool ir_only = false;  // desc.mixed == 2: the FP64 part serves GMRES-IR's outer loop only
     int gmres_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
                  senk_result *res);
+    // FP64 outer refinement around FP32 inner GCR(m) (mixed = 1 systems)
+    int gcr_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
+               senk_result *res);
+    // The refinement loop: r = b - A x in FP64 until ||r|| <= eps nrm_b; each
+    // step solves the FP32 system for r / ||r|| with inner_solve and adds
+    // ||r|| d to x.
+    int refine(double nrm_b, int max_outer, double eps, senk_result *res,
+               const std::function<void(senk_result *)> &inner_solve);
     void ensure_gmres(int m);
     void enqueue_gmres_cycle(int m);
     int gmres(double nrm_b, int outer, int m, double eps, senk_result *res);

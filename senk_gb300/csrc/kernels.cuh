@@ -10,6 +10,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "wf_layout.hpp"
 
 namespace senkgpu {
 
@@ -645,15 +646,34 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
 }
 
 // ------------------------------------------------------ dataflow sweeps
-// One launch per triangular sweep: CTAs take groups in processing order from a
-// counter, wait until every group their rows read from has published its flag
-// for this sweep, solve the group as k_sweep does, and publish their own flag.
-// A group only reads groups of earlier colours, which were taken earlier by
-// running CTAs, so every wait ends. ctrl = {counter, epoch, abort}: the epoch
-// numbers the sweeps (flags hold the epoch of the sweep that set them), a wait
-// that runs out of polls sets abort and *status, and every later wait gives up
-// at once.
-constexpr unsigned kFlagPolls = 1u << 20;
+// One launch per triangular sweep, one group of up to 32 chains per warp.
+//
+// Layout ("compact chains"): the chains of a colour are sorted by their entry
+// counts and taken 32 at a time; chain q of group g is lane q. Its external
+// entries (columns of other chains, all in earlier colours) are packed one
+// after another, entry k at off + k*32 + q, followed after the group's widest
+// chain by its in-chain entries, so a group pads only to its widest chain
+// (chains of similar counts are grouped). Both parts list rows in solve order
+// and each row's entries in the reference's subtraction order. Column words:
+// external (row << 27) | column, in-chain (row << 8) | chain-local column,
+// rows chain-local. Per chain: int2 {first row, E | I << 16}, E and I its
+// external and in-chain entry counts.
+//
+// Schedule: warps take groups in processing order from a counter, stage the
+// group's block into their shared memory with two TMA bulk copies, read x of
+// their chains' rows, and wait until every group their external columns belong
+// to has published its flag for this sweep (flags hold the sweep's epoch;
+// acquire/release at GPU scope). A group only reads groups taken before it by
+// running warps, so every wait ends. Then, per lane: the external entries'
+// products are gathered (all loads of a batch in flight together) and
+// subtracted row by row; the in-chain recurrence runs on chip in shared memory;
+// the rows are stored and the group's flag is published. The last warp to
+// finish resets the counter and starts the next epoch.
+//
+// ctrl = {counter, epoch, abort, warps finished}. A wait that runs out of polls
+// sets abort and *status; later waits give up at once; the launch then drains
+// and the last warp clears abort (the status stays set for the host).
+constexpr unsigned kFlagPolls = 1u << 21;  // polls of a dependency flag (64 ns back-off each) before giving up
 
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
@@ -667,138 +687,161 @@ __device__ __forceinline__ void st_release(int *p, int v)
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Starts a sweep: new epoch, counter back to 0 (one thread).
-static __global__ void k_df_begin(int *ctrl)
+template <typename T>
+__device__ __forceinline__ T ld_l2(const T *p) { return __ldcg(p); }
+
+// Shared memory of one warp: the staged block (columns, then values) of
+// slots_max slots, the chain rows tsh[BS][32] and, for U, the inverted diagonal
+// dsh[BS][32], then the warp's mbarrier (wf_bytes_for in wf_layout.hpp).
+template <typename VT, typename XT, int BS, bool UPPER>
+__host__ __device__ constexpr size_t wf_warp_bytes(int slots_max)
 {
-    ctrl[0] = 0;
-    ctrl[1] += 1;
+    return ((size_t)slots_max * 32 * (4 + sizeof(VT)) + (size_t)BS * 32 * sizeof(XT) * (UPPER ? 2 : 1) + 8 + 15) /
+           16 * 16;
 }
 
 template <typename VT, typename XT, int BS, bool UPPER>
-__global__ void __launch_bounds__(BS * 32)
-k_sweep_df(const GroupDesc *__restrict__ groups, int ng, const unsigned char *__restrict__ widths,
+__global__ void __launch_bounds__(256)
+k_sweep_wf(const WfGroup *__restrict__ groups, int ng, const int2 *__restrict__ chains,
            const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
            const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl, const XT *x,
-           XT *y, const int *gate, int *status, unsigned buf_bytes)
+           XT *y, const int *gate, int *status, int slots_max)
 {
-    static_assert(BS >= 2, "dataflow sweeps are for chains of two or more rows");
-    // Two staging buffers of buf_bytes (values, then columns, of one group):
-    // while warp 0 solves the current group's chains, warps 1.. fetch the next
-    // group and stage its block into the other buffer.
-    extern __shared__ __align__(16) unsigned char dfs[];
-    __shared__ XT tsh[BS][32];
-    __shared__ XT dsh[UPPER ? BS : 1][32];
-    __shared__ int wsh[2][2 * BS];
-    __shared__ GroupDesc dd[2];
-    __shared__ int item[2];
+    constexpr int G = sizeof(XT) == 4 ? 16 : 8;  // external entries gathered per batch
+    extern __shared__ __align__(128) unsigned char wfs[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const size_t per_warp = wf_warp_bytes<VT, XT, BS, UPPER>(slots_max);
+    unsigned char *base = wfs + (size_t)wib * per_warp;
+    int *cw = reinterpret_cast<int *>(base);
+    VT *vw = reinterpret_cast<VT *>(base + (size_t)slots_max * 32 * 4);
+    XT *tsh = reinterpret_cast<XT *>(base + (size_t)slots_max * 32 * (4 + sizeof(VT)));
+    XT *dsh = tsh + BS * 32;
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(base + per_warp - 16);
+    pdl_wait();  // the previous kernel (e.g. the other sweep) has finished
     if (gated(gate)) return;
-    const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
+    if (lane == 0) mbar_init(bar, 1);
+    __syncwarp();
     const int epoch = *(volatile const int *)(ctrl + 1);
-    // stage group g into buffer b (threads [t0, t0 + nt) of the CTA)
-    auto stage = [&](int g, int b, int t0, int nt) {
-        int slots = 0;
-#pragma unroll
-        for (int r = 0; r < 2 * BS; r++) slots += wsh[b][r];
-        const int vchunks = slots * 32 * (int)sizeof(VT) / 16, cchunks = slots * 32 * 4 / 16;
-        const uint4 *gv = reinterpret_cast<const uint4 *>(val + dd[b].off);
-        const uint4 *gc = reinterpret_cast<const uint4 *>(col + dd[b].off);
-        unsigned char *base = dfs + (size_t)b * buf_bytes;
-        uint4 *sv4 = reinterpret_cast<uint4 *>(base);
-        uint4 *sc4 = reinterpret_cast<uint4 *>(base + (size_t)slots * 32 * sizeof(VT));
-        for (int i = threadIdx.x - t0; i < vchunks; i += nt) sv4[i] = ld_stream(gv + i);
-        for (int i = threadIdx.x - t0; i < cchunks; i += nt) sc4[i] = ld_stream(gc + i);
-    };
-    // prologue: the first group
-    if (threadIdx.x == 0) item[0] = atomicAdd(ctrl, 1);
-    __syncthreads();
-    if (item[0] >= ng) return;
-    if (threadIdx.x < 2 * BS) wsh[0][threadIdx.x] = widths[(size_t)item[0] * 2 * BS + threadIdx.x];
-    if (threadIdx.x == 0) dd[0] = groups[item[0]];
-    __syncthreads();
-    stage(item[0], 0, 0, blockDim.x);
-    int cur = 0;
+    unsigned phase = 0;
     for (;;) {
-        const int g = item[cur];
-        const GroupDesc d = dd[cur];
-        // wait for the groups this one reads from
-        bool bad = false;
-        for (int i = dep_ptr[g] + threadIdx.x; i < dep_ptr[g + 1] && !bad; i += blockDim.x) {
-            const int *f = flags + dep_idx[i];
+        int g = 0;
+        if (lane == 0) g = atomicAdd(ctrl, 1);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ng) break;
+        const WfGroup d = groups[g];
+        const int slots = d.emax + d.imax;
+        // one read of the abort flag for the whole warp
+        bool ok = __shfl_sync(0xffffffffu, lane == 0 ? (int)(*(volatile const int *)(ctrl + 2) == 0) : 0, 0) != 0;
+        const bool staged = ok && slots > 0;
+        if (staged && lane == 0) {
+            mbar_expect_tx(bar, (unsigned)slots * 32u * (4u + (unsigned)sizeof(VT)));
+            bulk_g2s(cw, col + d.off, (unsigned)slots * 32u * 4u, bar);
+            bulk_g2s(vw, val + d.off, (unsigned)slots * 32u * (unsigned)sizeof(VT), bar);
+        }
+        const bool live = lane < d.nchains;
+        const int2 ch = live ? __ldg(chains + (size_t)g * 32 + lane) : make_int2(0, 0);
+        const int r0 = ch.x, E = ch.y & 0xffff, I = (int)((unsigned)ch.y >> 16);
+        // x of the chain's rows (and U's inverted diagonal) while the block arrives
+#pragma unroll
+        for (int l = 0; l < BS; l++) {
+            tsh[l * 32 + lane] = live ? x[r0 + l] : XT(0);
+            if (UPPER) dsh[l * 32 + lane] = live ? (XT)__ldg(dinv + r0 + l) : XT(0);
+        }
+        // the groups this one reads from
+        for (int i = dep_ptr[g] + lane; ok && i < dep_ptr[g + 1]; i += 32) {
+            const int *f = flags + __ldg(dep_idx + i);
             unsigned k = 0;
             while (ld_acquire(f) != epoch) {
-                __nanosleep(128);  // back off: spinning CTAs must not crowd out the producers' traffic
+                __nanosleep(64);
                 if (++k > kFlagPolls || *(volatile const int *)(ctrl + 2)) {
                     atomicExch(ctrl + 2, 1);
                     atomicExch(status, 1);
-                    bad = true;
+                    ok = false;
                     break;
                 }
             }
         }
-        if (threadIdx.x == 0) item[cur ^ 1] = atomicAdd(ctrl, 1);  // the next group
-        if (__syncthreads_or(bad)) return;  // (also: the staged block and item[cur ^ 1] are visible)
-        int eo = 0, etot = 0, slots = 0;
-#pragma unroll
-        for (int r = 0; r < BS; r++) {
-            if (r < l) eo += wsh[cur][r];
-            etot += wsh[cur][r];
-        }
-#pragma unroll
-        for (int r = 0; r < 2 * BS; r++) slots += wsh[cur][r];
-        const unsigned char *base = dfs + (size_t)cur * buf_bytes;
-        const VT *vb = reinterpret_cast<const VT *>(base);
-        const int *cb = reinterpret_cast<const int *>(base + (size_t)slots * 32 * sizeof(VT));
-        const bool live = q < d.nchains;
-        const int pos = d.pos0 + q * BS + l;
-        XT t = live ? x[pos] : XT(0);
-        const int we = wsh[cur][l];
-        for (int k = 0; k < we; k++) {
-            const int at = (eo + k) * 32 + q;
-            const int c = cb[at];
-            const VT v = vb[at];
-            if (c >= 0) t -= (XT)v * __ldcg(y + c);  // L2: written by other SMs in this launch
-        }
-        tsh[l][q] = t;
-        if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + pos) : XT(0);
-        __syncthreads();
-        const int gn = item[cur ^ 1];
-        if (l == 0) {
-            int io = etot;  // as in k_sweep: walked upwards for L, downwards for U
-            if (UPPER) {
-                for (int r = 0; r < BS; r++) io += wsh[cur][BS + r];
-            }
-#pragma unroll 4
-            for (int st = 0; st < BS; st++) {
-                const int r = UPPER ? BS - 1 - st : st;
-                XT tt = tsh[r][q];
-                const int wi = wsh[cur][BS + r];
-                if (UPPER) io -= wi;
-                const int ro = io;
-                if (!UPPER) io += wi;
-                for (int k = 0; k < wi; k++) {
-                    const int at = (ro + k) * 32 + q;
-                    const int c = cb[at];
-                    const VT v = vb[at];
-                    if (c >= 0) tt -= (XT)v * tsh[c][q];
+        ok = __all_sync(0xffffffffu, ok);
+        if (staged) {
+            const bool arrived = __all_sync(0xffffffffu, mbar_wait_bounded(bar, phase, kWaitLimit));
+            phase ^= 1u;
+            if (!arrived) {
+                // the copy did not complete: report, wait once more for it, and
+                // stop using this buffer (this warp takes no more groups)
+                if (lane == 0) {
+                    atomicExch(ctrl + 2, 1);
+                    atomicExch(status, 2);
                 }
-                if (UPPER) tt *= dsh[r][q];
-                tsh[r][q] = tt;
+                mbar_wait_bounded(bar, phase ^ 1u, kWaitLimit);
+                __syncwarp();
+                if (lane == 0) st_release(flags + g, epoch);
+                break;
             }
-        } else if (gn < ng) {
-            // warps 1..BS-1: describe and stage the next group
-            const int t = threadIdx.x - 32;
-            if (t < 2 * BS) wsh[cur ^ 1][t] = widths[(size_t)gn * 2 * BS + t];
-            if (t == 0) dd[cur ^ 1] = groups[gn];
-            asm volatile("bar.sync 1, %0;" ::"r"((BS - 1) * 32) : "memory");
-            stage(gn, cur ^ 1, 32, (BS - 1) * 32);
         }
-        __syncthreads();
-        if (live) y[pos] = tsh[l][q];
+        if (ok) {
+            // external entries: products gathered G at a time, subtracted row by row
+            XT t = XT(0);
+            int cur = -1;
+            for (int b = 0; b < d.emax; b += G) {
+                XT gv[G];
+#pragma unroll
+                for (int u = 0; u < G; u++) {
+                    const int e = b + u;
+                    gv[u] = XT(0);
+                    if (e < E) gv[u] = ld_l2(y + (cw[e * 32 + lane] & kColMask));
+                }
+#pragma unroll
+                for (int u = 0; u < G; u++) {
+                    const int e = b + u;
+                    if (e < E) {
+                        const int r = (int)((unsigned)cw[e * 32 + lane] >> kColBits);
+                        if (r != cur) {
+                            if (cur >= 0) tsh[cur * 32 + lane] = t;
+                            cur = r;
+                            t = tsh[r * 32 + lane];
+                        }
+                        t -= (XT)vw[e * 32 + lane] * gv[u];
+                    }
+                }
+            }
+            if (cur >= 0) tsh[cur * 32 + lane] = t;
+            // in-chain recurrence, rows in solve order
+            const int *iw = cw + d.emax * 32;
+            const VT *iv = vw + d.emax * 32;
+            int e = 0;
+#pragma unroll
+            for (int s = 0; s < BS; s++) {
+                const int r = UPPER ? BS - 1 - s : s;
+                XT tt = tsh[r * 32 + lane];
+                while (e < I) {
+                    const int w = iw[e * 32 + lane];
+                    if ((w >> 8) != r) break;
+                    tt -= (XT)iv[e * 32 + lane] * tsh[(w & 255) * 32 + lane];
+                    e++;
+                }
+                if (UPPER) tt *= dsh[r * 32 + lane];
+                tsh[r * 32 + lane] = tt;
+            }
+            if (live) {
+#pragma unroll
+                for (int l = 0; l < BS; l++) y[r0 + l] = tsh[l * 32 + lane];
+            }
+        }
         __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) st_release(flags + g, epoch);
-        if (gn >= ng) return;
-        cur ^= 1;
+        __syncwarp();
+        if (lane == 0) st_release(flags + g, epoch);
+    }
+    // the last warp to finish starts the next sweep's epoch
+    if (lane == 0) {
+        __threadfence();
+        const unsigned total = gridDim.x * (blockDim.x >> 5);
+        if ((unsigned)atomicAdd(ctrl + 3, 1) == total - 1) {
+            ctrl[0] = 0;
+            ctrl[2] = 0;
+            ctrl[3] = 0;
+            __threadfence();
+            atomicExch(ctrl + 1, epoch + 1);
+        }
     }
 }
 

@@ -7,6 +7,7 @@
 #include <cstdio>
 
 #include <chrono>
+#include <functional>
 
 #include "device.hpp"
 
@@ -34,7 +35,6 @@ struct PhaseClock {
 
 namespace {
 
-constexpr int kRedCtas = 4 * kNumSMs;  // CTAs of the multi-dot / update kernels
 
 template <typename T, int OP>
 void ew(const T *x, T *y, T *z, long long n, T a, T b, const double *a_dev, double a_mul, cudaStream_t s,
@@ -92,7 +92,6 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
     if (ir_only) {
         // nothing to build here for the preconditioner
     } else if (d.precond == SENK_PC_ILUB || d.precond == SENK_PC_ILUB_ABMC) {
-        SENK_REQUIRE(sizeof(T) == sizeof(double) && !d.mixed, "ILUB systems are FP64 only");
         SENK_REQUIRE((d.precond == SENK_PC_ILUB_ABMC) == (d.cptr != nullptr),
                      "SENK_PC_ILUB_ABMC needs cptr; SENK_PC_ILUB takes none");
         pcb = std::make_unique<IlubPlan<T>>();
@@ -137,7 +136,15 @@ void System<T>::create(const senk_system_desc &d, const senk_options *o, cudaStr
         di.dtype = SENK_F32;
         di.mixed = 0;
         di.val = nullptr;  // A comes from this system's device copy
-        if (d.precond != SENK_PC_NONE) {
+        if (d.precond == SENK_PC_ILUB || d.precond == SENK_PC_ILUB_ABMC) {
+            // BCSR factors: block row pointers of N / bnl block rows
+            SENK_REQUIRE(d.bnl > 0 && d.bnw > 0 && n % d.bnl == 0, "bad ILUB block shape");
+            const int nbr = n / d.bnl, bsz = d.bnl * d.bnw;
+            l32 = demote(d.lval, d.lrptr[nbr] * bsz);
+            u32 = demote(d.uval, d.urptr[nbr] * bsz);
+            di.lval = l32.data();
+            di.uval = u32.data();
+        } else if (d.precond != SENK_PC_NONE) {
             l32 = demote(d.lval, d.lrptr[n]);
             u32 = demote(d.uval, d.urptr[n]);
             di.lval = l32.data();
@@ -184,6 +191,7 @@ static void enqueue_orth(System<T> &S, int j, int m, int orth, const int *gate)
     GmresEpi g{S.H.p, S.cs.p, S.sn.p, S.e.p, j, m};
     GmresEpi none{};
     const int nv = j + 1;
+    const int kRedCtas = S.red.ctas;  // CTAs of the multi-dot / update kernels
     const dim3 gdot(kRedCtas, (nv + 7) / 8);
     cudaStream_t s = S.stream;
     if (orth == SENK_ORTH_MGS) {
@@ -351,7 +359,7 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
             else pc->sweep(pc->U, (const T *)t.p, t.p, stream, nullptr);
             break;
         case SENK_OP_DOT:
-            k_multidot<T, false><<<dim3(kRedCtas, 1), kThreads, 0, stream>>>(v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
+            k_multidot<T, false><<<dim3(red.ctas, 1), kThreads, 0, stream>>>(v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
             break;
         default: throw ArgError("unknown op");
         }
@@ -391,6 +399,26 @@ int System<T>::gmres_ir(double nrm_b, int max_outer, int m, double eps, double i
     SENK_REQUIRE(inner, "GMRES-IR needs a system created with mixed = 1");
     SENK_REQUIRE(max_outer >= 0 && inner_cycles >= 1 && inner_tol > 0, "bad GMRES-IR parameters");
     inner->ensure_gmres(m);
+    return refine(nrm_b, max_outer, eps, res, [&](senk_result *ri) {
+        inner->gmres(1.0, inner_cycles, m, inner_tol, ri);
+    });
+}
+
+template <typename T>
+int System<T>::gcr_ir(double nrm_b, int max_outer, int m, double eps, double inner_tol, int inner_cycles,
+                      senk_result *res)
+{
+    SENK_REQUIRE(inner && !ir_only, "GCR-IR needs a system created with mixed = 1");
+    SENK_REQUIRE(max_outer >= 0 && inner_cycles >= 1 && inner_tol > 0, "bad GCR-IR parameters");
+    return refine(nrm_b, max_outer, eps, res, [&](senk_result *ri) {
+        inner->gcr(1.0, inner_cycles, m, inner_tol, ri);
+    });
+}
+
+template <typename T>
+int System<T>::refine(double nrm_b, int max_outer, double eps, senk_result *res,
+                      const std::function<void(senk_result *)> &inner_solve)
+{
     const int grid = stream_grid(n, kThreads, 8);
     SENK_CUDA(cudaEventRecord(ev0, stream));
     long long iters = 0, launches = 0;
@@ -412,7 +440,7 @@ int System<T>::gmres_ir(double nrm_b, int max_outer, int m, double eps, double i
         k_ir_demote<<<grid, kThreads, 0, stream>>>(t.p, irs.p + 1, inner->b.p, n);
         SENK_CUDA(cudaMemsetAsync(inner->x.p, 0, inner->x.bytes(), stream));
         senk_result ri{};
-        inner->gmres(1.0, inner_cycles, m, inner_tol, &ri);
+        inner_solve(&ri);
         iters += ri.iters;
         launches += ri.launches + 2;
         brk |= ri.breakdown;
@@ -443,9 +471,9 @@ int System<T>::gmres_ir(double nrm_b, int max_outer, int m, double eps, double i
 }
 
 template <>
-int System<float>::gmres_ir(double, int, int, double, double, int, senk_result *)
+int System<float>::refine(double, int, double, senk_result *, const std::function<void(senk_result *)> &)
 {
-    throw ArgError("GMRES-IR runs on an FP64 system");
+    throw ArgError("iterative refinement runs on an FP64 system");
 }
 
 template struct System<double>;
@@ -616,6 +644,37 @@ int senk_system_gmres_ir(senk_system *sys, double nrm_b, int max_outer, int m, d
         SENK_REQUIRE(sys && sys->d, "GMRES-IR needs an FP64 system");
         senk_result r{};
         sys->d->gmres_ir(nrm_b, max_outer, m, epsilon, inner_tol, inner_cycles, &r);
+        if (res) *res = r;
+        return r.breakdown ? (int)kErrBreakdown : (int)kOk;
+    });
+}
+
+int senk_system_apply_pc(senk_system *sys, const void *x, void *y)
+{
+    return guarded("senk_system_apply_pc", [&] {
+        SENK_REQUIRE(sys && x && y, "null argument");
+        if (sys->d) {
+            SENK_REQUIRE(sys->d->has_pc(), "the system has no preconditioner");
+            sys->d->precondition_base((const double *)x, (double *)y, nullptr);
+            SENK_CUDA(cudaStreamSynchronize(sys->d->stream));
+            sys->d->check_pc();
+        } else {
+            SENK_REQUIRE(sys->f->has_pc(), "the system has no preconditioner");
+            sys->f->precondition_base((const float *)x, (float *)y, nullptr);
+            SENK_CUDA(cudaStreamSynchronize(sys->f->stream));
+            sys->f->check_pc();
+        }
+        return (int)kOk;
+    });
+}
+
+int senk_system_gcr_ir(senk_system *sys, double nrm_b, int max_outer, int m, double epsilon, double inner_tol,
+                       int inner_cycles, senk_result *res)
+{
+    return guarded("senk_system_gcr_ir", [&] {
+        SENK_REQUIRE(sys && sys->d, "GCR-IR needs an FP64 system");
+        senk_result r{};
+        sys->d->gcr_ir(nrm_b, max_outer, m, epsilon, inner_tol, inner_cycles, &r);
         if (res) *res = r;
         return r.breakdown ? (int)kErrBreakdown : (int)kOk;
     });

@@ -18,7 +18,6 @@ namespace senkgpu {
 
 namespace {
 
-constexpr int kRedCtas = 4 * kNumSMs;
 constexpr int kBicgChunk = 8;        // BiCGStab iterations launched between host checks
 constexpr int kHistCap = 1 << 20;    // most residual-history entries kept on the device
 
@@ -178,7 +177,7 @@ void copy_vec(const T *x, T *y, long long n, cudaStream_t s, const int *gate)
 template <typename T>
 void multidot(System<T> &S, const T *V, long long ldv, int nv, const T *w, double *hcol, const int *gate)
 {
-    k_multidot<T, false><<<dim3(kRedCtas, (nv + 7) / 8), kThreads, 0, S.stream>>>(
+    k_multidot<T, false><<<dim3(S.red.ctas, (nv + 7) / 8), kThreads, 0, S.stream>>>(
         V, ldv, nv, w, S.n, S.red.part.p, S.red.ticket.p, S.coef.p, hcol, gate);
 }
 
@@ -338,7 +337,7 @@ int System<T>::bicgstab(double nrm_b, int max_iter, double eps, senk_result *res
             A.apply(Ks, AKs, stream, gate);
             // [AKs.s, AKs.AKs]: s and AKs are adjacent columns
             multidot(*this, (const T *)s, ld, 2, (const T *)AKs, &st.p->s[kDsa], gate);
-            k_bicg_xr<T><<<kRedCtas, kThreads, 0, stream>>>(st.p, x.p, Kp, Ks, AKs, s, r, n, red.part.p,
+            k_bicg_xr<T><<<red.ctas, kThreads, 0, stream>>>(st.p, x.p, Kp, Ks, AKs, s, r, n, red.part.p,
                                                             red.ticket.p, hist.p, hist_cap, gate);
             multidot(*this, (const T *)r, ld, 1, (const T *)rs, &st.p->s[kRrsNew], gate);
             k_bicg_p<T><<<grid, kThreads, 0, stream>>>(st.p, p, AKp, r, n, gate);

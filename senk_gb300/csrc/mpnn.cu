@@ -449,7 +449,7 @@ struct Mpnn {
         SENK_CUDA(cudaMemset(status.p, 0, sizeof(int)));
         gnorm.alloc(1);
         rms.alloc(2);
-        red.alloc(kNumSMs * 8);  // two partials per CTA for k_step_alpha
+        red.alloc(sm_count() * 8);  // two partials per CTA for k_step_alpha
         acc.alloc(2);
         ticket.alloc(1);
         SENK_CUDA(cudaMemset(ticket.p, 0, sizeof(unsigned)));
@@ -561,7 +561,7 @@ struct Mpnn {
     template <typename T>
     void forward(const T *r, cudaStream_t s, bool keep_z)
     {
-        const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
+        const int rg = std::min(ceil_div(n, kThreads), sm_count() * 4);
         k_rms<T><<<rg, kThreads, 0, s>>>(r, n, red.p, ticket.p, rms.p);
         k_encode<T><<<ceil_div(n * kHid, kThreads), kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, H[0].p, X[0].p, n);
         const int tiles = ceil_div(n, 128);
@@ -606,7 +606,7 @@ struct Mpnn {
         SENK_LAUNCH_CHECK();
         A.apply(out, ailu.p, s, nullptr);
         A.apply(cstep.p, acstep.p, s, nullptr);
-        const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
+        const int rg = std::min(ceil_div(n, kThreads), sm_count() * 4);
         k_step_alpha<<<rg, kThreads, 0, s>>>(r, ailu.p, acstep.p, n, red.p, ticket.p, alpha.p);
         k_add_step<<<rg, kThreads, 0, s>>>(out, cstep.p, alpha.p, n);
         SENK_LAUNCH_CHECK();
@@ -623,7 +623,7 @@ struct Mpnn {
         SENK_CUDA(cudaMemsetAsync(G.p, 0, G.bytes(), s));
         SENK_CUDA(cudaMemsetAsync(acc.p, 0, acc.bytes(), s));
         forward<T>(r, s, true);
-        const int rg = std::min(ceil_div(n, kThreads), kNumSMs * 4);
+        const int rg = std::min(ceil_div(n, kThreads), sm_count() * 4);
         k_decode_c<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(H[kLayers].p, P.p, cbuf.p, n);
         if (loss_mode == 0) {
             k_target<T><<<rg, kThreads, 0, s>>>(e, ilu, rms.p, d, t.p, n, red.p, ticket.p, acc.p);
@@ -633,13 +633,13 @@ struct Mpnn {
             k_spmv_loss<<<rg, kThreads, 0, s>>>(ar.p, ac.p, av.p, cbuf.p, ebuf.p, n, 1.f / d, t.p, acc.p);
             k_spmv_grad<<<rg, kThreads, 0, s>>>(atr.p, atc.p, atv.p, ebuf.p, dcb.p, n, 1.f / d, acc.p);
         }
-        k_decode_back<<<kNumSMs * 4, kThreads, 0, s>>>(H[kLayers].p, P.p, dcb.p, dH.p, G.p, n);
+        k_decode_back<<<sm_count() * 4, kThreads, 0, s>>>(H[kLayers].p, P.p, dcb.p, dH.p, G.p, n);
         float *dh = dH.p, *dh2 = dH2.p;
         const int tiles = ceil_div(n, 128);
         for (int l = kLayers - 1; l >= 0; l--) {
             float *gl = G.p + kOffLayer + l * kLayerSize;
-            k_relu_back<<<kNumSMs * 8, kThreads, 0, s>>>(dh, Z[l].p, dZ.p, gl + 2 * kHid * kHid, n);
-            k_tc_gemm_tn<64><<<kNumSMs * 2, 128, kSmemTn, s>>>(X[l].p, 128, dZ.p, (int)n, gl, status.p);
+            k_relu_back<<<sm_count() * 8, kThreads, 0, s>>>(dh, Z[l].p, dZ.p, gl + 2 * kHid * kHid, n);
+            k_tc_gemm_tn<64><<<sm_count() * 2, 128, kSmemTn, s>>>(X[l].p, 128, dZ.p, (int)n, gl, status.p);
             TcArgs a;
             a.hin = dh;
             a.hout = dh2;
@@ -649,7 +649,7 @@ struct Mpnn {
             k_aggregate_back<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(tr.p, tcol.p, tv.p, dM.p, dh2, n);
             std::swap(dh, dh2);
         }
-        k_encode_back<T><<<kNumSMs * 8, kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, dh, G.p, n);
+        k_encode_back<T><<<sm_count() * 8, kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, dh, G.p, n);
         SENK_LAUNCH_CHECK();
     }
 
@@ -910,7 +910,7 @@ int senk_dev_gemm_tn_bf16(const void *X, const void *dZ, float *out, int n, void
         }
         cudaStream_t s = (cudaStream_t)stream;
         SENK_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * 128 * 64, s));
-        k_tc_gemm_tn<64><<<std::min(ceil_div(n, 64), kNumSMs * 2), 128, kSmemTn, s>>>((const bf16 *)X, 128,
+        k_tc_gemm_tn<64><<<std::min(ceil_div(n, 64), sm_count() * 2), 128, kSmemTn, s>>>((const bf16 *)X, 128,
                                                                                 (const bf16 *)dZ, n, out, st.p);
         SENK_LAUNCH_CHECK();
         int h = 0;

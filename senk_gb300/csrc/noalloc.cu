@@ -16,7 +16,7 @@ namespace senkgpu {
 namespace {
 
 constexpr int kNoAllocMaxCols = 16;           // most columns per call
-constexpr int kNoAllocCtas = 2 * kNumSMs;     // CTAs per column block (grid x)
+constexpr int kNoAllocCtas = 2 * kNumSMs;     // most CTAs per column block (grid x): 2 per SM of a GB300
 constexpr size_t kNoAllocTicketBytes = 256;   // ticket, padded to keep the partials aligned
 constexpr size_t kNoAllocScratchBytes =
     kNoAllocTicketBytes + sizeof(double) * (size_t)kNoAllocMaxCols * kNoAllocCtas;  // 39,168 bytes
@@ -30,7 +30,9 @@ std::mutex g_noalloc_mu;
 void *g_noalloc_addr[64] = {};  // device address of g_noalloc_scratch, per device
 
 // The array's name is only a host-side stand-in in host code; its device
-// address is looked up once per device, with that device current.
+// address is looked up once per device, with that device current, and kept for
+// the life of the process (a cudaDeviceReset between calls is not supported: the
+// kept address would belong to the destroyed context).
 unsigned char *noalloc_scratch()
 {
     int dev = 0;
@@ -71,6 +73,7 @@ extern "C" int senk_dev_multidot_d_noalloc(const double *V, long long ldv, int n
         // The ticket must start at zero; a call that failed part-way could have
         // left it set.
         SENK_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
+        // 2 CTAs per SM of this device, capped by the partials the array holds
         const int grid = std::min(stream_grid(N, kThreads, 2), kNoAllocCtas);
         k_multidot<double, false><<<dim3(grid, (nv + 7) / 8), kThreads, 0, s>>>(V, ldv, nv, w, N, part, ticket, out,
                                                                                nullptr, nullptr);

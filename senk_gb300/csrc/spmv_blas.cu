@@ -209,13 +209,13 @@ void SpmvOp<T>::residual(const T *x, const T *b, T *y, ReduceScratch &red, doubl
     red.ensure(s);
     if (use_sell) {
         const int grid = ceil_div(n, kThreads);
-        SENK_REQUIRE(grid <= ReduceScratch::kMaxCtas * ReduceScratch::kMaxCols, "N too large for the reduction scratch");
+        SENK_REQUIRE(grid <= red.ctas * ReduceScratch::kMaxCols, "N too large for the reduction scratch");
         k_residual_sell32<T><<<grid, kThreads, 0, s>>>(sval.p, scol.p, soff.p, x, b, y, n, red.part.p, red.ticket.p,
                                                        norm_out, inv_out);
         SENK_LAUNCH_CHECK();
         return;
     }
-    const int grid = std::min(stream_grid(n, kThreads / lanes, 8), ReduceScratch::kMaxCtas * ReduceScratch::kMaxCols);
+    const int grid = std::min(stream_grid(n, kThreads / lanes, 8), red.ctas * ReduceScratch::kMaxCols);
 #define SENK_RES_CASE(G) \
     case G: k_spmv_csr<T, T, G, 1, true><<<grid, kThreads, 0, s>>>(val.p, cind.p, rptr.p, x, b, y, n, red.part.p, red.ticket.p, norm_out, inv_out, nullptr); break;
     switch (lanes) {

@@ -1,17 +1,20 @@
 #pragma once
-// ILU sweep plans: the split factors re-laid out for colour-by-colour triangular
-// sweeps on the GPU (replaces include/senk_sparse.hpp:132-315, SptrsvCsr_l/_u in
-// their sequential, AMC and ABMC forms).
+// ILU sweep plans: the split factors re-laid out for triangular sweeps on the
+// GPU (replaces include/senk_sparse.hpp:132-315, SptrsvCsr_l/_u in their
+// sequential, AMC and ABMC forms).
 //
-// Layout ("chain-major"): the schedule is a list of colours (or level sets for
-// the natural order) in processing order. A chain is `bs` consecutive schedule
-// positions (one ABMC block) solved in order; 32 chains of a colour form a
-// group, solved by one CTA of bs warps. Per row, entries referencing other
-// chains are stored first (they are final before the colour starts, so the
-// thread gathers all of them at once) and entries inside the chain after all of
-// them, as chain-local row numbers; each part keeps the reference's subtraction
-// order (ascending columns for L, descending for U). Slot k of a row is a
-// 32-wide column across the group's chains, so a warp's loads coalesce.
+// Two layouts. Both take chains (`bs` consecutive schedule positions, one ABMC
+// block, solved in order) 32 at a time from one colour, and keep each row's
+// subtraction order (entries of other chains first, which are final before the
+// colour starts, then in-chain entries; each part in the reference's column
+// order: ascending for L, descending for U).
+//  * Compact chains (default for AMC/ABMC schedules, `k_sweep_wf`, one launch
+//    per sweep, one warp per group of 32 chains): each chain's entries are
+//    packed one after another, lane = chain, so a group pads only to its widest
+//    chain; the chains of a colour are sorted by their entry counts first.
+//  * Row slots (`k_sweep`, one launch per colour; level-set schedules of the
+//    natural order, and SENK_SWEEP_COLOURS): slot k of row l of every chain of
+//    a group is one 32-wide column, rows padded to the group's widest.
 #include <algorithm>
 #include <climits>
 #include <memory>
@@ -26,15 +29,10 @@ struct Group {
     int p0, p1;  // schedule positions [p0, p1)
 };
 
-// The groups each group reads from (dataflow sweeps), and the launch size.
-template <typename VT>
-void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> &gd, int bs, const int *cind,
-                        const int *rptr, bool upper, cudaStream_t s);
-
 template <typename VT>
 void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
                   const std::vector<Group> &groups, const std::vector<int> *rowmap, int bs,
-                  const std::vector<int> *group_of_row, cudaStream_t s, int sweep_mode = SENK_SWEEP_AUTO)
+                  const std::vector<int> *group_of_row, cudaStream_t s)
 {
     F.upper = upper;
     F.mapped = rowmap != nullptr;
@@ -179,64 +177,60 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.groups.upload(gd.data(), ng, s);
     F.widths.alloc(wd.size());
     F.widths.upload(wd.data(), wd.size(), s);
-    // Measured on the 128^3 convection-diffusion system (one ILU application):
-    // per-colour launches FP32 194 us, FP64 301 us; dataflow FP32 323 us,
-    // FP64 300 us. SENK_SWEEP_AUTO takes the per-colour launches.
-    F.dataflow = chains && sweep_mode == SENK_SWEEP_DATAFLOW;
-    if (F.dataflow) build_dependencies(F, N, gd, bs, cind, rptr, upper, s);
+    F.dataflow = false;
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
 }
 
+// Largest dynamic shared memory of one dataflow CTA.
+constexpr size_t kMaxWfSmem = 200 * 1024;
+
+// Compact chain layout (wf_layout.hpp) uploaded for k_sweep_wf. Returns false
+// (and builds nothing) when a group's block would not fit one warp's shared
+// memory; the caller then takes the row-slot layout.
 template <typename VT>
-void build_dependencies(SweepFactor<VT> &F, int N, const std::vector<GroupDesc> &gd, int bs, const int *cind,
-                        const int *rptr, bool upper, cudaStream_t s)
+bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
+                     const std::vector<Group> &colours, int bs, const std::vector<int> &colour_of, cudaStream_t s)
 {
-    const int ng = (int)gd.size();
-    std::vector<int> owner(N, -1);
-    for (int i = 0; i < ng; i++)
-        for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) owner[p] = i;
-    std::vector<std::vector<int>> deps(ng);
-    int bad = -1;
-#pragma omp parallel
-    {
-        std::vector<int> seen(ng, -1);  // per thread: the group that last listed each group
-#pragma omp for schedule(dynamic, 16)
-        for (int i = 0; i < ng; i++) {
-            std::vector<int> &dv = deps[i];
-            for (int p = gd[i].pos0; p < gd[i].pos0 + gd[i].nchains * bs; p++) {
-                const int cs = p - p % bs, ce = cs + bs;
-                for (int j = rptr[p] + (upper ? 1 : 0); j < rptr[p + 1]; j++) {
-                    const int c = cind[j];
-                    if (c >= cs && c < ce) continue;  // in-chain
-                    const int o = owner[c];
-                    if (o < 0 || o >= i) {
-#pragma omp atomic write
-                        bad = i;
-                        continue;
-                    }
-                    if (seen[o] != i) {
-                        seen[o] = i;
-                        dv.push_back(o);
-                    }
-                }
-            }
-        }
+    std::vector<WfColour> cr;
+    for (const Group &g : colours) cr.push_back({g.p0, g.p1});
+    WfLayout<VT> lay;
+    if (!make_wf_layout(lay, upper, N, val, cind, rptr, cr, bs, colour_of.data(), kMaxWfSmem)) return false;
+    const int ng = (int)lay.groups.size();
+    F.upper = upper;
+    F.mapped = false;
+    F.bs = bs;
+    F.dataflow = true;
+    F.ngroups = ng;
+    F.slots_max = lay.slots_max;
+    F.elems = (long long)lay.col.size();
+    F.nnz = lay.stored + (upper ? N : 0);
+    F.colour_groups.assign(1, 0);
+    F.colour_groups.push_back(ng);
+    F.colour_smem.assign(1, 0);
+    F.val.alloc(std::max<size_t>(lay.val.size(), 1));
+    F.val.upload(lay.val.data(), lay.val.size(), s);
+    F.col.alloc(std::max<size_t>(lay.col.size(), 1));
+    F.col.upload(lay.col.data(), lay.col.size(), s);
+    if (upper) {
+        F.dinv.alloc(N);
+        F.dinv.upload(lay.dinv.data(), N, s);
     }
-    SENK_REQUIRE(bad < 0, "group " + std::to_string(bad) + " reads a group that is not solved before it");
-    std::vector<int> ptr(ng + 1, 0), idx;
-    for (int i = 0; i < ng; i++) ptr[i + 1] = ptr[i] + (int)deps[i].size();
-    idx.reserve(ptr[ng]);
-    for (int i = 0; i < ng; i++) idx.insert(idx.end(), deps[i].begin(), deps[i].end());
-    F.dep_ptr.alloc(ptr.size());
-    F.dep_ptr.upload(ptr.data(), ptr.size(), s);
-    F.dep_idx.alloc(std::max<size_t>(idx.size(), 1));
-    F.dep_idx.upload(idx.data(), idx.size(), s);
+    F.wgroups.alloc(std::max(ng, 1));
+    F.wgroups.upload(lay.groups.data(), ng, s);
+    F.wchains.alloc(std::max<size_t>(lay.chains.size(), 1));
+    F.wchains.upload(lay.chains.data(), lay.chains.size(), s);
+    F.dep_ptr.alloc(lay.dep_ptr.size());
+    F.dep_ptr.upload(lay.dep_ptr.data(), lay.dep_ptr.size(), s);
+    F.dep_idx.alloc(std::max<size_t>(lay.dep_idx.size(), 1));
+    F.dep_idx.upload(lay.dep_idx.data(), lay.dep_idx.size(), s);
     F.flags.alloc(std::max(ng, 1));
     SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
+    const int ctrl0[4] = {0, 1, 0, 0};  // counter, epoch, abort, warps finished
     F.ctrl.alloc(4);
-    SENK_CUDA(cudaMemsetAsync(F.ctrl.p, 0, F.ctrl.bytes(), s));
-    SENK_CUDA(cudaStreamSynchronize(s));
+    F.ctrl.upload(ctrl0, 4, s);
+    SENK_CUDA(cudaStreamSynchronize(s));  // the layout's host arrays are released on return
+    return true;
 }
 
 // Level sets of a triangular factor for the natural order: level(i) = 1 + max
@@ -315,25 +309,58 @@ void allow_smem()
 }
 
 template <typename VT, typename XT, int BS, bool UPPER>
-void launch_dataflow(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
+void launch_wf(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
-    const int ng = F.colour_groups.back();
-    if (ng == 0) return;
-    auto kern = k_sweep_df<VT, XT, BS, UPPER>;
-    size_t smem = 0;  // the widest group's block
-    for (size_t b : F.colour_smem) smem = std::max(smem, b);
-    smem = (smem + 15) / 16 * 16;
-    SENK_REQUIRE(2 * smem <= kMaxStagedBytes,
-                 "a group's factor block exceeds the shared memory of the dataflow sweep");
+    if (F.ngroups == 0) return;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(F.wf_grid);
+    cfg.blockDim = dim3(F.wf_warps * 32);
+    cfg.dynamicSmemBytes = F.wf_smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_wf<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p, F.ngroups,
+                                 (const int2 *)F.wchains.p, (const VT *)F.val.p, (const int *)F.col.p,
+                                 (const VT *)F.dinv.p, (const int *)F.dep_ptr.p, (const int *)F.dep_idx.p,
+                                 F.flags.p, F.ctrl.p, x, y, gate, status, F.slots_max));
+}
+
+// Launch shape of a dataflow sweep: as many warps per CTA (up to 8) as the
+// shared memory allows, and as many CTAs as are resident at once (every warp
+// loops over groups, so the grid need not cover them).
+template <typename VT, int BS, bool UPPER>
+void shape_wf(SweepFactor<VT> &F)
+{
+    auto kern = k_sweep_wf<VT, VT, BS, UPPER>;
+    const size_t per_warp = wf_warp_bytes<VT, VT, BS, UPPER>(F.slots_max);
+    int warps = (int)std::min<size_t>(8, kMaxWfSmem / per_warp);
+    SENK_REQUIRE(warps >= 1, "a group's block exceeds the shared memory of the dataflow sweep");
+    warps = std::min(warps, std::max(1, F.ngroups));
+    F.wf_warps = warps;
+    F.wf_smem = per_warp * warps;
+    SENK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F.wf_smem));
     int per_sm = 0;
-    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 2 * smem));
-    const int grid = std::max(1, std::min(ng, std::max(per_sm, 1) * kNumSMs));
-    k_df_begin<<<1, 1, 0, s>>>(F.ctrl.p);
-    kern<<<grid, BS * 32, 2 * smem, s>>>((const GroupDesc *)F.groups.p, ng, (const unsigned char *)F.widths.p,
-                                      (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p,
-                                      F.dep_ptr.p, F.dep_idx.p, F.flags.p, F.ctrl.p, x, y, gate, status,
-                                      (unsigned)smem);
-    SENK_LAUNCH_CHECK();
+    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, F.wf_smem));
+    SENK_REQUIRE(per_sm >= 1, "the dataflow sweep does not fit an SM");
+    const int need = (F.ngroups + warps - 1) / warps;
+    F.wf_grid = std::max(1, std::min(need, per_sm * sm_count()));
+}
+
+template <typename VT, bool UPPER>
+void shape_wf_bs(SweepFactor<VT> &F)
+{
+    switch (F.bs) {
+    case 1: shape_wf<VT, 1, UPPER>(F); break;
+    case 2: shape_wf<VT, 2, UPPER>(F); break;
+    case 4: shape_wf<VT, 4, UPPER>(F); break;
+    case 8: shape_wf<VT, 8, UPPER>(F); break;
+    case 16: shape_wf<VT, 16, UPPER>(F); break;
+    case 32: shape_wf<VT, 32, UPPER>(F); break;
+    default: throw ArgError("unsupported chain length");
+    }
 }
 
 template <typename VT, typename XT, bool UPPER>
@@ -342,13 +369,15 @@ void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cud
     const int nc = (int)F.colour_groups.size() - 1;
     if (F.dataflow) {
         switch (F.bs) {
-        case 2: launch_dataflow<VT, XT, 2, UPPER>(F, status, x, y, s, gate); break;
-        case 4: launch_dataflow<VT, XT, 4, UPPER>(F, status, x, y, s, gate); break;
-        case 8: launch_dataflow<VT, XT, 8, UPPER>(F, status, x, y, s, gate); break;
-        case 16: launch_dataflow<VT, XT, 16, UPPER>(F, status, x, y, s, gate); break;
-        case 32: launch_dataflow<VT, XT, 32, UPPER>(F, status, x, y, s, gate); break;
+        case 1: launch_wf<VT, XT, 1, UPPER>(F, status, x, y, s, gate); break;
+        case 2: launch_wf<VT, XT, 2, UPPER>(F, status, x, y, s, gate); break;
+        case 4: launch_wf<VT, XT, 4, UPPER>(F, status, x, y, s, gate); break;
+        case 8: launch_wf<VT, XT, 8, UPPER>(F, status, x, y, s, gate); break;
+        case 16: launch_wf<VT, XT, 16, UPPER>(F, status, x, y, s, gate); break;
+        case 32: launch_wf<VT, XT, 32, UPPER>(F, status, x, y, s, gate); break;
         default: throw ArgError("unsupported chain length");
         }
+        SENK_LAUNCH_CHECK();
         return;
     }
     for (int c = 0; c < nc; c++) {
@@ -368,20 +397,9 @@ void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cud
     }
 }
 
-template <typename VT, typename XT, int BS>
-void allow_df_smem()
-{
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kMaxStagedBytes));
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_df<VT, XT, BS, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kMaxStagedBytes));
-}
-
 template <typename VT, typename XT>
 void allow_all_smem()
 {
-    allow_df_smem<VT, XT, 2>(); allow_df_smem<VT, XT, 4>(); allow_df_smem<VT, XT, 8>();
-    allow_df_smem<VT, XT, 16>(); allow_df_smem<VT, XT, 32>();
     allow_smem<VT, XT, 1, false, true>(); allow_smem<VT, XT, 1, true, true>();
     allow_smem<VT, XT, 1, false, false>(); allow_smem<VT, XT, 1, true, false>();
     allow_smem<VT, XT, 2, false, false>(); allow_smem<VT, XT, 2, true, false>();
@@ -431,10 +449,20 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s, sweep_mode);
+    // Measured on the 128^3 convection-diffusion system: the dataflow sweeps on
+    // compact chains are the default; SENK_SWEEP_COLOURS keeps one launch per
+    // colour on row slots.
+    const bool wf = sweep_mode != SENK_SWEEP_COLOURS;
+    if (!(wf && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, s)))
+        build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
+    else
+        shape_wf_bs<VT, false>(L);
     // For U, "earlier" means a later colour: flip the colour numbers.
     for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
-    build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s, sweep_mode);
+    if (!(wf && build_factor_wf(U, true, N, uval, ucind, urptr, bwd, bs, colour_of, s)))
+        build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
+    else
+        shape_wf_bs<VT, true>(U);
 }
 
 template <typename VT>
@@ -460,7 +488,14 @@ void IluPlan<VT>::check_status(cudaStream_t s) const
     int h = 0;
     SENK_CUDA(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SENK_CUDA(cudaStreamSynchronize(s));
-    if (h) throw CudaError{cudaErrorLaunchTimeout, "ILU sweep: a TMA wait did not complete", __FILE__, __LINE__};
+    if (!h) return;
+    // reported once: the next sweep starts clean
+    SENK_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+    SENK_CUDA(cudaStreamSynchronize(s));
+    throw CudaError{cudaErrorLaunchTimeout,
+                    h == 2 ? "ILU sweep: a TMA copy of a factor block did not complete"
+                           : "ILU sweep: a wait for an earlier group's rows ran out",
+                    __FILE__, __LINE__};
 }
 
 }  // namespace senkgpu

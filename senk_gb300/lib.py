@@ -98,6 +98,8 @@ def _declare(L):
     d("senk_system_gmres", [_P, _D, _I, _I, _D, Rp])
     d("senk_system_time_op", [_P, _I, _I, C.POINTER(_D), C.POINTER(C.c_longlong)])
     d("senk_system_gmres_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
+    d("senk_system_gcr_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
+    d("senk_system_apply_pc", [_P, _P, _P])
     d("senk_abmc_ilu_gmres_ir_d", [_P] * 10 + [_I, _I, _P, _P, _D, _I, _I, _I, _D, _D, _I, Op, Rp])
     gd = [_D, _I, _I, _I, _D]
     d("senk_bcsr_gmres_d", [_P] * 5 + gd + [_I, _I, Op, Rp])
@@ -131,6 +133,9 @@ def _declare(L):
     d("senk_ilu_plan_apply", [_P, _P, _P, _P])
     d("senk_ilu_plan_sweep", [_P, _I, _P, _P, _P])
     d("senk_ilu_plan_destroy", [_P])
+    d("senk_ilu_plan_create_sched", [C.POINTER(_P), _I, _I, _P, _P, _P, _P, _P, _P, _I, _P, _I, _I, _I])
+    d("senk_ilu_plan_status", [_P, _P])
+    d("senk_ilu_plan_test_stall", [_P, _I, _I])
     d("senk_mpnn_num_params", [])
     d("senk_mpnn_create", [C.POINTER(_P), _P, _I])
     d("senk_mpnn_destroy", [_P])

@@ -146,9 +146,28 @@ def normal_solution(n: int, seed: int = 1) -> np.ndarray:
     return np.random.default_rng(seed).standard_normal(n)
 
 
+def _sym3_max_eig(M: np.ndarray) -> np.ndarray:
+    """Largest eigenvalue of each symmetric 3x3 matrix in M[..., 3, 3], by the
+    closed-form trigonometric solution of the characteristic cubic (Smith,
+    "Eigenvalues of a symmetric 3 x 3 matrix", CACM 4(4), 1961)."""
+    q = (M[..., 0, 0] + M[..., 1, 1] + M[..., 2, 2]) / 3.0
+    p1 = M[..., 0, 1] ** 2 + M[..., 0, 2] ** 2 + M[..., 1, 2] ** 2
+    p2 = (M[..., 0, 0] - q) ** 2 + (M[..., 1, 1] - q) ** 2 + (M[..., 2, 2] - q) ** 2 + 2.0 * p1
+    p = np.sqrt(p2 / 6.0)
+    safe = np.where(p > 0, p, 1.0)
+    b00, b11, b22 = (M[..., 0, 0] - q) / safe, (M[..., 1, 1] - q) / safe, (M[..., 2, 2] - q) / safe
+    b01, b02, b12 = M[..., 0, 1] / safe, M[..., 0, 2] / safe, M[..., 1, 2] / safe
+    det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02)
+    phi = np.arccos(np.clip(det / 2.0, -1.0, 1.0)) / 3.0
+    return np.where(p > 0, q + 2.0 * p * np.cos(phi), q)
+
+
 def block27(n: int = 96, scale: float = 1.0, dominance: float = 1.1, seed: int = 0) -> Csr:
-    """Block-3x3 27-point system on an n^3 grid (3 unknowns per node, node-major:
-    row 3*node + k), seeded."""
+    """Block-3x3 system on an n^3 grid with a 27-point stencil (3 unknowns per
+    node, node-major: row 3*node + k), seeded. Off-diagonal blocks: entries
+    U(-1, 0) * scale; diagonal blocks S S^T + c I with S ~ U(-1, 1) and c chosen
+    so that their smallest eigenvalue is at least `dominance` times the sum of
+    the spectral norms of the row's off-diagonal blocks (plus 1e-3)."""
     rng = np.random.default_rng([seed, 27])
     nn = n ** 3
     node = np.arange(nn, dtype=np.int64)
@@ -163,12 +182,17 @@ def block27(n: int = 96, scale: float = 1.0, dominance: float = 1.1, seed: int =
                 keep.append(ok)
     nbrs = np.stack(nbrs, axis=1)        # nn x 27, ascending node index (dk, dj, di order)
     keep = np.stack(keep, axis=1)
-    blocks = -rng.uniform(0.0, 1.0, (nn, 27, 3, 3)) * scale
+    blocks = rng.uniform(0.0, 1.0, (nn, 27, 3, 3))
+    np.multiply(blocks, -scale, out=blocks)
     blocks[~keep] = 0.0
     centre = 13                           # (0, 0, 0)
-    offn = np.linalg.norm(blocks, ord=2, axis=(2, 3))
-    offn[:, centre] = 0.0
-    offsum = offn.sum(axis=1)
+    # spectral norms of the off-diagonal blocks: sqrt of the largest eigenvalue of B^T B
+    offsum = np.zeros(nn)
+    for t in range(27):
+        if t == centre:
+            continue
+        B = blocks[:, t]
+        offsum += np.sqrt(np.maximum(_sym3_max_eig(np.einsum("nki,nkj->nij", B, B)), 0.0))
     S = rng.uniform(-1.0, 1.0, (nn, 3, 3))
     D = S @ np.transpose(S, (0, 2, 1))
     lam = np.linalg.eigvalsh(D)[:, 0]
@@ -178,12 +202,32 @@ def block27(n: int = 96, scale: float = 1.0, dominance: float = 1.1, seed: int =
     cnt = keep.sum(axis=1) * 3
     rptr = np.zeros(3 * nn + 1, np.int64)
     rptr[1:] = np.cumsum(np.repeat(cnt, 3))
-    cols = (3 * nbrs[:, :, None] + np.arange(3)[None, None, :])       # nn x 27 x 3
-    cols = np.broadcast_to(cols[:, None, :, :], (nn, 3, 27, 3))       # node, a, nbr, b
-    vals = np.transpose(blocks, (0, 2, 1, 3))                          # node, a, nbr, b
+    vals = np.ascontiguousarray(np.transpose(blocks, (0, 2, 1, 3)))    # node, a, nbr, b
+    del blocks
     mask = np.broadcast_to(keep[:, None, :, None], (nn, 3, 27, 3))
-    return Csr(np.ascontiguousarray(vals[mask], np.float64), np.ascontiguousarray(cols[mask], np.int32),
-               rptr.astype(np.int32))
+    val = vals[mask]
+    del vals
+    cols = (3 * nbrs[:, :, None] + np.arange(3)[None, None, :]).astype(np.int32)   # nn x 27 x 3
+    col = np.broadcast_to(cols[:, None, :, :], (nn, 3, 27, 3))[mask]
+    return Csr(np.ascontiguousarray(val, np.float64), np.ascontiguousarray(col, np.int32), rptr.astype(np.int32))
+
+
+def block27_node_graph(n: int) -> Csr:
+    """Node graph of block27(n) (one entry per nonzero block), from the stencil."""
+    nn = n ** 3
+    node = np.arange(nn, dtype=np.int64)
+    i, j, k = node % n, (node // n) % n, node // (n * n)
+    nbrs, keep = [], []
+    for dk in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            for di in (-1, 0, 1):
+                ii, jj, kk = i + di, j + dj, k + dk
+                nbrs.append(ii + n * jj + n * n * kk)
+                keep.append((ii >= 0) & (ii < n) & (jj >= 0) & (jj < n) & (kk >= 0) & (kk < n))
+    nbrs, keep = np.stack(nbrs, axis=1), np.stack(keep, axis=1)
+    rptr = np.zeros(nn + 1, np.int64)
+    rptr[1:] = np.cumsum(keep.sum(axis=1))
+    return Csr(np.ones(int(rptr[-1])), nbrs[keep].astype(np.int32), rptr.astype(np.int32))
 
 
 def expand_node_permutation(LP_nodes: np.ndarray, bs: int = 3) -> tuple:

@@ -272,6 +272,32 @@ class System:
                                                                  inner_cycles, C.byref(r)))
         return r
 
+    def apply_precond(self, v):
+        """K v with the system's preconditioner, host vector in and out."""
+        v = _arr(v, self.dtype)
+        out = np.empty(self.n, self.dtype)
+        nb = v.nbytes
+        dx, dy = C.c_void_p(), C.c_void_p()
+        check("senk_mem_alloc", lib().senk_mem_alloc(C.byref(dx), nb))
+        try:
+            check("senk_mem_alloc", lib().senk_mem_alloc(C.byref(dy), nb))
+            try:
+                check("senk_mem_h2d", lib().senk_mem_h2d(dx, ptr(v), nb))
+                check("senk_system_apply_pc", lib().senk_system_apply_pc(self._h, dx, dy))
+                check("senk_mem_d2h", lib().senk_mem_d2h(ptr(out), dy, nb))
+            finally:
+                lib().senk_mem_free(dy)
+        finally:
+            lib().senk_mem_free(dx)
+        return out
+
+    def gcr_ir(self, nrm_b, max_outer, m, epsilon, inner_tol=1e-4, inner_cycles=2) -> Result:
+        """FP64-outer refinement around FP32 GCR(m) (systems created with mixed=1)."""
+        r = Result()
+        check("senk_system_gcr_ir", lib().senk_system_gcr_ir(self._h, nrm_b, max_outer, m, epsilon, inner_tol,
+                                                             inner_cycles, C.byref(r)))
+        return r
+
     def gcr(self, nrm_b, outer, m, epsilon) -> Result:
         r = Result()
         check("senk_system_gcr", lib().senk_system_gcr(self._h, nrm_b, outer, m, epsilon, C.byref(r)))

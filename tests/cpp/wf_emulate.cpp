@@ -1,0 +1,136 @@
+// CPU emulation of the dataflow ILU sweep (k_sweep_wf) on the compact chain
+// layout that the plan builds (senk_gb300/csrc/wf_layout.hpp): every access the
+// kernel makes is repeated here with its index checked against the buffer it
+// reads, groups run in processing order, and each gathered row is checked to be
+// finished and owned by a group on the reading group's dependency list. Test
+// code only: it runs no GPU code.
+#include <cstdio>
+#include <cstring>
+#include <set>
+#include <vector>
+
+#include "wf_layout.hpp"
+
+using namespace senkgpu;
+
+namespace {
+
+template <typename VT>
+int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, const int *cptr, int cnum, int bs,
+            const VT *x, VT *y, char *err, int errlen)
+{
+    auto fail = [&](const std::string &m) {
+        std::snprintf(err, errlen, "%s", m.c_str());
+        return 1;
+    };
+    try {
+        std::vector<WfColour> colours;
+        std::vector<int> colour_of(N);
+        for (int k = 0; k < cnum; k++) {
+            const int c = upper ? cnum - 1 - k : k;
+            colours.push_back({cptr[c] * bs, cptr[c + 1] * bs});
+            for (int p = cptr[c] * bs; p < cptr[c + 1] * bs; p++) colour_of[p] = k;
+        }
+        WfLayout<VT> L;
+        if (!make_wf_layout(L, upper != 0, N, val, cind, rptr, colours, bs, colour_of.data(), (size_t)1 << 30))
+            return fail("layout does not fit");
+        const int ng = (int)L.groups.size();
+        const size_t nslots = L.col.size();
+        std::vector<int> owner(N, -1), done(N, 0);
+        for (int g = 0; g < ng; g++)
+            for (int q = 0; q < L.groups[g].nchains; q++)
+                for (int l = 0; l < bs; l++) {
+                    const int r = L.chains[(size_t)g * 32 + q].x + l;
+                    if (r < 0 || r >= N) return fail("chain row out of range");
+                    if (owner[r] >= 0) return fail("row in two chains");
+                    owner[r] = g;
+                }
+        for (int r = 0; r < N; r++)
+            if (owner[r] < 0) return fail("row not in any chain");
+        std::vector<VT> yy(x, x + N);  // in place, as the plan's U sweep runs
+        for (int g = 0; g < ng; g++) {
+            const WfGroup d = L.groups[g];
+            const int slots = d.emax + d.imax;
+            if (slots > L.slots_max) return fail("group block larger than the warp's buffer");
+            if (d.off < 0 || (size_t)d.off + (size_t)slots * 32 > nslots) return fail("group block out of range");
+            if (d.off % 4) return fail("group block not 16-byte aligned");
+            std::set<int> deps(L.dep_idx.begin() + L.dep_ptr[g], L.dep_idx.begin() + L.dep_ptr[g + 1]);
+            for (int dg : deps)
+                if (dg < 0 || dg >= g) return fail("dependency not earlier");
+            // the staged block
+            const int *cw = L.col.data() + d.off;
+            const VT *vw = L.val.data() + d.off;
+            for (int lane = 0; lane < 32; lane++) {
+                const bool live = lane < d.nchains;
+                const int2 ch = L.chains[(size_t)g * 32 + lane];
+                if (!live) continue;
+                const int r0 = ch.x, E = ch.y & 0xffff, I = (int)((unsigned)ch.y >> 16);
+                if (E > d.emax || I > d.imax) return fail("chain count above the group's width");
+                std::vector<VT> tsh(bs), dsh(bs);
+                for (int l = 0; l < bs; l++) {
+                    tsh[l] = yy[r0 + l];
+                    if (upper) dsh[l] = L.dinv[r0 + l];
+                }
+                VT t = 0;
+                int cur = -1;
+                for (int e = 0; e < E; e++) {
+                    const size_t at = (size_t)e * 32 + lane;
+                    if (at >= (size_t)slots * 32) return fail("external slot out of block");
+                    const int w = cw[at];
+                    const int c = w & kColMask, r = (int)((unsigned)w >> kColBits);
+                    if (c < 0 || c >= N) return fail("gather out of range");
+                    if (!done[c]) return fail("gather of an unfinished row");
+                    if (!deps.count(owner[c])) return fail("gathered row's group not a dependency");
+                    if (r < 0 || r >= bs) return fail("row out of chain");
+                    if (r != cur) {
+                        if (cur >= 0) tsh[cur] = t;
+                        cur = r;
+                        t = tsh[r];
+                    }
+                    t -= vw[at] * yy[c];
+                }
+                if (cur >= 0) tsh[cur] = t;
+                int e = 0;
+                for (int s = 0; s < bs; s++) {
+                    const int r = upper ? bs - 1 - s : s;
+                    VT tt = tsh[r];
+                    while (e < I) {
+                        const size_t at = (size_t)(d.emax + e) * 32 + lane;
+                        if (at >= (size_t)slots * 32) return fail("in-chain slot out of block");
+                        const int w = cw[at];
+                        if ((w >> 8) != r) break;
+                        const int c = w & 255;
+                        if (c < 0 || c >= bs) return fail("in-chain column out of chain");
+                        if (upper ? c <= r : c >= r) return fail("in-chain column not solved before its row");
+                        tt -= vw[at] * tsh[c];
+                        e++;
+                    }
+                    if (upper) tt *= dsh[r];
+                    tsh[r] = tt;
+                }
+                if (e != I) return fail("in-chain entries left over");
+                for (int l = 0; l < bs; l++) yy[r0 + l] = tsh[l];
+            }
+            for (int lane = 0; lane < d.nchains; lane++)
+                for (int l = 0; l < bs; l++) done[L.chains[(size_t)g * 32 + lane].x + l] = 1;
+        }
+        std::memcpy(y, yy.data(), sizeof(VT) * N);
+        return 0;
+    } catch (const std::exception &ex) {
+        return fail(ex.what());
+    }
+}
+
+}  // namespace
+
+extern "C" int wf_emulate_d(int N, const double *val, const int *cind, const int *rptr, int upper, const int *cptr,
+                            int cnum, int bs, const double *x, double *y, char *err, int errlen)
+{
+    return emulate<double>(N, val, cind, rptr, upper, cptr, cnum, bs, x, y, err, errlen);
+}
+
+extern "C" int wf_emulate_s(int N, const float *val, const int *cind, const int *rptr, int upper, const int *cptr,
+                            int cnum, int bs, const float *x, float *y, char *err, int errlen)
+{
+    return emulate<float>(N, val, cind, rptr, upper, cptr, cnum, bs, x, y, err, errlen);
+}

@@ -148,15 +148,16 @@ def _factors(A, sched, bsize=16):
 
 
 class Plan:
-    def __init__(self, L_, U_, kind, sc, nc, bs, dtype=np.float64):
+    def __init__(self, L_, U_, kind, sc, nc, bs, dtype=np.float64, sweep=L.SWEEP_AUTO):
         self.h = C.c_void_p()
         T = dtype
         self.keep = [np.ascontiguousarray(a) for a in (L_.val.astype(T), L_.cind, L_.rptr, U_.val.astype(T),
                                                        U_.cind, U_.rptr)]
         cp = None if sc is None else np.ascontiguousarray(sc, np.int32)
         self.keep.append(cp)
-        self.code = L.lib().senk_ilu_plan_create(C.byref(self.h), L.F32 if T == np.float32 else L.F64, L_.n,
-                                                 *[L.ptr(a) for a in self.keep[:6]], kind, L.ptr(cp), nc, bs)
+        self.code = L.lib().senk_ilu_plan_create_sched(C.byref(self.h), L.F32 if T == np.float32 else L.F64, L_.n,
+                                                       *[L.ptr(a) for a in self.keep[:6]], kind, L.ptr(cp), nc, bs,
+                                                       sweep)
 
     def __del__(self):
         if self.h:
@@ -166,14 +167,17 @@ class Plan:
 SWEEPS = [("natural", 16), ("amc", 16), ("abmc", 16), ("abmc", 8), ("abmc", 32), ("abmc", 4), ("abmc", 2)]
 
 
+@pytest.mark.parametrize("sweep", [L.SWEEP_DATAFLOW, L.SWEEP_COLOURS])
 @pytest.mark.parametrize("case", ["poisson128", "convdiff24", "vardiff16"])
 @pytest.mark.parametrize("sched,bsize", SWEEPS)
-def test_ilu_sweeps_f64(torch, port, case, sched, bsize):
+def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
     A = CASES[case]()
     if sched == "abmc" and A.n % bsize:
         pytest.skip("N not a multiple of bsize")
+    if sched == "natural" and sweep == L.SWEEP_COLOURS:
+        pytest.skip("the natural order has one schedule (level sets)")
     Ar, L_, U_, sc, nc, kind, bs = _factors(A, sched, bsize)
-    pl = Plan(L_, U_, kind, sc, nc, bs)
+    pl = Plan(L_, U_, kind, sc, nc, bs, sweep=sweep)
     L.check("plan", pl.code)
     v = np.random.default_rng(5).uniform(-1, 1, A.n)
     xd = dev(torch, v)
@@ -186,17 +190,22 @@ def test_ilu_sweeps_f64(torch, port, case, sched, bsize):
     want = port.sptrsv(U_, want_l, True)
     assert rel(host(tl), want_l) <= 1e-12
     assert rel(host(yd), want) <= 1e-12
-    # in place: x == y
+    # in place: x == y, twice (the dataflow sweeps start a new epoch each time)
+    x2 = xd.clone()
     L.check("apply", L.lib().senk_ilu_plan_apply(pl.h, xd.data_ptr(), xd.data_ptr(), None))
     torch.cuda.synchronize()
     assert rel(host(xd), want) <= 1e-12
+    L.check("apply", L.lib().senk_ilu_plan_apply(pl.h, x2.data_ptr(), x2.data_ptr(), None))
+    L.check("status", L.lib().senk_ilu_plan_status(pl.h, None))
+    assert rel(host(x2), want) <= 1e-12
 
 
-@pytest.mark.parametrize("sched,bsize", [("abmc", 16), ("natural", 16), ("amc", 16)])
-def test_ilu_sweeps_f32(torch, port, sched, bsize):
+@pytest.mark.parametrize("sweep", [L.SWEEP_DATAFLOW, L.SWEEP_COLOURS])
+@pytest.mark.parametrize("sched,bsize", [("abmc", 16), ("natural", 16), ("amc", 16), ("abmc", 4)])
+def test_ilu_sweeps_f32(torch, port, sched, bsize, sweep):
     A = P.convdiff3d(24, 0.5)
     Ar, L_, U_, sc, nc, kind, bs = _factors(A, sched, bsize)
-    pl = Plan(L_, U_, kind, sc, nc, bs, np.float32)
+    pl = Plan(L_, U_, kind, sc, nc, bs, np.float32, sweep=sweep)
     L.check("plan", pl.code)
     v = np.random.default_rng(6).uniform(-1, 1, A.n).astype(np.float32)
     xd = dev(torch, v)
@@ -220,6 +229,54 @@ def test_ilu_sweep_golden(torch, small):
     torch.cuda.synchronize()
     assert rel(host(yd), s["y_ilu_abmc"]) <= 1e-12
     assert rel(host(yd), s["y_ilu_seq"]) <= 1e-12
+
+
+def test_ilu_sweep_at_benchmark_size(torch, port):
+    """The dataflow sweeps on the 64^3 convection-diffusion system (65,536
+    chains, 11 colours) against the oracle, FP64 and FP32, several applications
+    in a row."""
+    A = P.convdiff3d(64, 0.5)
+    Ar, L_, U_, sc, nc, kind, bs = _factors(A, "abmc", 16)
+    v = np.random.default_rng(9).uniform(-1, 1, A.n)
+    want = port.sptrsv(U_, port.sptrsv(L_, v, False), True)
+    for T, tol in ((np.float64, 1e-12), (np.float32, 1e-5)):
+        pl = Plan(L_, U_, kind, sc, nc, bs, T)
+        L.check("plan", pl.code)
+        xd = dev(torch, v.astype(T))
+        yd = torch.zeros(A.n, dtype=xd.dtype, device="cuda")
+        for _ in range(3):
+            L.check("apply", L.lib().senk_ilu_plan_apply(pl.h, xd.data_ptr(), yd.data_ptr(), None))
+        L.check("status", L.lib().senk_ilu_plan_status(pl.h, None))
+        if T == np.float32:
+            want32 = port.ilu_apply(L_.astype(np.float32), U_.astype(np.float32), v.astype(np.float32),
+                                    dtype=np.float32)
+            assert rel(host(yd), want32) <= tol
+        else:
+            assert rel(host(yd), want) <= tol
+
+
+def test_dataflow_wait_that_runs_out_is_reported(torch):
+    """A group made to wait on its own flag (which nothing sets in time) gives up
+    after its bounded wait; the call reports the failure, the device stays usable,
+    and a fresh plan sweeps correctly afterwards."""
+    A = P.convdiff3d(24, 0.5)
+    Ar, L_, U_, sc, nc, kind, bs = _factors(A, "abmc", 16)
+    pl = Plan(L_, U_, kind, sc, nc, bs, sweep=L.SWEEP_DATAFLOW)
+    L.check("plan", pl.code)
+    # a group of a later colour (one that reads other groups)
+    assert any(L.lib().senk_ilu_plan_test_stall(pl.h, 0, g) == L.OK for g in range(12, 0, -1))
+    v = np.random.default_rng(8).uniform(-1, 1, A.n)
+    xd = dev(torch, v)
+    yd = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    L.check("apply", L.lib().senk_ilu_plan_apply(pl.h, xd.data_ptr(), yd.data_ptr(), None))
+    code = L.lib().senk_ilu_plan_status(pl.h, None)
+    assert code == L.ERR_CUDA
+    assert "wait" in L.lib().senk_last_error().decode()
+    torch.cuda.synchronize()
+    pl2 = Plan(L_, U_, kind, sc, nc, bs, sweep=L.SWEEP_DATAFLOW)
+    L.check("plan", pl2.code)
+    L.check("apply", L.lib().senk_ilu_plan_apply(pl2.h, xd.data_ptr(), yd.data_ptr(), None))
+    L.check("status", L.lib().senk_ilu_plan_status(pl2.h, None))
 
 
 def test_plan_rejects_bad_schedules():

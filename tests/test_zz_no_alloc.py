@@ -2,9 +2,9 @@
 
 It serves callers that cannot allocate device memory when they call in: an
 application whose own pool owns all GPU memory from start-up, or a latency-
-critical loop where cudaMalloc could synchronise the device. It must give the
-same numbers as the allocating entry point senk_dev_dot_d, call after call,
-although every call reuses one fixed scratch array. This file is collected last
+critical loop where cudaMalloc could synchronise the device. It must agree with
+numpy's dot products and with the allocating entry point senk_dev_dot_d to
+rounding, call after call, although every call reuses one fixed scratch array. This file is collected last
 so that a run stopping at the first failure has run every other test first.
 """
 import ctypes as C
@@ -53,6 +53,8 @@ def test_noalloc_matches_allocating_dot_on_consecutive_calls():
         torch.cuda.synchronize()
         got = out.cpu().numpy()
         scale = np.abs(V * w).sum(axis=1)
+        # against an independent host reference and against the allocating entry
+        assert np.all(np.abs(got - V @ w) <= 1e-12 * scale)
         assert np.all(np.abs(got - want) <= 1e-12 * scale)
 
 
