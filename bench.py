@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "solve ms to 1e-8 FP64 true rel. residual (ABMC-ILU(0) GMRES(30), mixed-precision GMRES-IR)"
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ilu_apply_traffic_convdiff128.md")
+TRAFFIC_JSON = os.path.join(ROOT, "profiles", "traffic.json")
 
 
 def parse():
@@ -60,6 +60,12 @@ def parse():
     ap.add_argument("--only", default="both", choices=["both", "mixed", "plain"], help="which solves to time")
     ap.add_argument("--inner-tol", type=float, default=1e-4)
     ap.add_argument("--inner-cycles", type=int, default=2)
+    ap.add_argument("--legs", default="bicgstab,c1,c3,c4,learned",
+                    help="extra legs beside the headline: bicgstab (BiCGStab on the headline system), c1 (2D "
+                         "Poisson 128^2), c3 (variable-coefficient 160^3), c4 (block-3x3 96^3), learned")
+    ap.add_argument("--c3-n", type=int, default=160)
+    ap.add_argument("--c4-n", type=int, default=96)
+    ap.add_argument("--leg-steps", type=int, default=2, help="timed solves per extra leg (after one warm-up)")
     return ap.parse_args()
 
 
@@ -188,17 +194,15 @@ def learned_leg(n=16, train_seeds=range(100, 116), test_seeds=(900, 901, 902), e
 
 
 def traffic_for(kernel):
-    """DRAM bytes (read + write) of one launch of `kernel`, from the ncu summary's
-    `traffic <kernel> <bytes>` lines."""
+    """DRAM bytes (read + write) of one launch of `kernel` (an ILU/ILUB application
+    or an SpMV of a named workload) from ncu, as recorded in profiles/traffic.json
+    with the command that measured it."""
     try:
-        with open(PROFILE_TRAFFIC) as f:
-            for ln in f:
-                parts = ln.strip().strip("`").split()
-                if len(parts) == 3 and parts[0] == "traffic" and parts[1] == kernel:
-                    return int(parts[2])
-    except (OSError, ValueError):
-        pass
-    return None
+        with open(TRAFFIC_JSON) as f:
+            v = json.load(f).get(kernel)
+        return int(v["bytes"]) if isinstance(v, dict) else None
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
 
 
 def cpu_solve(port, Ar, Lf, Uf, nc, sc, b, eps, m, threads):
@@ -210,6 +214,206 @@ def cpu_solve(port, Ar, Lf, Uf, nc, sc, b, eps, m, threads):
     ms = (time.perf_counter() - t0) * 1e3
     port.set_threads(1)
     return ms, it, x
+
+
+def _mean(xs):
+    return sum(xs) / len(xs)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _timed(fn, steps, reset):
+    """One untimed warm-up, then `steps` timed solves (device time on the
+    library's stream); the last result is returned with the mean."""
+    out = []
+    for i in range(steps + 1):
+        reset()
+        r = fn()
+        if i:
+            out.append(r)
+    return _mean([r.solve_ms for r in out]), out[-1]
+
+
+def _kernel(sy, op, hbm, reps=10):
+    ms, by = sy.time_op(op, reps)
+    gbs = by / (ms * 1e-3) / 1e9 if ms > 0 else float("nan")
+    return {"ms": round(ms, 4), "bytes": int(by), "gbs": round(gbs, 1), "frac": round(gbs / hbm, 4)}
+
+
+def leg_bicgstab(sysm, Ar, b, nb, steps):
+    """FP64 ABMC-ILU(0) BiCGStab on the headline system
+    (include/senk_bicgstab.hpp:107-196; ABMC sweeps as for GMRES)."""
+    ms, r = _timed(lambda: sysm.bicgstab(nb, 10000, 1e-8), steps, sysm.zero_x)
+    x = sysm.get_x()
+    return {"ms": ms, "iterations": r.iters, "converged": bool(r.converged),
+            "true_residual": float(np.linalg.norm(b - Ar.matvec(x)) / nb), "dtype": "f64"}
+
+
+def leg_c1(steps, with_cpu):
+    """2D 5-point Poisson 128^2 (N = 16,384), b = A*1, ILU(0)-GMRES(30) to 1e-8 in
+    natural order (level-set sweeps) and in ABMC order (bsize 16): warm GPU solves
+    beside the CPU restatement of the reference on all host cores."""
+    import oracle
+    from senk_gb300 import lib as L
+    from senk_gb300 import problems as P
+    from senk_gb300 import setup as S
+    from senk_gb300 import solver as SV
+    A = P.poisson2d(128)
+    b = A.matvec(np.ones(A.n))
+    nb = float(np.linalg.norm(b))
+    out = {"workload": "poisson2d 128^2, b = A*1, ILU(0)-GMRES(30), eps 1e-8, x0=0", "N": A.n, "nnz": A.nnz}
+    Lf, Uf, _ = S.Split(S.Ilu0(A), "L-DU", True)
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    La, Ua, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
+    cases = {"natural": (A, Lf, Uf, L.PC_ILU, None, 0, 1, b), "abmc16": (Ar, La, Ua, L.PC_ILU_ABMC, sc, nc, 16, b[LP])}
+    port = oracle.port(threads=os.cpu_count() or 1) if with_cpu else None
+    for name, (M, Lx, Ux, pc, cp, cn, bs, rhs) in cases.items():
+        sy = SV.System(M, Lx, Ux, pc, cp, cn, bs, m_max=30)
+        try:
+            sy.set_rhs(rhs)
+            ms, r = _timed(lambda: sy.gmres(nb, 10000 // 30, 30, 1e-8), max(steps, 5), sy.zero_x)
+            x = sy.get_x()
+        finally:
+            sy.close()
+        row = {"ms": ms, "iterations": r.iters, "true_residual": float(np.linalg.norm(rhs - M.matvec(x)) / nb),
+               "us_per_iteration": 1e3 * ms / max(r.iters, 1)}
+        if port is not None:
+            opc = oracle.PC_ILU if pc == L.PC_ILU else oracle.PC_ILU_ABMC
+            times, it = [], None
+            for i in range(4):
+                t0 = time.perf_counter()
+                _, it, _, _ = port.solve("gmres", M, rhs, L=Lx, U=Ux, pc=opc, cptr=cp, cnum=cn, bsize=bs,
+                                         outer=10000 // 30, m=30, eps=1e-8, nrm_b=nb)
+                if i:
+                    times.append((time.perf_counter() - t0) * 1e3)
+            row["cpu_ms"] = _mean(times)
+            row["cpu_iterations"] = it
+            row["cpu_cores"] = os.cpu_count() or 1
+        out[name] = row
+    if port is not None:
+        port.set_threads(1)
+    return out
+
+
+def leg_c3(n, steps, hbm, with_cpu):
+    """Variable-coefficient diffusion n^3 (face coefficients exp of a Gaussian
+    random field, sigma 1.5, correlation length 8), x_true ~ N(0,1): plain FP64
+    ABMC-ILU(0)-GMRES(50) against FP64-outer GMRES-IR with FP32 factors, sweeps,
+    inner SpMV and basis, both to 1e-10 FP64 true residual."""
+    import oracle
+    from senk_gb300 import lib as L
+    from senk_gb300 import problems as P
+    from senk_gb300 import setup as S
+    from senk_gb300 import solver as SV
+    t0 = time.perf_counter()
+    A = P.vardiff3d(n, 1.5, 8.0, 0)
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    Lf, Uf, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
+    b = Ar.matvec(P.normal_solution(A.n, 1)[LP])
+    nb = float(np.linalg.norm(b))
+    setup_s = time.perf_counter() - t0
+    sy = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=50, mixed=1)
+    try:
+        sy.set_rhs(b)
+        pms, rp = _timed(lambda: sy.gmres(nb, 10000 // 50, 50, 1e-10), steps, sy.zero_x)
+        xp = sy.get_x()
+        mms, rm = _timed(lambda: sy.gmres_ir(nb, 30, 50, 1e-10, 1e-4, 2), steps, sy.zero_x)
+        xm = sy.get_x()
+        kern = {"ilu_apply_f32": _kernel(sy, L.OP_INNER + L.OP_PRECOND, hbm),
+                "ilu_apply_f64": _kernel(sy, L.OP_PRECOND, hbm),
+                "spmv_f32": _kernel(sy, L.OP_INNER + L.OP_SPMV, hbm),
+                "spmv_f64": _kernel(sy, L.OP_SPMV, hbm)}
+    finally:
+        sy.close()
+    out = {"workload": f"vardiff3d {n}^3, sigma 1.5, corr 8, seed 0, ABMC bsize 16, ILU(0), GMRES(50), eps 1e-10",
+           "N": Ar.n, "nnz": Ar.nnz, "colours": nc, "setup_s": round(setup_s, 1),
+           "plain_fp64": {"ms": pms, "iterations": rp.iters, "converged": bool(rp.converged),
+                          "true_residual": float(np.linalg.norm(b - Ar.matvec(xp)) / nb)},
+           "gmres_ir": {"ms": mms, "iterations": rm.iters, "outer_steps": rm.cycles, "converged": bool(rm.converged),
+                        "true_residual": float(np.linalg.norm(b - Ar.matvec(xm)) / nb),
+                        "rel_err_vs_plain_fp64": _rel(xm, xp)},
+           "kernels": kern,
+           "roofline": dict(kernel="ILU(0) application, FP32 factors", bound="hbm", peak=hbm, unit="GB/s",
+                            achieved=kern["ilu_apply_f32"]["gbs"], frac=kern["ilu_apply_f32"]["frac"],
+                            traffic=traffic_for(f"ilu_apply_f32_vardiff{n}"))}
+    if with_cpu:
+        # one restart cycle (50 iterations) of the CPU restatement on all host cores
+        port = oracle.port(threads=os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        port.solve("gmres", Ar, b, L=Lf, U=Uf, pc=oracle.PC_ILU_ABMC, cptr=sc, cnum=nc, bsize=16, outer=1, m=50,
+                   eps=1e-10, nrm_b=nb)
+        cyc = (time.perf_counter() - t0) * 1e3
+        port.set_threads(1)
+        out["cpu_baseline"] = {"ms_per_50_iterations": cyc, "est_full_solve_ms": cyc * rp.iters / 50,
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": "one GMRES(50) restart cycle of the FP64 solve, scaled to the GPU's "
+                                         "iteration count"}
+    return out
+
+
+def leg_c4(n, steps, hbm, with_cpu):
+    """Block-3x3 27-point system on n^3 nodes (dense 3x3 blocks, off-diagonal
+    entries U(-1,0), SPD diagonal blocks with block dominance 1.1), ABMC on the
+    node graph (4 nodes = 12 rows per block), ILUB(3x3): FP64 GCR(20) against
+    FP64-outer GCR-IR with FP32 ILUB, inner SpMV and vectors, both to 1e-8."""
+    import oracle
+    from senk_gb300 import lib as L
+    from senk_gb300 import problems as P
+    from senk_gb300 import setup as S
+    from senk_gb300 import solver as SV
+    t0 = time.perf_counter()
+    A = P.block27(n, seed=0)
+    G = P.block27_node_graph(n)
+    nc, sc, LPn, _ = S.GetABMCPermutation(G.cind, G.rptr, G.n, 4, False, "connect")
+    LP, RP = P.expand_node_permutation(LPn, 3)
+    Ar = S.Reordering(A, LP, RP)
+    del A
+    Lf, Uf, _ = S.Split(S.Ilu0(S.AllocBlockZero(Ar, 3, 3)), "L-DU", True)
+    bl, bu = S.Csr2Bcsr(Lf, 3, 3), S.Csr2Bcsr(Uf, 3, 3)
+    del Lf, Uf
+    b = Ar.matvec(P.uniform_solution(Ar.n, 2)[LP])
+    nb = float(np.linalg.norm(b))
+    setup_s = time.perf_counter() - t0
+    sy = SV.System(Ar, bl, bu, L.PC_ILUB_ABMC, sc, nc, 12, m_max=0, block=(3, 3), mixed=1)
+    try:
+        sy.set_rhs(b)
+        pms, rp = _timed(lambda: sy.gcr(nb, 500, 20, 1e-8), steps, sy.zero_x)
+        xp = sy.get_x()
+        mms, rm = _timed(lambda: sy.gcr_ir(nb, 30, 20, 1e-8, 1e-4, 5), steps, sy.zero_x)
+        xm = sy.get_x()
+        kern = {"ilub_apply_f32": _kernel(sy, L.OP_INNER + L.OP_PRECOND, hbm),
+                "ilub_apply_f64": _kernel(sy, L.OP_PRECOND, hbm),
+                "spmv_f32": _kernel(sy, L.OP_INNER + L.OP_SPMV, hbm),
+                "spmv_f64": _kernel(sy, L.OP_SPMV, hbm)}
+    finally:
+        sy.close()
+    out = {"workload": f"block27 {n}^3 nodes, 3x3 blocks, ABMC on nodes (4 per block), ILUB(3x3), GCR(20), "
+                       "eps 1e-8", "N": Ar.n, "nnz": Ar.nnz, "colours": nc, "setup_s": round(setup_s, 1),
+           "plain_fp64": {"ms": pms, "iterations": rp.iters, "converged": bool(rp.converged),
+                          "true_residual": float(np.linalg.norm(b - Ar.matvec(xp)) / nb)},
+           "gcr_ir": {"ms": mms, "iterations": rm.iters, "outer_steps": rm.cycles, "converged": bool(rm.converged),
+                      "true_residual": float(np.linalg.norm(b - Ar.matvec(xm)) / nb),
+                      "rel_err_vs_plain_fp64": _rel(xm, xp)},
+           "kernels": kern,
+           "roofline": dict(kernel="ILUB(3x3) application, FP32 factors", bound="hbm", peak=hbm, unit="GB/s",
+                            achieved=kern["ilub_apply_f32"]["gbs"], frac=kern["ilub_apply_f32"]["frac"],
+                            traffic=traffic_for(f"ilub_apply_f32_block27_{n}"))}
+    if with_cpu:
+        port = oracle.port(threads=os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        port.solve("gcr", Ar, b, L=bl, U=bu, pc=oracle.PC_ILUB_ABMC, cptr=sc, cnum=nc, bsize=12, bnl=3, bnw=3,
+                   outer=1, m=20, eps=1e-8, nrm_b=nb)
+        cyc = (time.perf_counter() - t0) * 1e3
+        port.set_threads(1)
+        out["cpu_baseline"] = {"ms_per_20_iterations": cyc, "est_full_solve_ms": cyc * max(rp.iters, 20) / 20,
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": "one GCR(20) restart cycle of the FP64 solve, scaled to the GPU's "
+                                         "iteration count"}
+    return out
 
 
 def run_reference(args, rank):
@@ -276,16 +480,18 @@ def run_gpu(args, rank, world):
                 sysm.zero_x()
                 res_m.append(mixed())
     if do_mixed:
-        x = sysm.get_x()
-        true_m = float(np.linalg.norm(b - Ar.matvec(x)) / nb)
+        x_m = sysm.get_x()
+        true_m = float(np.linalg.norm(b - Ar.matvec(x_m)) / nb)
     for _ in range(args.steps):
         if do_plain:
             sysm.zero_x()
             res_p.append(plain())
     if do_plain:
-        x = sysm.get_x()
-        true_p = float(np.linalg.norm(b - Ar.matvec(x)) / nb)
+        x_p = sysm.get_x()
+        true_p = float(np.linalg.norm(b - Ar.matvec(x_p)) / nb)
     barrier(world)
+    legs = [x for x in args.legs.split(",") if x]
+    bicg = leg_bicgstab(sysm, Ar, b, nb, args.leg_steps) if "bicgstab" in legs and rank == 0 else None
     mean = lambda rs: sum(r.solve_ms for r in rs) / len(rs)
     hbm, peak_kind = peaks()
     reps = 0 if args.no_kernels else 20
@@ -302,22 +508,36 @@ def run_gpu(args, rank, world):
     sysm.close()
     e2e = None
     if not args.no_e2e and do_mixed:
-        e2e_ms, rr = [], None
-        for i in range(max(1, min(args.steps, 3)) + 1):  # the first call is an untimed warm-up
+        e2e_ms, rr, cold = [], None, None
+        for i in range(max(1, min(args.steps, 3)) + 1):  # the first call builds the device system
             xh = np.zeros(Ar.n)
             t0 = time.perf_counter()
             rr = SV.AbmcIluGmresIr(Ar.val, Ar.cind, Ar.rptr, Lf.val, Lf.cind, Lf.rptr, Uf.val, Uf.cind, Uf.rptr, sc,
                                    nc, 16, b, xh, nb, ir_outer, args.m, Ar.n, args.eps, args.inner_tol,
                                    args.inner_cycles, orth=orth, spmv=spmv, sweep=sweep)
+            ms = (time.perf_counter() - t0) * 1e3
             if i > 0:
-                e2e_ms.append((time.perf_counter() - t0) * 1e3)
+                e2e_ms.append(ms)
+            else:
+                cold = {"ms": ms, "h2d_bytes": int(rr.h2d_bytes)}
         e2e = {"value": allmax(world, sum(e2e_ms) / len(e2e_ms)), "unit": "ms",
                "h2d_bytes_per_step": int(rr.h2d_bytes), "d2h_bytes_per_step": int(rr.d2h_bytes),
-               "steps": len(e2e_ms), "iterations": rr.iters,
-               "note": "drop-in C ABI call senk_abmc_ilu_gmres_ir_d with host arrays; wall clock"}
+               "steps": len(e2e_ms), "iterations": rr.iters, "first_call": cold,
+               "note": "drop-in C ABI call senk_abmc_ilu_gmres_ir_d with host arrays, wall clock; A and the "
+                       "factors stay on the device between calls (content-hashed every call), so a step "
+                       "uploads b and x0 and reads x back; first_call includes building the device system"}
     learned = None
-    if not args.no_learned and rank == 0:
+    if not args.no_learned and "learned" in legs and rank == 0:
         learned = learned_leg()
+    with_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
+    extra = {}
+    if rank == 0:
+        if "c1" in legs:
+            extra["c1"] = leg_c1(args.leg_steps, with_cpu)
+        if "c3" in legs:
+            extra["c3"] = leg_c3(args.c3_n, args.leg_steps, peaks()[0], with_cpu)
+        if "c4" in legs:
+            extra["c4"] = leg_c4(args.c4_n, args.leg_steps, peaks()[0], with_cpu)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -348,6 +568,8 @@ def run_gpu(args, rank, world):
         "plain_fp64": None if rp is None else {"ms": allmax(world, mean(res_p)), "iterations": rp.iters,
                                                "cycles": rp.cycles, "implicit_residual": rp.res,
                                                "true_residual": true_p},
+        "mixed_rel_err_vs_plain_fp64": _rel(x_m, x_p) if (rm and rp) else None,
+        "bicgstab": bicg,
         "e2e": e2e,
         "gpu_launches": int(sum(x.launches for x in (res_m if do_mixed else res_p))),
         "roofline": {"kernel": "ILU(0) application (ABMC L and U sweeps, all colours), "
@@ -358,6 +580,7 @@ def run_gpu(args, rank, world):
         "kernels": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in kern.items()},
         "cpu_baseline": cpu,
         "learned": learned,
+        **extra,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)

@@ -71,12 +71,15 @@ typedef struct {
     int sweep;        /* SENK_SWEEP_* */
 } senk_options;
 
-/* How the ILU sweeps of AMC/ABMC factors are scheduled. */
-#define SENK_SWEEP_AUTO 0     /* the faster schedule as measured: dataflow */
-#define SENK_SWEEP_COLOURS 1  /* one launch per colour */
-#define SENK_SWEEP_DATAFLOW 2 /* one launch per sweep: each warp takes a group of 32
-                                 chains, waits on the flags of the groups it reads,
-                                 solves it and publishes its own flag */
+/* How the ILU sweeps of AMC/ABMC factors are scheduled. Chains (ABMC blocks;
+ * single rows for AMC) are taken 32 to a group from one colour. */
+#define SENK_SWEEP_AUTO 0     /* compact chain layout, one launch per colour, one
+                                 warp per group (the faster schedule as measured) */
+#define SENK_SWEEP_COLOURS 1  /* row-slot layout, one launch per colour, one CTA
+                                 per group */
+#define SENK_SWEEP_DATAFLOW 2 /* compact chain layout, one launch per sweep: each
+                                 warp takes a group, waits on the flags of the
+                                 groups it reads, solves it and publishes its own */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0
@@ -88,7 +91,16 @@ typedef struct {
 
 /* ======================================================= drop-in solvers ==
  * Host arrays in, x updated in place; one call uploads, solves on the GPU and
- * copies x back, like one call of the reference template. opt may be NULL. */
+ * copies x back, like one call of the reference template. opt may be NULL.
+ * The device copies of A and the factors (with their sweep layout and the
+ * captured solver graphs) are kept for the next call: a call whose entry,
+ * sizes, build options (spmv, sweep), host array addresses and array contents
+ * (a 64-bit hash of every input array, computed on each call) match a kept
+ * system uploads only b and x. The two most recent systems of each precision
+ * are kept; drop-in calls are serialised by the library. */
+/* Turns that cache on (mode 1, the default) or off (0: every call builds its
+ * system, and the kept ones are freed now). Returns the previous mode. */
+int senk_dropin_cache(int mode);
 
 /* senk::solver::Gmresm<double> (include/senk_gmres.hpp:33-37) */
 int senk_gmres_d(const double *val, const int *cind, const int *rptr,
@@ -401,10 +413,8 @@ int senk_ilub_plan_create(senk_ilu_plan **out, int N, int bnl, int bnw,
                           const double *blval, const int *blcind, const int *blrptr,
                           const double *buval, const int *bucind, const int *burptr,
                           const int *cptr, int cnum, int bsize);
-/* senk_ilu_plan_create with the sweep schedule chosen (SENK_SWEEP_*): AUTO and
- * DATAFLOW sweep AMC/ABMC factors in one launch per triangular sweep, COLOURS
- * in one launch per colour. The natural order always runs level set by level
- * set. */
+/* senk_ilu_plan_create with the sweep schedule of AMC/ABMC factors chosen
+ * (SENK_SWEEP_*). The natural order always runs level set by level set. */
 int senk_ilu_plan_create_sched(senk_ilu_plan **out, int dtype, int N,
                                const void *lval, const int *lcind, const int *lrptr,
                                const void *uval, const int *ucind, const int *urptr,
@@ -473,6 +483,21 @@ int senk_system_learned_fallback(senk_system *sys);
  * out[128][64] = X^T dZ (X n x 128, dZ n x 64, BF16). */
 int senk_dev_gemm_bf16(const void *A, const void *Bt, float *C, int n, int K, int NO, void *stream);
 int senk_dev_gemm_tn_bf16(const void *X, const void *dZ, float *out, int n, void *stream);
+
+/* senk::matrix::Ilu0<T> (include/senk_matrix.hpp:418-448) on the device, in
+ * place: val, cind, rptr are device arrays of a CSR matrix with sorted columns.
+ * With cptr (host, cnum colours; AMC: bsize 1, ABMC: blocks of bsize rows) the
+ * chains of each colour are factorised concurrently, one thread per chain; the
+ * matrix must be in that colour order (a row reading a row of its own colour
+ * outside its chain is rejected with SENK_ERR_ARG). cptr NULL: the natural
+ * order, level set by level set (the pattern is read back to form them). Each
+ * row performs the reference's operations in its order without FMA
+ * contraction, so the factors equal Ilu0's bit for bit. A zero pivot returns
+ * SENK_ERR_ZERO_PIVOT (the reference prints and exits). Synchronous. */
+int senk_dev_ilu0_d(double *val, const int *cind, const int *rptr, int N,
+                    const int *cptr, int cnum, int bsize, void *stream);
+int senk_dev_ilu0_s(float *val, const int *cind, const int *rptr, int N,
+                    const int *cptr, int cnum, int bsize, void *stream);
 
 /* ===================================================== host setup (CPU) ==
  * The reference's setup functions, bit-exact, for callers without C++ headers.

@@ -1,7 +1,9 @@
 """Builds libsenk_gpu.so in-tree for sm_103a (nvcc, no cmake).
 
 Every CUDA translation unit is compiled in parallel with
-``-gencode arch=compute_103a,code=sm_103a``; the host-only unit with g++. The
+``-gencode arch=compute_103a,code=sm_103a``; the host-only unit with g++. Host
+code is built without floating-point contraction (``-ffp-contract=off``), so the
+setup functions round exactly as the reference does on x86 and on Arm hosts. The
 result lands in ``senk_gb300/_lib/libsenk_gpu.so``; objects in ``senk_gb300/_build``.
 Rebuilds only what changed (sources or headers newer than the object).
 """
@@ -31,8 +33,9 @@ def nvcc() -> str:
 
 
 def _headers():
+    # the build script itself too: a change of flags rebuilds everything
     return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp")) + \
-        glob.glob(os.path.join(ROOT, "include", "*.h*"))
+        glob.glob(os.path.join(ROOT, "include", "*.h*")) + [os.path.abspath(__file__)]
 
 
 def _stale(obj: str, src: str, deps) -> bool:
@@ -50,10 +53,13 @@ def _compile(src: str, verbose: bool) -> str:
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
     if src.endswith(".cu"):
         cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-               "-Xcompiler", "-fPIC,-fopenmp", "-Xptxas", "-warn-spills", *inc, "-c", src, "-o", obj]
+               "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off", "-Xptxas", "-warn-spills", *inc, "-c", src, "-o", obj]
     else:
+        # no FMA contraction in host code: the setup (Ilu0, Ilup, ...) must round
+        # as the reference does on every host (g++ contracts by default on Arm)
         cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
-        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-I", cuda_inc, *inc, "-c", src, "-o", obj]
+        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I", cuda_inc, *inc, "-c", src,
+               "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -162,10 +162,22 @@ struct SweepFactor {
     std::vector<size_t> colour_smem; // bytes to stage the largest group of each colour
     long long elems = 0;           // padded slots
     long long nnz = 0;             // stored off-diagonal entries (+N for U's diagonal)
-    // dataflow sweep (compact chain layout, one warp per group): groups, chain
-    // descriptors, the groups each group reads from, per-group flags and the
-    // launch's control words
-    bool dataflow = false;
+    // compact chain layout (one warp per group): groups, chain descriptors and,
+    // for the dataflow launch, the groups each group reads from, per-group flags
+    // and the launch's control words
+    bool compact = false;          // compact chain layout (else row slots)
+    bool dataflow = false;         // compact: one launch per sweep (else one per colour)
+    std::vector<int> colour_slots; // compact: widest block of each colour
+    DevBuf<unsigned char> wcounts; // compact: per chain, external and in-chain counts of each row
+    // compact, per colour: the launches of a sweep in order; a run covers
+    // several consecutive small colours synchronised by group flags
+    struct Launch {
+        int g0, g1;        // groups
+        bool run;          // flag-synchronised run of small colours
+        bool early_x;      // x may be read before the wait on the previous kernel
+        size_t smem;       // dynamic shared memory
+    };
+    std::vector<Launch> launches;
     DevBuf<WfGroup> wgroups;
     DevBuf<int2> wchains;
     DevBuf<int> dep_ptr, dep_idx, flags, ctrl;

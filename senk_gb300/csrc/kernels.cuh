@@ -334,6 +334,85 @@ k_multidot(const XT *__restrict__ V, long long ldv, int nv, const XT *__restrict
     }
 }
 
+// 16-byte vectors of the Krylov kernels: float4 / double2.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+__device__ __forceinline__ float vdot(const float4 &a, const float4 &b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+__device__ __forceinline__ double vdot(const double2 &a, const double2 &b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ void vaxpy(float4 &y, float a, const float4 &x) { y.x -= a * x.x; y.y -= a * x.y; y.z -= a * x.z; y.w -= a * x.w; }
+__device__ __forceinline__ void vaxpy(double2 &y, double a, const double2 &x) { y.x -= a * x.x; y.y -= a * x.y; }
+
+// k_multidot with 16-byte loads: n and ldv are multiples of the vector width
+// and V, w are 16-byte aligned (the launcher checks). Each thread keeps CH
+// column sums over two vectors per step; the combination across threads and
+// CTAs is k_multidot's.
+template <typename XT, bool ACCUM>
+__global__ void __launch_bounds__(kThreads)
+k_multidot_v(const XT *__restrict__ V, long long ldv, int nv, const XT *__restrict__ w, long long n,
+             double *part, unsigned *ticket, double *coef, double *hcol, const int *gate)
+{
+    if (gated(gate)) return;
+    using VT = typename Vec16<XT>::type;
+    constexpr int W = Vec16<XT>::n;
+    constexpr int CH = 8;
+    const int c0 = blockIdx.y * CH;
+    const int nc = min(CH, nv - c0);
+    XT acc[CH];
+#pragma unroll
+    for (int q = 0; q < CH; q++) acc[q] = 0;
+    const long long nvec = n / W, ldvec = ldv / W;
+    const VT *wv = reinterpret_cast<const VT *>(w);
+    const VT *Vv = reinterpret_cast<const VT *>(V) + (long long)c0 * ldvec;
+    const long long S = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + S < nvec; i += 2 * S) {
+        const VT w0 = wv[i], w1 = wv[i + S];
+#pragma unroll
+        for (int q = 0; q < CH; q++) {
+            if (q < nc) {
+                const VT a0 = ld_stream(Vv + q * ldvec + i), a1 = ld_stream(Vv + q * ldvec + i + S);
+                acc[q] += vdot(a0, w0);
+                acc[q] += vdot(a1, w1);
+            }
+        }
+    }
+    for (; i < nvec; i += S) {
+        const VT w0 = wv[i];
+#pragma unroll
+        for (int q = 0; q < CH; q++)
+            if (q < nc) acc[q] += vdot(ld_stream(Vv + q * ldvec + i), w0);
+    }
+    __shared__ double sh[CH][kThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < CH; q++) {
+        double v = warp_sum((double)acc[q]);
+        if (lane == 0) sh[q][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < CH * 32) {
+        const int q = threadIdx.x >> 5;
+        double v = lane < (int)(blockDim.x >> 5) ? sh[q][lane] : 0.0;
+        v = warp_sum(v);
+        if (lane == 0 && q < nc) part[(long long)(c0 + q) * gridDim.x + blockIdx.x] = v;
+    }
+    const unsigned total = gridDim.x * gridDim.y;
+    if (last_cta_arrives(ticket, total)) {
+        const int P = gridDim.x;
+        for (int k = wid; k < nv; k += blockDim.x >> 5) {
+            double s = 0;
+            for (int p = lane; p < P; p += 32) s += part[(long long)k * P + p];
+            s = warp_sum(s);
+            if (lane == 0) {
+                coef[k] = s;
+                if (hcol) hcol[k] = ACCUM ? hcol[k] + s : s;
+            }
+        }
+    }
+}
+
 // Epilogues run by one thread of the last CTA of k_update, after ||w|| is known.
 enum UpdateEpilogue : int {
     kEpiNone = 0,      // store sqrt(sum) into *norm_out, 1/sqrt into st->scale
@@ -439,6 +518,95 @@ k_update(const XT *__restrict__ V, long long ldv, int nv, const double *__restri
             else st->scale = 1.0 / hn;
         }
     }
+}
+
+// k_update with 16-byte loads and stores (same conditions as k_multidot_v).
+template <typename XT, int EPI>
+__global__ void __launch_bounds__(kThreads)
+k_update_v(const XT *__restrict__ V, long long ldv, int nv, const double *__restrict__ coef,
+           XT *__restrict__ w, long long n, double *part, unsigned *ticket, double *norm_out,
+           KrylovState *st, GmresEpi g, const int *gate)
+{
+    if (gated(gate)) return;
+    using VT = typename Vec16<XT>::type;
+    constexpr int W = Vec16<XT>::n;
+    __shared__ XT sc[64];
+    if (threadIdx.x < nv) sc[threadIdx.x] = (XT)coef[threadIdx.x];
+    __syncthreads();
+    XT nacc = 0;
+    const long long nvec = n / W, ldvec = ldv / W;
+    VT *wv = reinterpret_cast<VT *>(w);
+    const VT *Vv = reinterpret_cast<const VT *>(V);
+    const long long S = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + S < nvec; i += 2 * S) {
+        VT v0 = wv[i], v1 = wv[i + S];
+#pragma unroll 4
+        for (int k = 0; k < nv; k++) {
+            const VT a0 = ld_stream(Vv + k * ldvec + i), a1 = ld_stream(Vv + k * ldvec + i + S);
+            vaxpy(v0, sc[k], a0);
+            vaxpy(v1, sc[k], a1);
+        }
+        wv[i] = v0;
+        wv[i + S] = v1;
+        nacc += vdot(v0, v0);
+        nacc += vdot(v1, v1);
+    }
+    for (; i < nvec; i += S) {
+        VT v0 = wv[i];
+        for (int k = 0; k < nv; k++) vaxpy(v0, sc[k], ld_stream(Vv + k * ldvec + i));
+        wv[i] = v0;
+        nacc += vdot(v0, v0);
+    }
+    __shared__ double sh[32];
+    double t = block_sum((double)nacc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    if (last_cta_arrives(ticket, gridDim.x)) {
+        double s = 0;
+        if (threadIdx.x < 32) {
+            for (int i2 = threadIdx.x; i2 < (int)gridDim.x; i2 += 32) s += part[i2];
+            s = warp_sum(s);
+        }
+        if (threadIdx.x == 0) {
+            const double hn = sqrt(s);
+            if (norm_out) *norm_out = hn;
+            if (EPI == kEpiGmres) gmres_givens_step(st, g, hn);
+            else st->scale = 1.0 / hn;
+        }
+    }
+}
+
+// Whether the Krylov kernels may take 16-byte vectors for these operands.
+template <typename XT>
+inline bool vec16_ok(const void *a, const void *b, long long n, long long ld)
+{
+    constexpr int W = 16 / sizeof(XT);
+    return n % W == 0 && ld % W == 0 && ((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0;
+}
+
+// Launchers that take the 16-byte kernels when the operands allow.
+template <typename XT, bool ACCUM>
+inline void launch_multidot(dim3 grid, cudaStream_t s, const XT *V, long long ldv, int nv, const XT *w, long long n,
+                            double *part, unsigned *ticket, double *coef, double *hcol, const int *gate)
+{
+    if (vec16_ok<XT>(V, w, n, ldv)) {
+        // the same number of CTAs in all: column blocks share the row slices
+        grid.x = max(1u, grid.x / grid.y);
+        k_multidot_v<XT, ACCUM><<<grid, kThreads, 0, s>>>(V, ldv, nv, w, n, part, ticket, coef, hcol, gate);
+    } else {
+        k_multidot<XT, ACCUM><<<grid, kThreads, 0, s>>>(V, ldv, nv, w, n, part, ticket, coef, hcol, gate);
+    }
+}
+
+template <typename XT, int EPI>
+inline void launch_update(int grid, cudaStream_t s, const XT *V, long long ldv, int nv, const double *coef, XT *w,
+                          long long n, double *part, unsigned *ticket, double *norm_out, KrylovState *st, GmresEpi g,
+                          const int *gate)
+{
+    if (vec16_ok<XT>(V, w, n, ldv))
+        k_update_v<XT, EPI><<<grid, kThreads, 0, s>>>(V, ldv, nv, coef, w, n, part, ticket, norm_out, st, g, gate);
+    else
+        k_update<XT, EPI><<<grid, kThreads, 0, s>>>(V, ldv, nv, coef, w, n, part, ticket, norm_out, st, g, gate);
 }
 
 // Back-solve of the Hessenberg least squares (include/senk_blas2.hpp:24-34) for
@@ -700,14 +868,66 @@ __host__ __device__ constexpr size_t wf_warp_bytes(int slots_max)
            16 * 16;
 }
 
+// Solves one staged group (compact chain layout) for lane `lane` = chain:
+// tsh[BS][32] holds x of the chain's rows on entry and the solved rows on exit
+// (dsh: U's inverted diagonal). Products of the external entries are gathered
+// G at a time (all loads of a batch in flight together) and subtracted row by
+// row; then the in-chain recurrence, rows in solve order, on chip.
+template <typename VT, typename XT, int BS, bool UPPER>
+__device__ __forceinline__ void wf_solve_group(const WfGroup &d, int E, int I, const int *cw, const VT *vw, XT *tsh,
+                                               const XT *dsh, const XT *y, int lane)
+{
+    constexpr int G = sizeof(XT) == 4 ? 16 : 8;
+    XT t = XT(0);
+    int cur = -1;
+    for (int b = 0; b < d.emax; b += G) {
+        XT gv[G];
+#pragma unroll
+        for (int u = 0; u < G; u++) {
+            const int e = b + u;
+            gv[u] = XT(0);
+            if (e < E) gv[u] = ld_l2(y + (cw[e * 32 + lane] & kColMask));
+        }
+#pragma unroll
+        for (int u = 0; u < G; u++) {
+            const int e = b + u;
+            if (e < E) {
+                const int r = (int)((unsigned)cw[e * 32 + lane] >> kColBits);
+                if (r != cur) {
+                    if (cur >= 0) tsh[cur * 32 + lane] = t;
+                    cur = r;
+                    t = tsh[r * 32 + lane];
+                }
+                t -= (XT)vw[e * 32 + lane] * gv[u];
+            }
+        }
+    }
+    if (cur >= 0) tsh[cur * 32 + lane] = t;
+    const int *iw = cw + d.emax * 32;
+    const VT *iv = vw + d.emax * 32;
+    int e = 0;
+#pragma unroll
+    for (int s = 0; s < BS; s++) {
+        const int r = UPPER ? BS - 1 - s : s;
+        XT tt = tsh[r * 32 + lane];
+        while (e < I) {
+            const int w = iw[e * 32 + lane];
+            if ((w >> 8) != r) break;
+            tt -= (XT)iv[e * 32 + lane] * tsh[(w & 255) * 32 + lane];
+            e++;
+        }
+        if (UPPER) tt *= dsh[r * 32 + lane];
+        tsh[r * 32 + lane] = tt;
+    }
+}
+
 template <typename VT, typename XT, int BS, bool UPPER>
 __global__ void __launch_bounds__(256)
-k_sweep_wf(const WfGroup *__restrict__ groups, int ng, const int2 *__restrict__ chains,
+k_sweep_wf(const WfGroup *__restrict__ groups, int g0, int ng, const int2 *__restrict__ chains,
            const VT *__restrict__ val, const int *__restrict__ col, const VT *__restrict__ dinv,
            const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl, const XT *x,
            XT *y, const int *gate, int *status, int slots_max)
 {
-    constexpr int G = sizeof(XT) == 4 ? 16 : 8;  // external entries gathered per batch
     extern __shared__ __align__(128) unsigned char wfs[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const size_t per_warp = wf_warp_bytes<VT, XT, BS, UPPER>(slots_max);
@@ -725,7 +945,7 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int ng, const int2 *__restrict__ 
     unsigned phase = 0;
     for (;;) {
         int g = 0;
-        if (lane == 0) g = atomicAdd(ctrl, 1);
+        if (lane == 0) g = g0 + atomicAdd(ctrl, 1);
         g = __shfl_sync(0xffffffffu, g, 0);
         if (g >= ng) break;
         const WfGroup d = groups[g];
@@ -779,49 +999,7 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int ng, const int2 *__restrict__ 
             }
         }
         if (ok) {
-            // external entries: products gathered G at a time, subtracted row by row
-            XT t = XT(0);
-            int cur = -1;
-            for (int b = 0; b < d.emax; b += G) {
-                XT gv[G];
-#pragma unroll
-                for (int u = 0; u < G; u++) {
-                    const int e = b + u;
-                    gv[u] = XT(0);
-                    if (e < E) gv[u] = ld_l2(y + (cw[e * 32 + lane] & kColMask));
-                }
-#pragma unroll
-                for (int u = 0; u < G; u++) {
-                    const int e = b + u;
-                    if (e < E) {
-                        const int r = (int)((unsigned)cw[e * 32 + lane] >> kColBits);
-                        if (r != cur) {
-                            if (cur >= 0) tsh[cur * 32 + lane] = t;
-                            cur = r;
-                            t = tsh[r * 32 + lane];
-                        }
-                        t -= (XT)vw[e * 32 + lane] * gv[u];
-                    }
-                }
-            }
-            if (cur >= 0) tsh[cur * 32 + lane] = t;
-            // in-chain recurrence, rows in solve order
-            const int *iw = cw + d.emax * 32;
-            const VT *iv = vw + d.emax * 32;
-            int e = 0;
-#pragma unroll
-            for (int s = 0; s < BS; s++) {
-                const int r = UPPER ? BS - 1 - s : s;
-                XT tt = tsh[r * 32 + lane];
-                while (e < I) {
-                    const int w = iw[e * 32 + lane];
-                    if ((w >> 8) != r) break;
-                    tt -= (XT)iv[e * 32 + lane] * tsh[(w & 255) * 32 + lane];
-                    e++;
-                }
-                if (UPPER) tt *= dsh[r * 32 + lane];
-                tsh[r * 32 + lane] = tt;
-            }
+            wf_solve_group<VT, XT, BS, UPPER>(d, E, I, cw, vw, tsh, dsh, y, lane);
             if (live) {
 #pragma unroll
                 for (int l = 0; l < BS; l++) y[r0 + l] = tsh[l * 32 + lane];
@@ -841,6 +1019,146 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int ng, const int2 *__restrict__ 
             ctrl[3] = 0;
             __threadfence();
             atomicExch(ctrl + 1, epoch + 1);
+        }
+    }
+}
+
+// One colour per launch on the compact chain layout, one CTA of BS warps per
+// group: warp l takes row l of every chain (lane q = chain q) and subtracts
+// that row's external entries, read from the staged block at lane q's offset
+// for row l (the per-chain row counts give it; reads of slot e*32+q hit bank q
+// whatever e is, so they are conflict-free); warp 0 then runs the in-chain
+// recurrence of every chain on chip; all warps store the finished rows.
+//
+// The group's block, its row counts (TMA) and U's inverted diagonal are read
+// before the kernel waits for the previous kernel (programmatic dependent
+// launch), and the next kernel may start its own prologue once this one has
+// passed its wait. With early_x, x is read before the wait too: the host sets
+// it only where the previous kernel in the chain cannot be writing these rows
+// (not for the first colour of a sweep).
+//
+// RUN: the launch covers a run of small colours, one CTA per group; a CTA
+// waits until the groups of the run that its rows read from have published
+// their flags for this launch (groups of earlier launches are complete by
+// stream order), and publishes its own. A group only waits on lower-numbered
+// CTAs of a run small enough to be resident at once, and every wait is
+// bounded (abort flag and *status = 1); ctrl = {unused, epoch, abort, CTAs
+// finished}, and the last CTA starts the next epoch. A TMA wait that runs out
+// sets *status = 2.
+template <typename VT, typename XT, int BS, bool UPPER, bool RUN>
+__global__ void __launch_bounds__(BS * 32)
+k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
+           const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
+           const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x,
+           const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl)
+{
+    extern __shared__ __align__(128) unsigned char ccs[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ XT tsh[BS][32];
+    __shared__ XT dsh[UPPER ? BS : 1][32];
+    const int g = g0 + blockIdx.x;
+    const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
+    const WfGroup d = groups[g];
+    const int slots = d.emax + d.imax;
+    const unsigned cbytes = (unsigned)slots * 32u * 4u, vbytes = (unsigned)slots * 32u * (unsigned)sizeof(VT);
+    constexpr unsigned nbytes = 32u * 2u * BS;
+    int *cw = reinterpret_cast<int *>(ccs);
+    VT *vw = reinterpret_cast<VT *>(ccs + cbytes);
+    unsigned char *cnt = ccs + cbytes + vbytes;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, cbytes + vbytes + nbytes);
+        if (slots > 0) {
+            bulk_g2s(cw, col + d.off, cbytes, &bar);
+            bulk_g2s(vw, val + d.off, vbytes, &bar);
+        }
+        bulk_g2s(cnt, counts + (size_t)g * nbytes, nbytes, &bar);
+    }
+    __syncthreads();
+    const bool live = q < d.nchains;
+    const int2 ch = live ? __ldg(chains + (size_t)g * 32 + q) : make_int2(0, 0);
+    const int row = ch.x + l;
+    if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + row) : XT(0);
+    XT t = XT(0);
+    if (early_x && live) t = x[row];
+    pdl_wait();  // the previous colour (or the producer of x) has finished
+    pdl_launch_dependents();
+    bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(status, 2);
+        if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
+        ok = false;
+    }
+    if (gated(gate)) return;  // the whole launch returns: no run accounting either
+    int epoch = 0;
+    if (RUN) {
+        epoch = *(volatile const int *)(ctrl + 1);
+        bool bad = !ok;
+        for (int i = dep_ptr[g] + threadIdx.x; !bad && i < dep_ptr[g + 1]; i += blockDim.x) {
+            const int *f = flags + __ldg(dep_idx + i);
+            unsigned k = 0;
+            while (ld_acquire(f) != epoch) {
+                __nanosleep(32);
+                if (++k > kFlagPolls || *(volatile const int *)(ctrl + 2)) {
+                    atomicExch(ctrl + 2, 1);
+                    atomicExch(status, 1);
+                    bad = true;
+                    break;
+                }
+            }
+        }
+        ok = !__syncthreads_or(bad);
+    }
+    if (ok) {
+        if (!early_x && live) t = x[row];
+        // row l's external entries; in lane q's stream rows come in solve order
+        const unsigned char *cq = cnt + q * 2 * BS;
+        int eo = 0;
+#pragma unroll
+        for (int r = 0; r < BS; r++)
+            if (UPPER ? r > l : r < l) eo += cq[r];
+        const int ne = cq[l];
+#pragma unroll 4
+        for (int k = 0; k < ne; k++) {
+            const int at = (eo + k) * 32 + q;
+            t -= (XT)vw[at] * ld_l2(y + (cw[at] & kColMask));
+        }
+        tsh[l][q] = t;
+        __syncthreads();
+        if (l == 0) {
+            const int *iw = cw + d.emax * 32;
+            const VT *iv = vw + d.emax * 32;
+            const int I = (int)((unsigned)ch.y >> 16);
+            int e = 0;
+#pragma unroll 4
+            for (int s = 0; s < BS; s++) {
+                const int r = UPPER ? BS - 1 - s : s;
+                XT tt = tsh[r][q];
+                while (e < I) {
+                    const int w = iw[e * 32 + q];
+                    if ((w >> 8) != r) break;
+                    tt -= (XT)iv[e * 32 + q] * tsh[w & 255][q];
+                    e++;
+                }
+                if (UPPER) tt *= dsh[r][q];
+                tsh[r][q] = tt;
+            }
+        }
+        __syncthreads();
+        if (live) y[row] = tsh[l][q];
+    }
+    if (RUN) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            st_release(flags + g, epoch);
+            __threadfence();
+            if ((unsigned)atomicAdd(ctrl + 3, 1) == gridDim.x - 1) {
+                ctrl[2] = 0;
+                ctrl[3] = 0;
+                __threadfence();
+                atomicExch(ctrl + 1, epoch + 1);
+            }
         }
     }
 }

@@ -10,6 +10,7 @@
 #include <functional>
 
 #include "device.hpp"
+#include "dropin_cache.hpp"
 
 namespace senkgpu {
 
@@ -197,30 +198,30 @@ static void enqueue_orth(System<T> &S, int j, int m, int orth, const int *gate)
     if (orth == SENK_ORTH_MGS) {
         for (int k = 0; k <= j; k++) {
             const T *vk = S.V.p + (long long)k * ld;
-            k_multidot<T, false><<<dim3(kRedCtas, 1), kThreads, 0, s>>>(vk, ld, 1, w, ld, S.red.part.p,
+            launch_multidot<T, false>(dim3(kRedCtas, 1), s, vk, ld, 1, w, ld, S.red.part.p,
                                                                          S.red.ticket.p, S.coef.p, hcol + k, gate);
             if (k == j)
-                k_update<T, kEpiGmres><<<kRedCtas, kThreads, 0, s>>>(vk, ld, 1, S.coef.p, w, ld, S.red.part.p,
+                launch_update<T, kEpiGmres>(kRedCtas, s, vk, ld, 1, S.coef.p, w, ld, S.red.part.p,
                                                                      S.red.ticket.p, nullptr, S.st.p, g, gate);
             else
-                k_update<T, kEpiNone><<<kRedCtas, kThreads, 0, s>>>(vk, ld, 1, S.coef.p, w, ld, S.red.part.p,
+                launch_update<T, kEpiNone>(kRedCtas, s, vk, ld, 1, S.coef.p, w, ld, S.red.part.p,
                                                                     S.red.ticket.p, nullptr, S.st.p, none, gate);
         }
         return;
     }
-    k_multidot<T, false><<<gdot, kThreads, 0, s>>>(S.V.p, ld, nv, w, ld, S.red.part.p, S.red.ticket.p, S.coef.p,
+    launch_multidot<T, false>(gdot, s, S.V.p, ld, nv, w, ld, S.red.part.p, S.red.ticket.p, S.coef.p,
                                                    hcol, gate);
     if (orth == SENK_ORTH_CGS) {
-        k_update<T, kEpiGmres><<<kRedCtas, kThreads, 0, s>>>(S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
+        launch_update<T, kEpiGmres>(kRedCtas, s, S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
                                                              S.red.ticket.p, nullptr, S.st.p, g, gate);
         return;
     }
     // CGS2: second pass corrects the coefficients (H += correction).
-    k_update<T, kEpiNone><<<kRedCtas, kThreads, 0, s>>>(S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
+    launch_update<T, kEpiNone>(kRedCtas, s, S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
                                                         S.red.ticket.p, nullptr, S.st.p, none, gate);
-    k_multidot<T, true><<<gdot, kThreads, 0, s>>>(S.V.p, ld, nv, w, ld, S.red.part.p, S.red.ticket.p, S.coef.p,
+    launch_multidot<T, true>(gdot, s, S.V.p, ld, nv, w, ld, S.red.part.p, S.red.ticket.p, S.coef.p,
                                                   hcol, gate);
-    k_update<T, kEpiGmres><<<kRedCtas, kThreads, 0, s>>>(S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
+    launch_update<T, kEpiGmres>(kRedCtas, s, S.V.p, ld, nv, S.coef.p, w, ld, S.red.part.p,
                                                          S.red.ticket.p, nullptr, S.st.p, g, gate);
 }
 
@@ -359,7 +360,7 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
             else pc->sweep(pc->U, (const T *)t.p, t.p, stream, nullptr);
             break;
         case SENK_OP_DOT:
-            k_multidot<T, false><<<dim3(red.ctas, 1), kThreads, 0, stream>>>(v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
+            launch_multidot<T, false>(dim3(red.ctas, 1), stream, v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
             break;
         default: throw ArgError("unknown op");
         }
@@ -502,15 +503,17 @@ int dropin_gmres(const char *fn, const T *val, const int *cind, const int *rptr,
         d.m_max = m;
         senk_options o{};
         if (opt) o = *opt;
-        System<T> S;
-        S.create(d, &o);
+        std::lock_guard<std::mutex> lk(dropin_mutex());
+        bool built = false;
+        auto sp = dropin_system<T>(fn, d, o, &built);
+        System<T> &S = *sp;
         S.b.upload(b, N, S.stream);
         S.x.upload(x, N, S.stream);
         senk_result r{};
         S.gmres(nrm_b, outer, m, eps, &r);
         SENK_CUDA(cudaMemcpyAsync(x, S.x.p, sizeof(T) * N, cudaMemcpyDeviceToHost, S.stream));
         SENK_CUDA(cudaStreamSynchronize(S.stream));
-        r.h2d_bytes = S.h2d_bytes + 2LL * sizeof(T) * N;
+        r.h2d_bytes = (built ? S.h2d_bytes : 0) + 2LL * sizeof(T) * N;
         r.d2h_bytes = (long long)sizeof(T) * N;
         if (res) *res = r;
         return r.breakdown ? (int)kErrBreakdown : (int)kOk;
@@ -649,6 +652,15 @@ int senk_system_gmres_ir(senk_system *sys, double nrm_b, int max_outer, int m, d
     });
 }
 
+int senk_dropin_cache(int mode)
+{
+    std::lock_guard<std::mutex> lk(dropin_mutex());
+    const int prev = dropin_cache_mode();
+    dropin_cache_mode() = mode ? 1 : 0;
+    if (!mode) dropin_cache_clear();
+    return prev;
+}
+
 int senk_system_apply_pc(senk_system *sys, const void *x, void *y)
 {
     return guarded("senk_system_apply_pc", [&] {
@@ -699,15 +711,17 @@ int senk_abmc_ilu_gmres_ir_d(const double *val, const int *cind, const int *rptr
         d.mixed = 2;  // the FP64 part only computes residuals and updates
         senk_options o{};
         if (opt) o = *opt;
-        System<double> S;
-        S.create(d, &o);
+        std::lock_guard<std::mutex> lk(dropin_mutex());
+        bool built = false;
+        auto sp = dropin_system<double>("senk_abmc_ilu_gmres_ir_d", d, o, &built);
+        System<double> &S = *sp;
         S.b.upload(b, N, S.stream);
         S.x.upload(x, N, S.stream);
         senk_result r{};
         S.gmres_ir(nrm_b, max_outer, m, epsilon, inner_tol, inner_cycles, &r);
         SENK_CUDA(cudaMemcpyAsync(x, S.x.p, sizeof(double) * N, cudaMemcpyDeviceToHost, S.stream));
         SENK_CUDA(cudaStreamSynchronize(S.stream));
-        r.h2d_bytes = S.h2d_bytes + 2LL * sizeof(double) * N;
+        r.h2d_bytes = (built ? S.h2d_bytes : 0) + 2LL * sizeof(double) * N;
         r.d2h_bytes = (long long)sizeof(double) * N;
         if (res) *res = r;
         return r.breakdown ? (int)kErrBreakdown : (int)kOk;

@@ -13,6 +13,7 @@
 #include <functional>
 
 #include "device.hpp"
+#include "dropin_cache.hpp"
 
 namespace senkgpu {
 
@@ -177,7 +178,7 @@ void copy_vec(const T *x, T *y, long long n, cudaStream_t s, const int *gate)
 template <typename T>
 void multidot(System<T> &S, const T *V, long long ldv, int nv, const T *w, double *hcol, const int *gate)
 {
-    k_multidot<T, false><<<dim3(S.red.ctas, (nv + 7) / 8), kThreads, 0, S.stream>>>(
+    launch_multidot<T, false>(dim3(S.red.ctas, (nv + 7) / 8), S.stream, 
         V, ldv, nv, w, S.n, S.red.part.p, S.red.ticket.p, S.coef.p, hcol, gate);
 }
 
@@ -449,8 +450,10 @@ int solve_dropin(const char *fn, Method method, const T *val, const int *cind, c
     d.bnw = bnw;
     senk_options o{};
     if (opt) o = *opt;
-    System<T> S;
-    S.create(d, &o);
+    std::lock_guard<std::mutex> lk(dropin_mutex());
+    bool built = false;
+    auto sp = dropin_system<T>(fn, d, o, &built);
+    System<T> &S = *sp;
     S.b.upload(b, N, S.stream);
     S.x.upload(x, N, S.stream);
     senk_result r{};
@@ -459,7 +462,7 @@ int solve_dropin(const char *fn, Method method, const T *val, const int *cind, c
     else S.bicgstab(nrm_b, outer_or_maxit, eps, &r);
     SENK_CUDA(cudaMemcpyAsync(x, S.x.p, sizeof(T) * N, cudaMemcpyDeviceToHost, S.stream));
     SENK_CUDA(cudaStreamSynchronize(S.stream));
-    r.h2d_bytes = S.h2d_bytes + 2LL * sizeof(T) * N;
+    r.h2d_bytes = (built ? S.h2d_bytes : 0) + 2LL * sizeof(T) * N;
     r.d2h_bytes = (long long)sizeof(T) * N;
     if (res) *res = r;
     return r.breakdown ? (int)kErrBreakdown : (int)kOk;

@@ -178,9 +178,14 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.widths.alloc(wd.size());
     F.widths.upload(wd.data(), wd.size(), s);
     F.dataflow = false;
+    F.compact = false;
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
 }
+
+// Largest block staged through shared memory; bigger groups read the factor
+// from global memory instead.
+constexpr size_t kMaxStagedBytes = 160 * 1024;
 
 // Largest dynamic shared memory of one dataflow CTA.
 constexpr size_t kMaxWfSmem = 200 * 1024;
@@ -190,24 +195,28 @@ constexpr size_t kMaxWfSmem = 200 * 1024;
 // memory; the caller then takes the row-slot layout.
 template <typename VT>
 bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
-                     const std::vector<Group> &colours, int bs, const std::vector<int> &colour_of, cudaStream_t s)
+                     const std::vector<Group> &colours, int bs, const std::vector<int> &colour_of, bool dataflow,
+                     cudaStream_t s)
 {
     std::vector<WfColour> cr;
     for (const Group &g : colours) cr.push_back({g.p0, g.p1});
     WfLayout<VT> lay;
-    if (!make_wf_layout(lay, upper, N, val, cind, rptr, cr, bs, colour_of.data(), kMaxWfSmem)) return false;
+    if (!make_wf_layout(lay, upper, N, val, cind, rptr, cr, bs, colour_of.data(),
+                        dataflow ? kMaxWfSmem : kMaxStagedBytes))
+        return false;
     const int ng = (int)lay.groups.size();
     F.upper = upper;
     F.mapped = false;
     F.bs = bs;
-    F.dataflow = true;
+    F.compact = true;
+    F.dataflow = dataflow;
     F.ngroups = ng;
     F.slots_max = lay.slots_max;
     F.elems = (long long)lay.col.size();
     F.nnz = lay.stored + (upper ? N : 0);
-    F.colour_groups.assign(1, 0);
-    F.colour_groups.push_back(ng);
-    F.colour_smem.assign(1, 0);
+    F.colour_groups = lay.colour_groups;
+    F.colour_slots = lay.colour_slots;
+    F.colour_smem.assign(F.colour_slots.size(), 0);
     F.val.alloc(std::max<size_t>(lay.val.size(), 1));
     F.val.upload(lay.val.data(), lay.val.size(), s);
     F.col.alloc(std::max<size_t>(lay.col.size(), 1));
@@ -220,15 +229,75 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.wgroups.upload(lay.groups.data(), ng, s);
     F.wchains.alloc(std::max<size_t>(lay.chains.size(), 1));
     F.wchains.upload(lay.chains.data(), lay.chains.size(), s);
-    F.dep_ptr.alloc(lay.dep_ptr.size());
-    F.dep_ptr.upload(lay.dep_ptr.data(), lay.dep_ptr.size(), s);
-    F.dep_idx.alloc(std::max<size_t>(lay.dep_idx.size(), 1));
-    F.dep_idx.upload(lay.dep_idx.data(), lay.dep_idx.size(), s);
-    F.flags.alloc(std::max(ng, 1));
-    SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
-    const int ctrl0[4] = {0, 1, 0, 0};  // counter, epoch, abort, warps finished
-    F.ctrl.alloc(4);
-    F.ctrl.upload(ctrl0, 4, s);
+    F.wcounts.alloc(std::max<size_t>(lay.counts.size(), 16));
+    F.wcounts.upload(lay.counts.data(), lay.counts.size(), s);
+    if (!dataflow) {
+        // Launches: one per colour, except that consecutive colours of at most
+        // kRunGroups groups each (the few-group colours at the end of L and the
+        // start of U) share one flag-synchronised launch of at most
+        // kRunMaxGroups CTAs, all resident at once.
+        constexpr int kRunGroups = 160, kRunMaxGroups = 512;
+        const int nc = (int)lay.colour_groups.size() - 1;
+        auto block_smem = [&](int c0, int c1) {
+            int sl = 0;
+            for (int c = c0; c < c1; c++) sl = std::max(sl, lay.colour_slots[c]);
+            return ((size_t)sl * 32 * (4 + sizeof(VT)) + 32 * 2 * (size_t)bs + 15) / 16 * 16;
+        };
+        std::vector<int> in_run(ng, -1);
+        std::vector<int> dptr(ng + 1, 0), didx;
+        for (int c = 0; c < nc;) {
+            int e = c;
+            int tot = 0;
+            while (e < nc && lay.colour_groups[e + 1] - lay.colour_groups[e] <= kRunGroups &&
+                   tot + (lay.colour_groups[e + 1] - lay.colour_groups[e]) <= kRunMaxGroups) {
+                tot += lay.colour_groups[e + 1] - lay.colour_groups[e];
+                e++;
+            }
+            typename SweepFactor<VT>::Launch L{};
+            L.early_x = c > 0;
+            if (e - c >= 2) {
+                L.g0 = lay.colour_groups[c];
+                L.g1 = lay.colour_groups[e];
+                L.run = true;
+                L.smem = block_smem(c, e);
+                for (int g = L.g0; g < L.g1; g++) in_run[g] = L.g0;
+                c = e;
+            } else {
+                L.g0 = lay.colour_groups[c];
+                L.g1 = lay.colour_groups[c + 1];
+                L.run = false;
+                L.smem = block_smem(c, c + 1);
+                c++;
+            }
+            if (L.g1 > L.g0) F.launches.push_back(L);
+        }
+        // dependencies of run groups on groups of the same run
+        for (int g = 0; g < ng; g++) {
+            if (in_run[g] >= 0)
+                for (int k = lay.dep_ptr[g]; k < lay.dep_ptr[g + 1]; k++)
+                    if (lay.dep_idx[k] >= in_run[g]) didx.push_back(lay.dep_idx[k]);
+            dptr[g + 1] = (int)didx.size();
+        }
+        F.dep_ptr.alloc(dptr.size());
+        F.dep_ptr.upload(dptr.data(), dptr.size(), s);
+        F.dep_idx.alloc(std::max<size_t>(didx.size(), 1));
+        F.dep_idx.upload(didx.data(), didx.size(), s);
+        F.flags.alloc(std::max(ng, 1));
+        SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
+        const int ctrl0[4] = {0, 1, 0, 0};  // unused, epoch, abort, CTAs finished
+        F.ctrl.alloc(4);
+        F.ctrl.upload(ctrl0, 4, s);
+    } else {
+        F.dep_ptr.alloc(lay.dep_ptr.size());
+        F.dep_ptr.upload(lay.dep_ptr.data(), lay.dep_ptr.size(), s);
+        F.dep_idx.alloc(std::max<size_t>(lay.dep_idx.size(), 1));
+        F.dep_idx.upload(lay.dep_idx.data(), lay.dep_idx.size(), s);
+        F.flags.alloc(std::max(ng, 1));
+        SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
+        const int ctrl0[4] = {0, 1, 0, 0};  // counter, epoch, abort, warps finished
+        F.ctrl.alloc(4);
+        F.ctrl.upload(ctrl0, 4, s);
+    }
     SENK_CUDA(cudaStreamSynchronize(s));  // the layout's host arrays are released on return
     return true;
 }
@@ -266,9 +335,6 @@ void level_schedule(int N, const int *cind, const int *rptr, bool upper, std::ve
     for (int l = 0; l <= maxlev; l++) groups.push_back({cnt[l], cnt[l + 1]});
 }
 
-// Largest block staged through shared memory; bigger groups read the factor
-// from global memory instead.
-constexpr size_t kMaxStagedBytes = 160 * 1024;
 
 template <typename VT, typename XT, int BS, bool UPPER, bool MAPPED, bool STAGED>
 void launch_group(const SweepFactor<VT> &F, int *status, int gb, int ge, size_t smem, const XT *x, XT *y,
@@ -322,10 +388,46 @@ void launch_wf(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaSt
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_wf<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p, F.ngroups,
+    SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_wf<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p, 0, F.ngroups,
                                  (const int2 *)F.wchains.p, (const VT *)F.val.p, (const int *)F.col.p,
                                  (const VT *)F.dinv.p, (const int *)F.dep_ptr.p, (const int *)F.dep_idx.p,
                                  F.flags.p, F.ctrl.p, x, y, gate, status, F.slots_max));
+}
+
+// Compact chains, one launch per colour (k_sweep_cc), chained by programmatic
+// dependent launch; runs of small colours share one flag-synchronised launch.
+template <typename VT, typename XT, int BS, bool UPPER>
+void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
+{
+    for (const auto &L : F.launches) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(L.g1 - L.g0);
+        cfg.blockDim = dim3(BS * 32);
+        cfg.dynamicSmemBytes = L.smem;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        auto kern = L.run ? k_sweep_cc<VT, XT, BS, UPPER, true> : k_sweep_cc<VT, XT, BS, UPPER, false>;
+        SENK_CUDA(cudaLaunchKernelEx(&cfg, kern, (const WfGroup *)F.wgroups.p, L.g0, (const int2 *)F.wchains.p,
+                                     (const unsigned char *)F.wcounts.p, (const VT *)F.val.p, (const int *)F.col.p,
+                                     (const VT *)F.dinv.p, x, y, gate, status, (int)L.early_x,
+                                     (const int *)F.dep_ptr.p, (const int *)F.dep_idx.p, F.flags.p, F.ctrl.p));
+    }
+}
+
+template <typename VT, int BS, bool UPPER>
+void shape_cc(SweepFactor<VT> &F)
+{
+    size_t most = 0;
+    for (const auto &L : F.launches) most = std::max(most, L.smem);
+    const int bytes = (int)std::max<size_t>(most, 48 * 1024);
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   bytes));
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   bytes));
 }
 
 // Launch shape of a dataflow sweep: as many warps per CTA (up to 8) as the
@@ -349,16 +451,23 @@ void shape_wf(SweepFactor<VT> &F)
     F.wf_grid = std::max(1, std::min(need, per_sm * sm_count()));
 }
 
+template <typename VT, bool UPPER, int BS>
+void shape_compact_bs(SweepFactor<VT> &F)
+{
+    if (F.dataflow) shape_wf<VT, BS, UPPER>(F);
+    else shape_cc<VT, BS, UPPER>(F);
+}
+
 template <typename VT, bool UPPER>
 void shape_wf_bs(SweepFactor<VT> &F)
 {
     switch (F.bs) {
-    case 1: shape_wf<VT, 1, UPPER>(F); break;
-    case 2: shape_wf<VT, 2, UPPER>(F); break;
-    case 4: shape_wf<VT, 4, UPPER>(F); break;
-    case 8: shape_wf<VT, 8, UPPER>(F); break;
-    case 16: shape_wf<VT, 16, UPPER>(F); break;
-    case 32: shape_wf<VT, 32, UPPER>(F); break;
+    case 1: shape_compact_bs<VT, UPPER, 1>(F); break;
+    case 2: shape_compact_bs<VT, UPPER, 2>(F); break;
+    case 4: shape_compact_bs<VT, UPPER, 4>(F); break;
+    case 8: shape_compact_bs<VT, UPPER, 8>(F); break;
+    case 16: shape_compact_bs<VT, UPPER, 16>(F); break;
+    case 32: shape_compact_bs<VT, UPPER, 32>(F); break;
     default: throw ArgError("unsupported chain length");
     }
 }
@@ -367,16 +476,18 @@ template <typename VT, typename XT, bool UPPER>
 void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
     const int nc = (int)F.colour_groups.size() - 1;
-    if (F.dataflow) {
+    if (F.compact) {
+#define SENK_COMPACT_CASE(BS)                                                      \
+    case BS:                                                                       \
+        if (F.dataflow) launch_wf<VT, XT, BS, UPPER>(F, status, x, y, s, gate);    \
+        else launch_cc<VT, XT, BS, UPPER>(F, status, x, y, s, gate);               \
+        break;
         switch (F.bs) {
-        case 1: launch_wf<VT, XT, 1, UPPER>(F, status, x, y, s, gate); break;
-        case 2: launch_wf<VT, XT, 2, UPPER>(F, status, x, y, s, gate); break;
-        case 4: launch_wf<VT, XT, 4, UPPER>(F, status, x, y, s, gate); break;
-        case 8: launch_wf<VT, XT, 8, UPPER>(F, status, x, y, s, gate); break;
-        case 16: launch_wf<VT, XT, 16, UPPER>(F, status, x, y, s, gate); break;
-        case 32: launch_wf<VT, XT, 32, UPPER>(F, status, x, y, s, gate); break;
+            SENK_COMPACT_CASE(1) SENK_COMPACT_CASE(2) SENK_COMPACT_CASE(4) SENK_COMPACT_CASE(8)
+            SENK_COMPACT_CASE(16) SENK_COMPACT_CASE(32)
         default: throw ArgError("unsupported chain length");
         }
+#undef SENK_COMPACT_CASE
         SENK_LAUNCH_CHECK();
         return;
     }
@@ -449,17 +560,19 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    // Measured on the 128^3 convection-diffusion system: the dataflow sweeps on
-    // compact chains are the default; SENK_SWEEP_COLOURS keeps one launch per
-    // colour on row slots.
-    const bool wf = sweep_mode != SENK_SWEEP_COLOURS;
-    if (!(wf && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, s)))
+    // Compact chains, one launch per colour (AUTO) or one dataflow launch per
+    // sweep (DATAFLOW); SENK_SWEEP_COLOURS keeps the row-slot layout with one
+    // CTA per group. A factor whose widest group does not fit shared memory
+    // falls back to row slots.
+    const bool compact = sweep_mode != SENK_SWEEP_COLOURS;
+    const bool df = sweep_mode == SENK_SWEEP_DATAFLOW;
+    if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s)))
         build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
     else
         shape_wf_bs<VT, false>(L);
     // For U, "earlier" means a later colour: flip the colour numbers.
     for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
-    if (!(wf && build_factor_wf(U, true, N, uval, ucind, urptr, bwd, bs, colour_of, s)))
+    if (!(compact && build_factor_wf(U, true, N, uval, ucind, urptr, bwd, bs, colour_of, df, s)))
         build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
     else
         shape_wf_bs<VT, true>(U);

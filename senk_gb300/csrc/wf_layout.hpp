@@ -12,7 +12,10 @@
 // descending for U) and each row's entries in the reference's subtraction
 // order (include/senk_sparse.hpp:132-167: ascending columns for L, descending
 // for U, the U diagonal kept apart as dinv). Column words: external
-// (row << 27) | column; in-chain (row << 8) | chain-local column.
+// (row << 27) | column; in-chain (row << 8) | chain-local column. Per chain
+// also 2*bs bytes: the external then the in-chain entry count of each
+// chain-local row (rows in their natural order), for kernels that split a
+// chain's rows over warps.
 #pragma once
 
 #include <vector_functions.h>
@@ -55,10 +58,13 @@ template <typename VT>
 struct WfLayout {
     std::vector<WfGroup> groups;  // in processing order
     std::vector<int2> chains;     // per group 32 x {first row, E | I << 16} (unused lanes {0, 0})
+    std::vector<unsigned char> counts;  // per group 32 x 2*bs row counts (external, in-chain)
     std::vector<VT> val;          // block values
     std::vector<int> col;         // block column words
     std::vector<VT> dinv;         // U: inverted diagonal per row
     std::vector<int> dep_ptr, dep_idx;  // groups each group reads from (all earlier)
+    std::vector<int> colour_groups;     // group range of each colour (size colours + 1)
+    std::vector<int> colour_slots;      // widest block of each colour
     int slots_max = 0;
     long long stored = 0;         // off-diagonal entries stored
 };
@@ -96,6 +102,14 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
                 else ne++;
             }
         }
+        for (int row = cs; row < ce && ok; row++) {  // at most 255 entries of each kind per row
+            int re = 0, ri = 0;
+            for (int j = rptr[row] + (upper ? 1 : 0); j < rptr[row + 1]; j++) {
+                if (cind[j] >= cs && cind[j] < ce) ri++;
+                else re++;
+            }
+            ok = re <= 255 && ri <= 255;
+        }
         if (!ok || ne > 0xffff || ni > 0x7fff) {
 #pragma omp atomic write
             bad = b;
@@ -110,6 +124,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
     // chains of each colour sorted by their counts, 32 to a group
     std::vector<WfGroup> gd;
     std::vector<int2> chv;
+    std::vector<int> cg(1, 0);
     long long covered = 0;
     for (const WfColour &c : colours) {
         if (c.p0 % bs || c.p1 % bs || c.p1 < c.p0 || c.p0 < 0 || c.p1 > N)
@@ -134,6 +149,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
             }
             gd.push_back(d);
         }
+        cg.push_back((int)gd.size());
     }
     if (covered != N) throw std::invalid_argument("colours do not cover the N rows");
     const int ng = (int)gd.size();
@@ -148,6 +164,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
     if (wf_bytes_for<VT>(smax, bs, upper) > max_smem) return false;
     out.val.assign((size_t)off, VT(0));
     out.col.assign((size_t)off, 0);
+    out.counts.assign((size_t)ng * 32 * 2 * bs, 0);
     out.dinv.assign(upper ? N : 0, VT(0));
     std::vector<int> owner(N, -1);  // group of each row
     long long stored = 0;
@@ -161,13 +178,16 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
                 const int l = upper ? bs - 1 - st : st;  // rows in solve order
                 const int row = r0 + l;
                 owner[row] = g;
+                unsigned char *cnt = out.counts.data() + ((size_t)g * 32 + q) * 2 * bs;
                 auto put = [&](int j) {
                     const int c = cind[j];
                     if (c >= r0 && c < r0 + bs) {
+                        cnt[bs + l]++;
                         const long long at = d.off + (long long)(d.emax + ki++) * 32 + q;
                         out.col[at] = (l << 8) | (c - r0);
                         out.val[at] = val[j];
                     } else {
+                        cnt[l]++;
                         const long long at = d.off + (long long)(ke++) * 32 + q;
                         out.col[at] = (int)(((unsigned)l << kColBits) | (unsigned)c);
                         out.val[at] = val[j];
@@ -219,6 +239,11 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
     out.dep_idx.clear();
     out.dep_idx.reserve(out.dep_ptr[ng]);
     for (int g = 0; g < ng; g++) out.dep_idx.insert(out.dep_idx.end(), deps[g].begin(), deps[g].end());
+    out.colour_slots.assign(cg.size() - 1, 0);
+    for (size_t c = 0; c + 1 < cg.size(); c++)
+        for (int g = cg[c]; g < cg[c + 1]; g++)
+            out.colour_slots[c] = std::max(out.colour_slots[c], gd[g].emax + gd[g].imax);
+    out.colour_groups = std::move(cg);
     out.groups = std::move(gd);
     out.chains = std::move(chv);
     out.slots_max = smax;

@@ -100,6 +100,9 @@ def _declare(L):
     d("senk_system_gmres_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
     d("senk_system_gcr_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
     d("senk_system_apply_pc", [_P, _P, _P])
+    d("senk_dev_ilu0_d", [_P, _P, _P, _I, _P, _I, _I, _P])
+    d("senk_dropin_cache", [_I])
+    d("senk_dev_ilu0_s", [_P, _P, _P, _I, _P, _I, _I, _P])
     d("senk_abmc_ilu_gmres_ir_d", [_P] * 10 + [_I, _I, _P, _P, _D, _I, _I, _I, _D, _D, _I, Op, Rp])
     gd = [_D, _I, _I, _I, _D]
     d("senk_bcsr_gmres_d", [_P] * 5 + gd + [_I, _I, Op, Rp])

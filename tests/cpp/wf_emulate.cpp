@@ -66,6 +66,24 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                 if (!live) continue;
                 const int r0 = ch.x, E = ch.y & 0xffff, I = (int)((unsigned)ch.y >> 16);
                 if (E > d.emax || I > d.imax) return fail("chain count above the group's width");
+                // per-row counts as the CTA-per-group kernel reads them: row l's
+                // external entries start after those of the rows before it in
+                // solve order, and each carries row l in its word
+                const unsigned char *cq = L.counts.data() + ((size_t)g * 32 + lane) * 2 * bs;
+                int esum = 0, isum = 0;
+                for (int l = 0; l < bs; l++) {
+                    int eo = 0;
+                    for (int r = 0; r < bs; r++)
+                        if (upper ? r > l : r < l) eo += cq[r];
+                    for (int k = 0; k < cq[l]; k++) {
+                        const size_t at = (size_t)(eo + k) * 32 + lane;
+                        if (at >= (size_t)d.emax * 32) return fail("row offset beyond the external slots");
+                        if ((int)((unsigned)cw[at] >> kColBits) != l) return fail("row count points at another row");
+                    }
+                    esum += cq[l];
+                    isum += cq[bs + l];
+                }
+                if (esum != E || isum != I) return fail("row counts do not add up to the chain's counts");
                 std::vector<VT> tsh(bs), dsh(bs);
                 for (int l = 0; l < bs; l++) {
                     tsh[l] = yy[r0 + l];
