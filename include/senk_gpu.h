@@ -461,9 +461,11 @@ int senk_mpnn_bind(senk_mpnn *net, senk_system *sys);
 int senk_mpnn_set_loss(senk_mpnn *net, int mode);
 /* Global gradient-norm clip of the Adam steps (default 1; <= 0: off). */
 int senk_mpnn_set_clip(senk_mpnn *net, float clip);
-/* Step of the correction in the GCR hook: 0 (default) K(r) = ILU(r) + c;
- * 1 K(r) = ILU(r) + alpha c, alpha = argmin |r - A(ILU(r) + alpha c)|, computed
- * on the device (one extra SpMV pair and a reduction per application). */
+/* Step of the correction (the GCR hook and senk_mpnn_apply): 1 (default)
+ * K(r) = ILU(r) + alpha c, alpha = argmin |r - A(ILU(r) + alpha c)|, computed on
+ * the device (one extra SpMV pair and a reduction per application), so that one
+ * application never leaves a larger residual than ILU(r) alone; 0 K(r) = ILU(r)
+ * + c. */
 int senk_mpnn_set_step(senk_mpnn *net, int mode);
 /* Loss of one residual/error pair; gradient to grad (host, may be NULL). */
 int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const double *e, double *loss,
@@ -471,7 +473,7 @@ int senk_mpnn_loss_grad(senk_mpnn *net, senk_system *sys, const double *r, const
 /* loss_grad, then one Adam step (beta 0.9 / 0.999, eps 1e-8) with rate lr. */
 int senk_mpnn_train_step(senk_mpnn *net, senk_system *sys, const double *r, const double *e, float lr,
                          double *loss);
-/* out = K(r) (device vectors). */
+/* out = K(r) (device vectors), with the step mode set by senk_mpnn_set_step. */
 int senk_mpnn_apply(senk_mpnn *net, senk_system *sys, const double *r, double *out);
 /* Use K in the system's GCR (net NULL: plain ILU again). When a restart cycle
  * reduces the residual by less than `stall`, the solve falls back to plain ILU

@@ -1125,24 +1125,47 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         }
         tsh[l][q] = t;
         __syncthreads();
-        if (l == 0) {
+        // In-chain recurrence, BS lanes per chain (lane = row), 32 / BS chains
+        // per warp, all warps busy: the rows are finished in solve order; the
+        // lane of the row finished at step s (U: after its inverted diagonal)
+        // broadcasts it by a shuffle within the chain's lanes, and every lane
+        // whose next in-chain entry is that column subtracts it. A lane's
+        // entries come in the same order as the steps (the reference's column
+        // order), two of them held in registers and refilled from the block.
+        if (BS > 1 || UPPER) {
+            constexpr int CPW = 32 / BS;  // chains per warp
+            const int lane = threadIdx.x & 31;
+            const int qc = l * CPW + lane / BS, rr = lane % BS;
             const int *iw = cw + d.emax * 32;
             const VT *iv = vw + d.emax * 32;
-            const int I = (int)((unsigned)ch.y >> 16);
-            int e = 0;
-#pragma unroll 4
+            const unsigned char *cc = cnt + qc * 2 * BS;
+            int io = 0;
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+                if (UPPER ? r > rr : r < rr) io += cc[BS + r];
+            int left = cc[BS + rr];
+            XT tt = tsh[rr][qc];
+            const XT di = UPPER ? dsh[rr][qc] : XT(1);
+            int c0 = -1, c1 = -1;
+            XT v0 = XT(0), v1 = XT(0);
+            int at = io;
+            if (left > 0) { c0 = iw[at * 32 + qc] & 255; v0 = (XT)iv[at * 32 + qc]; at++; }
+            if (left > 1) { c1 = iw[at * 32 + qc] & 255; v1 = (XT)iv[at * 32 + qc]; at++; }
+#pragma unroll
             for (int s = 0; s < BS; s++) {
-                const int r = UPPER ? BS - 1 - s : s;
-                XT tt = tsh[r][q];
-                while (e < I) {
-                    const int w = iw[e * 32 + q];
-                    if ((w >> 8) != r) break;
-                    tt -= (XT)iv[e * 32 + q] * tsh[w & 255][q];
-                    e++;
+                const int c = UPPER ? BS - 1 - s : s;
+                if (UPPER && rr == c) tt *= di;
+                const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
+                if (c0 == c) {
+                    tt -= v0 * yc;
+                    left--;
+                    c0 = c1;
+                    v0 = v1;
+                    c1 = -1;
+                    if (left > 1) { c1 = iw[at * 32 + qc] & 255; v1 = (XT)iv[at * 32 + qc]; at++; }
                 }
-                if (UPPER) tt *= dsh[r][q];
-                tsh[r][q] = tt;
             }
+            tsh[rr][qc] = tt;
         }
         __syncthreads();
         if (live) y[row] = tsh[l][q];

@@ -424,7 +424,7 @@ struct Mpnn {
     DevBuf<double> cstep, acstep, alpha;  // scaled correction c, A c, and the step alpha
     int loss_mode = 1;            // 0: error space, 1: residual space
     float clip = 1.0f;            // global gradient-norm clip of the Adam step (<= 0: off)
-    int step_mode = 0;            // 0: K = ILU + c, 1: K = ILU + alpha c (least-squares alpha)
+    int step_mode = 1;            // 0: K = ILU + c, 1: K = ILU + alpha c (least-squares alpha, the default)
     DevBuf<float> gnorm;
     // activations
     DevBuf<bf16> X[kLayers], Z[kLayers], dZ;
@@ -840,7 +840,7 @@ int senk_mpnn_apply(senk_mpnn *net, senk_system *sys, const double *r, double *o
         System<double> &S = *sys->d;
         SENK_REQUIRE(net->net.bound == &S, "bind the network to this system first");
         S.precondition_base(r, out, nullptr);
-        net->net.apply<double>(r, out, S.stream);
+        net->net.apply_step(S.A, r, out, S.stream);
         net->net.check_status(S.stream);
         return (int)kOk;
     });

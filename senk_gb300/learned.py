@@ -196,21 +196,39 @@ def train(torch, net: Net, n: int, seeds, epochs: int = 1, lr: float = 3e-4, cyc
     return losses
 
 
-def compare_gcr(net: Net, mb: Member, m: int = 20, eps: float = 1e-8, max_outer: int = 500, stall: float = 0.9):
+def compare_gcr(net: Net, mb: Member, m: int = 20, eps: float = 1e-8, max_outer: int = 500, stall: float = 0.9,
+                fixed_cycles: int = 0, gmres_m: int = 0):
     """Plain ILU(0)-GCR(m) and flexible GCR(m) with K = ILU + net on one system:
-    iterations, solve ms, FP64 true residuals, and the fall-back cycle."""
-    sysm = make_system(mb)
+    iterations, solve ms, FP64 true residuals, and the fall-back cycle. With
+    fixed_cycles, both also run exactly that many restart cycles and report the
+    FP64 true residual reached (finer than GCR's restart-granular counts); with
+    gmres_m, plain FP64 ILU(0)-GMRES(gmres_m) on the same system is timed too."""
+    sysm = make_system(mb, m_max=gmres_m)
     nb = float(np.linalg.norm(mb.b))
 
     def true_res(x):
         return float(np.linalg.norm(mb.b - mb.A.matvec(x)) / nb)
 
+    def after_cycles():
+        sysm.set_rhs(mb.b)
+        sysm.gcr(nb, fixed_cycles, m, 1e-300)
+        return true_res(sysm.get_x())
+
     out = {}
+    if gmres_m:
+        sysm.set_rhs(mb.b)
+        sysm.gmres(nb, 10000 // gmres_m, gmres_m, eps)  # warm-up
+        sysm.set_rhs(mb.b)
+        rg: Result = sysm.gmres(nb, 10000 // gmres_m, gmres_m, eps)
+        out["gmres"] = dict(iters=rg.iters, ms=rg.solve_ms, converged=bool(rg.converged),
+                            true_res=true_res(sysm.get_x()))
     sysm.set_rhs(mb.b)
     sysm.gcr(nb, max_outer, m, eps)  # warm-up (graph capture)
     sysm.set_rhs(mb.b)
     r0: Result = sysm.gcr(nb, max_outer, m, eps)
     out["plain"] = dict(iters=r0.iters, ms=r0.solve_ms, converged=bool(r0.converged), true_res=true_res(sysm.get_x()))
+    if fixed_cycles:
+        out["plain"]["res_after_cycles"] = after_cycles()
     net.bind(sysm)
     net.attach(sysm, stall)
     sysm.set_rhs(mb.b)
@@ -221,9 +239,32 @@ def compare_gcr(net: Net, mb: Member, m: int = 20, eps: float = 1e-8, max_outer:
     out["learned"] = dict(iters=r1.iters, ms=r1.solve_ms, converged=bool(r1.converged),
                           true_res=true_res(sysm.get_x()), wall_ms=1e3 * (time.perf_counter() - t0),
                           fallback_cycle=lib().senk_system_learned_fallback(sysm._h))
+    if fixed_cycles:
+        net.attach(sysm, 1e300)  # no fall-back while comparing a fixed number of cycles
+        out["learned"]["res_after_cycles"] = after_cycles()
     Net.detach(sysm)
     sysm.close()
     return out
+
+
+def bytes_per_application(n: int, nnz: int) -> dict:
+    """Bytes one application of the network moves (at least once each), against
+    one FP64 ILU(0) application and one FP64 SpMV on the same graph (n nodes,
+    nnz entries of A): FP32 activations H (64 per node), BF16 GEMM operands X
+    (128 per node: h and the aggregate m), the row-normalised graph (value and
+    column per entry), per layer the aggregate's gathers of neighbours' h rows,
+    its m output, and the GEMM's X read, H read, H and next X written."""
+    layers, hid = LAYERS, HID
+    graph = nnz * 8 + (n + 1) * 4
+    streamed = graph + n * hid * 2 + n * 2 * hid * 2 + n * hid * 4 * 2 + n * hid * 2  # per layer, HBM
+    gathers = nnz * hid * 2                                                          # per layer, mostly L2
+    encode = n * (8 + 8) + n * hid * (4 + 2)
+    decode = n * hid * 4 + n * 8 * 2
+    net = encode + layers * streamed + decode
+    ilu = nnz * 12 + n * 8 * 5
+    spmv = nnz * 12 + 4 * (n + 1) + 16 * n
+    return {"network_streamed": int(net), "network_gathers": int(layers * gathers), "ilu0_fp64": int(ilu),
+            "spmv_fp64": int(spmv), "network_over_ilu": round(net / ilu, 1)}
 
 
 def main(argv=None):
@@ -247,18 +288,22 @@ def main(argv=None):
     ap.add_argument("--m", type=int, default=20)
     ap.add_argument("--loss", type=int, default=1, help="1 residual space, 0 error space")
     ap.add_argument("--save", default=None, help="write the trained parameters (.npy)")
-    ap.add_argument("--step", type=int, default=0, help="1: least-squares step of the correction in the GCR")
+    ap.add_argument("--step", type=int, default=1, help="0: fixed step, 1: least-squares step of the correction")
+    ap.add_argument("--fixed-cycles", type=int, default=3, help="also compare residuals after this many cycles")
+    ap.add_argument("--gmres", type=int, default=30, help="also time plain FP64 ILU(0)-GMRES(m) (0: no)")
+    ap.add_argument("--load", default=None, help="start from these parameters (.npy)")
     args = ap.parse_args(argv)
-    net = Net(seed=0)
+    net = Net(np.load(args.load) if args.load else None, seed=0)
     net.set_loss(args.loss)
     net.set_step(args.step)
     check("senk_mpnn_set_clip", lib().senk_mpnn_set_clip(net._h, args.clip))
     t0 = time.perf_counter()
-    losses = train(torch, net, args.n, range(1000, 1000 + args.train), args.epochs, args.lr)
+    losses = train(torch, net, args.n, range(1000, 1000 + args.train), args.epochs, args.lr) if args.train else [0.0]
     train_s = time.perf_counter() - t0
     results = []
     for s in range(900000, 900000 + args.test):
-        results.append(dict(seed=s, **compare_gcr(net, family_member(args.n, s), m=args.m)))
+        results.append(dict(seed=s, **compare_gcr(net, family_member(args.n, s), m=args.m,
+                                                  fixed_cycles=args.fixed_cycles, gmres_m=args.gmres)))
     if args.save:
         np.save(args.save, net.params)
     plain = [r["plain"]["iters"] for r in results]
@@ -270,6 +315,15 @@ def main(argv=None):
                learned_ms=[round(r["learned"]["ms"], 2) for r in results],
                learned_true_res=[r["learned"]["true_res"] for r in results],
                fallback=[r["learned"]["fallback_cycle"] for r in results])
+    if args.fixed_cycles:
+        out["plain_res_after_cycles"] = [r["plain"]["res_after_cycles"] for r in results]
+        out["learned_res_after_cycles"] = [r["learned"]["res_after_cycles"] for r in results]
+    if args.gmres:
+        out["gmres_fp64_iters"] = [r["gmres"]["iters"] for r in results]
+        out["gmres_fp64_ms"] = [round(r["gmres"]["ms"], 2) for r in results]
+    mb = family_member(args.n, 900000) if args.test else None
+    if mb is not None:
+        out["bytes_per_application"] = bytes_per_application(mb.A.n, mb.A.nnz)
     print(json.dumps(out))
     net.close()
 

@@ -61,6 +61,7 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
             const int *cw = L.col.data() + d.off;
             const VT *vw = L.val.data() + d.off;
             for (int lane = 0; lane < 32; lane++) {
+                bool par_check = false;
                 const bool live = lane < d.nchains;
                 const int2 ch = L.chains[(size_t)g * 32 + lane];
                 if (!live) continue;
@@ -84,6 +85,10 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                     isum += cq[bs + l];
                 }
                 if (esum != E || isum != I) return fail("row counts do not add up to the chain's counts");
+                // the lane-per-row form of the in-chain recurrence (k_sweep_cc)
+                // is checked against the sequential walk below: tsh_par holds
+                // its result, computed from the same phase-1 values
+                par_check = true;
                 std::vector<VT> tsh(bs), dsh(bs);
                 for (int l = 0; l < bs; l++) {
                     tsh[l] = yy[r0 + l];
@@ -108,6 +113,45 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                     t -= vw[at] * yy[c];
                 }
                 if (cur >= 0) tsh[cur] = t;
+                std::vector<VT> tsh_par(tsh);
+                if (par_check) {
+                    // lane rr keeps its next two in-chain entries; step s finishes
+                    // column c and every lane whose next entry is c uses it
+                    std::vector<int> left(bs), at(bs), c0(bs, -1), c1(bs, -1);
+                    std::vector<VT> v0(bs, 0), v1(bs, 0);
+                    const int *iw = cw + (size_t)d.emax * 32;
+                    const VT *iv = vw + (size_t)d.emax * 32;
+                    for (int rr = 0; rr < bs; rr++) {
+                        int io = 0;
+                        for (int r = 0; r < bs; r++)
+                            if (upper ? r > rr : r < rr) io += cq[bs + r];
+                        left[rr] = cq[bs + rr];
+                        at[rr] = io;
+                        if (left[rr] > 0) { c0[rr] = iw[(size_t)at[rr] * 32 + lane] & 255; v0[rr] = iv[(size_t)at[rr] * 32 + lane]; at[rr]++; }
+                        if (left[rr] > 1) { c1[rr] = iw[(size_t)at[rr] * 32 + lane] & 255; v1[rr] = iv[(size_t)at[rr] * 32 + lane]; at[rr]++; }
+                    }
+                    for (int s = 0; s < bs; s++) {
+                        const int c = upper ? bs - 1 - s : s;
+                        if (upper) tsh_par[c] *= dsh[c];
+                        const VT yc = tsh_par[c];
+                        for (int rr = 0; rr < bs; rr++) {
+                            if (rr == c || c0[rr] != c) continue;
+                            tsh_par[rr] -= v0[rr] * yc;
+                            left[rr]--;
+                            c0[rr] = c1[rr];
+                            v0[rr] = v1[rr];
+                            c1[rr] = -1;
+                            if (left[rr] > 1) {
+                                if ((size_t)at[rr] >= (size_t)d.imax) return fail("in-chain window beyond the block");
+                                c1[rr] = iw[(size_t)at[rr] * 32 + lane] & 255;
+                                v1[rr] = iv[(size_t)at[rr] * 32 + lane];
+                                at[rr]++;
+                            }
+                        }
+                    }
+                    for (int rr = 0; rr < bs; rr++)
+                        if (left[rr] != 0) return fail("lane-per-row recurrence left entries unused");
+                }
                 int e = 0;
                 for (int s = 0; s < bs; s++) {
                     const int r = upper ? bs - 1 - s : s;
@@ -127,6 +171,8 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                     tsh[r] = tt;
                 }
                 if (e != I) return fail("in-chain entries left over");
+                for (int r = 0; r < bs; r++)
+                    if (tsh_par[r] != tsh[r]) return fail("lane-per-row recurrence differs from the sequential one");
                 for (int l = 0; l < bs; l++) yy[r0 + l] = tsh[l];
             }
             for (int lane = 0; lane < d.nchains; lane++)

@@ -71,6 +71,7 @@ def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
     net = LN.Net(params)
     try:
         net.bind(sysm)
+        net.set_step(0)
         rng = np.random.default_rng(5)
         r = rng.standard_normal(mb.A.n)
         e = rng.standard_normal(mb.A.n) * 0.05
@@ -86,6 +87,21 @@ def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
         corr_got, corr_want = got - ilu_h, want - ilu_h
         assert rel(corr_got, corr_want) <= 1e-2
         assert rel(got, want) <= 1e-3
+        # the least-squares step, element by element: K(r) = ILU(r) + alpha c with
+        # alpha = (q . Ac) / (Ac . Ac), q = r - A ILU(r), in FP64 on the host
+        net.set_step(1)
+        out1 = torch.zeros_like(rd)
+        net.apply(sysm, rd.data_ptr(), out1.data_ptr())
+        got1 = out1.cpu().numpy()
+        q = r - mb.A.matvec(ilu_h)
+        ac = mb.A.matvec(corr_want)
+        alpha = float(q @ ac / (ac @ ac))
+        want1 = ilu_h + alpha * corr_want
+        alpha_got = float((got1 - ilu_h) @ corr_want / (corr_want @ corr_want))
+        assert abs(alpha_got - alpha) <= 1e-2 * abs(alpha), (alpha_got, alpha)
+        assert rel(got1, want1) <= 1e-3
+        # one application leaves no larger residual than ILU(r) alone
+        assert np.linalg.norm(r - mb.A.matvec(got1)) <= np.linalg.norm(q) * (1 + 1e-6)
         for mode in (1, 0):
             net.set_loss(mode)
             loss, grad = net.loss_grad(sysm, rd.data_ptr(), ed.data_ptr())
@@ -94,7 +110,9 @@ def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
             for lo, hi in [(M.OFF_WIN, M.OFF_LAYER)] + [
                     (M.OFF_LAYER + l * M.LAYER_SIZE, M.OFF_LAYER + (l + 1) * M.LAYER_SIZE)
                     for l in range(M.LAYERS)] + [(M.OFF_WOUT, M.NPARAMS)]:
-                assert rel(grad[lo:hi], gw[lo:hi]) <= 2e-2, (mode, lo, hi, rel(grad[lo:hi], gw[lo:hi]))
+                err = rel(grad[lo:hi], gw[lo:hi])
+                print(f"gradient block [{lo}, {hi}) mode {mode}: {err:.2e}")
+                assert err <= 2e-2, (mode, lo, hi, err)
     finally:
         net.close()
         sysm.close()
@@ -122,7 +140,7 @@ def test_least_squares_step_gcr_converges(torch):
     net = LN.Net(seed=0)
     try:
         LN.train(torch, net, 16, seeds=range(100, 116), epochs=3, lr=3e-4)
-        net.set_step(1)
+        net.set_step(1)  # (the default)
         for s in (900, 901):
             c = LN.compare_gcr(net, LN.family_member(16, s), m=20)
             assert c["learned"]["converged"] and c["learned"]["true_res"] < 1e-8
@@ -136,6 +154,7 @@ def test_stagnating_network_falls_back_to_plain_ilu(torch):
     p = M.init_params(1)
     p[M.OFF_WOUT:M.OFF_BOUT] = 50.0  # a large, useless correction
     net = LN.Net(p)
+    net.set_step(0)  # the fixed step: the least-squares step would only shrink it
     try:
         c = LN.compare_gcr(net, mb, m=20, stall=0.9)
         assert c["learned"]["converged"] and c["learned"]["true_res"] < 1e-8
