@@ -16,10 +16,15 @@ namespace solver {
 template <typename T>
 void Bicgstab(T *val, int *cind, int *rptr, T *b, T *x, T nrm_b, int max_iter, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "Bicgstab: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_bicgstab_d(val, cind, rptr, b, x, nrm_b, max_iter, N, epsilon, &o, nullptr),
-                  "senk_bicgstab_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_bicgstab_s(val, cind, rptr, b, x, nrm_b, max_iter, N, epsilon, &o, nullptr),
+                      "senk_bicgstab_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "Bicgstab: T must be double or float");
+        device::Check(senk_bicgstab_d(val, cind, rptr, b, x, nrm_b, max_iter, N, epsilon, &o, nullptr),
+                      "senk_bicgstab_d");
+    }
 }
 
 /** IluBicgstab<T> (:107-196). */
@@ -27,11 +32,17 @@ template <typename T>
 void IluBicgstab(T *val, int *cind, int *rptr, T *lval, int *lcind, int *lrptr, T *uval, int *ucind, int *urptr,
                  T *b, T *x, T nrm_b, int max_iter, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "IluBicgstab: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_ilu_bicgstab_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, max_iter,
-                                      N, epsilon, &o, nullptr),
-                  "senk_ilu_bicgstab_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_ilu_bicgstab_s(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b,
+                                          max_iter, N, epsilon, &o, nullptr),
+                      "senk_ilu_bicgstab_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "IluBicgstab: T must be double or float");
+        device::Check(senk_ilu_bicgstab_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b,
+                                          max_iter, N, epsilon, &o, nullptr),
+                      "senk_ilu_bicgstab_d");
+    }
 }
 
 /** IlubBicgstab<T,bnl,bnw> (:198-267). */

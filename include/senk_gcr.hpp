@@ -16,9 +16,13 @@ namespace solver {
 template <typename T>
 void Gcrm(T *val, int *cind, int *rptr, T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "Gcrm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_gcr_d(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, &o, nullptr), "senk_gcr_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_gcr_s(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, &o, nullptr), "senk_gcr_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "Gcrm: T must be double or float");
+        device::Check(senk_gcr_d(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, &o, nullptr), "senk_gcr_d");
+    }
 }
 
 /** IluGcrm<T> (:93-161). */
@@ -26,11 +30,17 @@ template <typename T>
 void IluGcrm(T *val, int *cind, int *rptr, T *lval, int *lcind, int *lrptr, T *uval, int *ucind, int *urptr, T *b,
              T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "IluGcrm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_ilu_gcr_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, outer, m, N,
-                                 epsilon, &o, nullptr),
-                  "senk_ilu_gcr_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_ilu_gcr_s(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, outer, m,
+                                     N, epsilon, &o, nullptr),
+                      "senk_ilu_gcr_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "IluGcrm: T must be double or float");
+        device::Check(senk_ilu_gcr_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, outer, m,
+                                     N, epsilon, &o, nullptr),
+                      "senk_ilu_gcr_d");
+    }
 }
 
 /** IlubGcrm<T,bnl,bnw> (:163-231). */

@@ -20,10 +20,14 @@ namespace solver {
 template <typename T>
 void Gmresm(T *val, int *cind, int *rptr, T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "Gmresm: the GPU library implements T = double");
     senk_options o = device::Printing();
     o.orth = SENK_ORTH_MGS;  // the reference's Gram-Schmidt
-    device::Check(senk_gmres_d(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, &o, nullptr), "senk_gmres_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_gmres_s(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, &o, nullptr), "senk_gmres_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "Gmresm: T must be double or float");
+        device::Check(senk_gmres_d(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, &o, nullptr), "senk_gmres_d");
+    }
 }
 
 /** Gmresm<T,bnl,bnw> (:113-195): GMRES(m) on a BCSR matrix. */
@@ -60,11 +64,17 @@ template <typename T>
 void AmcIluGmresm(T *val, int *cind, int *rptr, T *lval, int *lcind, int *lrptr, T *uval, int *ucind, int *urptr,
                   int *cptr, int cnum, T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "AmcIluGmresm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_amc_ilu_gmres_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, b, x,
-                                       nrm_b, outer, m, N, epsilon, &o, nullptr),
-                  "senk_amc_ilu_gmres_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_amc_ilu_gmres_s(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, b, x,
+                                           nrm_b, outer, m, N, epsilon, &o, nullptr),
+                      "senk_amc_ilu_gmres_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "AmcIluGmresm: T must be double or float");
+        device::Check(senk_amc_ilu_gmres_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, b, x,
+                                           nrm_b, outer, m, N, epsilon, &o, nullptr),
+                      "senk_amc_ilu_gmres_d");
+    }
 }
 
 /** AbmcIluGmresm<T> (:391-465): sweeps colour by colour over ABMC blocks. */

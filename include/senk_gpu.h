@@ -108,6 +108,12 @@ int senk_gmres_d(const double *val, const int *cind, const int *rptr,
                  int outer, int m, int N, double epsilon,
                  const senk_options *opt, senk_result *res);
 
+/* senk::solver::Gmresm<float> (include/senk_gmres.hpp:33-37) */
+int senk_gmres_s(const float *val, const int *cind, const int *rptr,
+                 const float *b, float *x, float nrm_b,
+                 int outer, int m, int N, float epsilon,
+                 const senk_options *opt, senk_result *res);
+
 /* senk::solver::IluGmresm<T> (include/senk_gmres.hpp:197-203) */
 int senk_ilu_gmres_d(const double *val, const int *cind, const int *rptr,
                      const double *lval, const int *lcind, const int *lrptr,
@@ -129,6 +135,15 @@ int senk_amc_ilu_gmres_d(const double *val, const int *cind, const int *rptr,
                          const int *cptr, int cnum,
                          const double *b, double *x, double nrm_b,
                          int outer, int m, int N, double epsilon,
+                         const senk_options *opt, senk_result *res);
+
+/* senk::solver::AmcIluGmresm<float> (include/senk_gmres.hpp:293-300) */
+int senk_amc_ilu_gmres_s(const float *val, const int *cind, const int *rptr,
+                         const float *lval, const int *lcind, const int *lrptr,
+                         const float *uval, const int *ucind, const int *urptr,
+                         const int *cptr, int cnum,
+                         const float *b, float *x, float nrm_b,
+                         int outer, int m, int N, float epsilon,
                          const senk_options *opt, senk_result *res);
 
 /* senk::solver::AbmcIluGmresm<T> (include/senk_gmres.hpp:391-398) */
@@ -209,6 +224,17 @@ int senk_ilu_gcr_d(const double *val, const int *cind, const int *rptr,
                    const double *b, double *x, double nrm_b,
                    int outer, int m, int N, double epsilon,
                    const senk_options *opt, senk_result *res);
+/* senk::solver::Gcrm<float>, IluGcrm<float> (include/senk_gcr.hpp:30-34, 93-99) */
+int senk_gcr_s(const float *val, const int *cind, const int *rptr,
+               const float *b, float *x, float nrm_b,
+               int outer, int m, int N, float epsilon,
+               const senk_options *opt, senk_result *res);
+int senk_ilu_gcr_s(const float *val, const int *cind, const int *rptr,
+                   const float *lval, const int *lcind, const int *lrptr,
+                   const float *uval, const int *ucind, const int *urptr,
+                   const float *b, float *x, float nrm_b,
+                   int outer, int m, int N, float epsilon,
+                   const senk_options *opt, senk_result *res);
 /* senk::solver::IlubGcrm<double,bnl,bnw> (include/senk_gcr.hpp:163-169) */
 int senk_ilub_gcr_d(const double *val, const int *cind, const int *rptr,
                     const double *blval, const int *blcind, const int *blrptr,
@@ -222,6 +248,17 @@ int senk_bicgstab_d(const double *val, const int *cind, const int *rptr,
                     const double *b, double *x, double nrm_b,
                     int max_iter, int N, double epsilon,
                     const senk_options *opt, senk_result *res);
+/* senk::solver::Bicgstab<float>, IluBicgstab<float> (include/senk_bicgstab.hpp:29-33, 107-113) */
+int senk_bicgstab_s(const float *val, const int *cind, const int *rptr,
+                    const float *b, float *x, float nrm_b,
+                    int max_iter, int N, float epsilon,
+                    const senk_options *opt, senk_result *res);
+int senk_ilu_bicgstab_s(const float *val, const int *cind, const int *rptr,
+                        const float *lval, const int *lcind, const int *lrptr,
+                        const float *uval, const int *ucind, const int *urptr,
+                        const float *b, float *x, float nrm_b,
+                        int max_iter, int N, float epsilon,
+                        const senk_options *opt, senk_result *res);
 /* senk::solver::IluBicgstab<double> (include/senk_bicgstab.hpp:107-113) */
 int senk_ilu_bicgstab_d(const double *val, const int *cind, const int *rptr,
                         const double *lval, const int *lcind, const int *lrptr,

@@ -169,12 +169,10 @@ struct SweepFactor {
     bool dataflow = false;         // compact: one launch per sweep (else one per colour)
     std::vector<int> colour_slots; // compact: widest block of each colour
     DevBuf<unsigned char> wcounts; // compact: per chain, external and in-chain counts of each row
-    // compact, per colour: the launches of a sweep in order; a run covers
-    // several consecutive small colours synchronised by group flags
+    // compact, per colour: the launches of a sweep in order
     struct Launch {
-        int g0, g1;        // groups
-        bool run;          // flag-synchronised run of small colours
-        bool early_x;      // x may be read before the wait on the previous kernel
+        int g0, g1;        // groups of the colour
+        int early_x;       // 1: x is read before the wait on the previous kernel
         size_t smem;       // dynamic shared memory
     };
     std::vector<Launch> launches;

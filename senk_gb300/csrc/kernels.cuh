@@ -576,12 +576,14 @@ k_update_v(const XT *__restrict__ V, long long ldv, int nv, const double *__rest
     }
 }
 
-// Whether the Krylov kernels may take 16-byte vectors for these operands.
+// Whether the Krylov kernels take 16-byte vectors for these operands: FP32
+// vectors only (measured: the FP64 form of the dot product stalls on the
+// texture pipe and runs at less than half the scalar kernel's rate).
 template <typename XT>
 inline bool vec16_ok(const void *a, const void *b, long long n, long long ld)
 {
     constexpr int W = 16 / sizeof(XT);
-    return n % W == 0 && ld % W == 0 && ((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0;
+    return sizeof(XT) == 4 && n % W == 0 && ld % W == 0 && ((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0;
 }
 
 // Launchers that take the 16-byte kernels when the operands allow.
@@ -1027,30 +1029,21 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int g0, int ng, const int2 *__res
 // group: warp l takes row l of every chain (lane q = chain q) and subtracts
 // that row's external entries, read from the staged block at lane q's offset
 // for row l (the per-chain row counts give it; reads of slot e*32+q hit bank q
-// whatever e is, so they are conflict-free); warp 0 then runs the in-chain
-// recurrence of every chain on chip; all warps store the finished rows.
+// whatever e is, so they are conflict-free), gathering y through L1 (earlier
+// colours were written by earlier kernels); then the in-chain recurrence with
+// one lane per row (below); all warps store the finished rows.
 //
 // The group's block, its row counts (TMA) and U's inverted diagonal are read
 // before the kernel waits for the previous kernel (programmatic dependent
-// launch), and the next kernel may start its own prologue once this one has
-// passed its wait. With early_x, x is read before the wait too: the host sets
-// it only where the previous kernel in the chain cannot be writing these rows
-// (not for the first colour of a sweep).
-//
-// RUN: the launch covers a run of small colours, one CTA per group; a CTA
-// waits until the groups of the run that its rows read from have published
-// their flags for this launch (groups of earlier launches are complete by
-// stream order), and publishes its own. A group only waits on lower-numbered
-// CTAs of a run small enough to be resident at once, and every wait is
-// bounded (abort flag and *status = 1); ctrl = {unused, epoch, abort, CTAs
-// finished}, and the last CTA starts the next epoch. A TMA wait that runs out
-// sets *status = 2.
-template <typename VT, typename XT, int BS, bool UPPER, bool RUN>
+// launch). With early_x, x is read before the wait too and the next kernel may
+// start its prologue only once this one has passed its wait; the host sets it
+// only where the kernels still running cannot be writing these rows (not for
+// the first colour of a sweep). A TMA wait that runs out sets *status = 2.
+template <typename VT, typename XT, int BS, bool UPPER>
 __global__ void __launch_bounds__(BS * 32)
 k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
            const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
-           const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x,
-           const int *__restrict__ dep_ptr, const int *__restrict__ dep_idx, int *flags, int *ctrl)
+           const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x)
 {
     extern __shared__ __align__(128) unsigned char ccs[];
     __shared__ __align__(8) unsigned long long bar;
@@ -1081,35 +1074,17 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
     if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + row) : XT(0);
     XT t = XT(0);
     if (early_x && live) t = x[row];
+    if (!early_x) pdl_launch_dependents();
     pdl_wait();  // the previous colour (or the producer of x) has finished
-    pdl_launch_dependents();
-    bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (early_x) pdl_launch_dependents();
+    const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
     if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) atomicExch(status, 2);
         if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
-        ok = false;
+        return;
     }
-    if (gated(gate)) return;  // the whole launch returns: no run accounting either
-    int epoch = 0;
-    if (RUN) {
-        epoch = *(volatile const int *)(ctrl + 1);
-        bool bad = !ok;
-        for (int i = dep_ptr[g] + threadIdx.x; !bad && i < dep_ptr[g + 1]; i += blockDim.x) {
-            const int *f = flags + __ldg(dep_idx + i);
-            unsigned k = 0;
-            while (ld_acquire(f) != epoch) {
-                __nanosleep(32);
-                if (++k > kFlagPolls || *(volatile const int *)(ctrl + 2)) {
-                    atomicExch(ctrl + 2, 1);
-                    atomicExch(status, 1);
-                    bad = true;
-                    break;
-                }
-            }
-        }
-        ok = !__syncthreads_or(bad);
-    }
-    if (ok) {
+    if (gated(gate)) return;
+    {
         if (!early_x && live) t = x[row];
         // row l's external entries; in lane q's stream rows come in solve order
         const unsigned char *cq = cnt + q * 2 * BS;
@@ -1121,7 +1096,7 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 #pragma unroll 4
         for (int k = 0; k < ne; k++) {
             const int at = (eo + k) * 32 + q;
-            t -= (XT)vw[at] * ld_l2(y + (cw[at] & kColMask));
+            t -= (XT)vw[at] * __ldg(y + (cw[at] & kColMask));
         }
         tsh[l][q] = t;
         __syncthreads();
@@ -1169,20 +1144,6 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         }
         __syncthreads();
         if (live) y[row] = tsh[l][q];
-    }
-    if (RUN) {
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            st_release(flags + g, epoch);
-            __threadfence();
-            if ((unsigned)atomicAdd(ctrl + 3, 1) == gridDim.x - 1) {
-                ctrl[2] = 0;
-                ctrl[3] = 0;
-                __threadfence();
-                atomicExch(ctrl + 1, epoch + 1);
-            }
-        }
     }
 }
 

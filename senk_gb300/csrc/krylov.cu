@@ -747,6 +747,22 @@ int senk_gmres_d(const double *val, const int *cind, const int *rptr, const doub
                                 nullptr, SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
 }
 
+int senk_gmres_s(const float *val, const int *cind, const int *rptr, const float *b, float *x, float nrm_b, int outer,
+                 int m, int N, float epsilon, const senk_options *opt, senk_result *res)
+{
+    return dropin_gmres<float>("senk_gmres_s", val, cind, rptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                               SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+int senk_amc_ilu_gmres_s(const float *val, const int *cind, const int *rptr, const float *lval, const int *lcind,
+                         const int *lrptr, const float *uval, const int *ucind, const int *urptr, const int *cptr,
+                         int cnum, const float *b, float *x, float nrm_b, int outer, int m, int N, float epsilon,
+                         const senk_options *opt, senk_result *res)
+{
+    return dropin_gmres<float>("senk_amc_ilu_gmres_s", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                               SENK_PC_ILU_AMC, cptr, cnum, 1, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
 int senk_ilu_gmres_d(const double *val, const int *cind, const int *rptr, const double *lval, const int *lcind,
                      const int *lrptr, const double *uval, const int *ucind, const int *urptr, const double *b,
                      double *x, double nrm_b, int outer, int m, int N, double epsilon, const senk_options *opt,

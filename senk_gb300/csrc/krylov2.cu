@@ -565,6 +565,46 @@ int senk_ilu_bicgstab_d(const double *val, const int *cind, const int *rptr, con
     });
 }
 
+int senk_gcr_s(const float *val, const int *cind, const int *rptr, const float *b, float *x, float nrm_b, int outer,
+               int m, int N, float epsilon, const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_gcr_s", [&] {
+        return solve_dropin<float>("senk_gcr_s", kGcr, val, cind, rptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                   nullptr, SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+    });
+}
+
+int senk_ilu_gcr_s(const float *val, const int *cind, const int *rptr, const float *lval, const int *lcind,
+                   const int *lrptr, const float *uval, const int *ucind, const int *urptr, const float *b, float *x,
+                   float nrm_b, int outer, int m, int N, float epsilon, const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_ilu_gcr_s", [&] {
+        return solve_dropin<float>("senk_ilu_gcr_s", kGcr, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                                   SENK_PC_ILU, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+    });
+}
+
+int senk_bicgstab_s(const float *val, const int *cind, const int *rptr, const float *b, float *x, float nrm_b,
+                    int max_iter, int N, float epsilon, const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_bicgstab_s", [&] {
+        return solve_dropin<float>("senk_bicgstab_s", kBicgstab, val, cind, rptr, nullptr, nullptr, nullptr, nullptr,
+                                   nullptr, nullptr, SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b, max_iter, 0, N, epsilon,
+                                   opt, res);
+    });
+}
+
+int senk_ilu_bicgstab_s(const float *val, const int *cind, const int *rptr, const float *lval, const int *lcind,
+                        const int *lrptr, const float *uval, const int *ucind, const int *urptr, const float *b,
+                        float *x, float nrm_b, int max_iter, int N, float epsilon, const senk_options *opt,
+                        senk_result *res)
+{
+    return guarded("senk_ilu_bicgstab_s", [&] {
+        return solve_dropin<float>("senk_ilu_bicgstab_s", kBicgstab, val, cind, rptr, lval, lcind, lrptr, uval, ucind,
+                                   urptr, SENK_PC_ILU, nullptr, 0, 0, b, x, nrm_b, max_iter, 0, N, epsilon, opt, res);
+    });
+}
+
 int senk_abmc_ilu_bicgstab_d(const double *val, const int *cind, const int *rptr, const double *lval,
                              const int *lcind, const int *lrptr, const double *uval, const int *ucind,
                              const int *urptr, const int *cptr, int cnum, int bsize, const double *b, double *x,

@@ -232,61 +232,16 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.wcounts.alloc(std::max<size_t>(lay.counts.size(), 16));
     F.wcounts.upload(lay.counts.data(), lay.counts.size(), s);
     if (!dataflow) {
-        // Launches: one per colour, except that consecutive colours of at most
-        // kRunGroups groups each (the few-group colours at the end of L and the
-        // start of U) share one flag-synchronised launch of at most
-        // kRunMaxGroups CTAs, all resident at once.
-        constexpr int kRunGroups = 160, kRunMaxGroups = 512;
+        // one launch per colour; x is read early from the second colour on
         const int nc = (int)lay.colour_groups.size() - 1;
-        auto block_smem = [&](int c0, int c1) {
-            int sl = 0;
-            for (int c = c0; c < c1; c++) sl = std::max(sl, lay.colour_slots[c]);
-            return ((size_t)sl * 32 * (4 + sizeof(VT)) + 32 * 2 * (size_t)bs + 15) / 16 * 16;
-        };
-        std::vector<int> in_run(ng, -1);
-        std::vector<int> dptr(ng + 1, 0), didx;
-        for (int c = 0; c < nc;) {
-            int e = c;
-            int tot = 0;
-            while (e < nc && lay.colour_groups[e + 1] - lay.colour_groups[e] <= kRunGroups &&
-                   tot + (lay.colour_groups[e + 1] - lay.colour_groups[e]) <= kRunMaxGroups) {
-                tot += lay.colour_groups[e + 1] - lay.colour_groups[e];
-                e++;
-            }
+        for (int c = 0; c < nc; c++) {
             typename SweepFactor<VT>::Launch L{};
-            L.early_x = c > 0;
-            if (e - c >= 2) {
-                L.g0 = lay.colour_groups[c];
-                L.g1 = lay.colour_groups[e];
-                L.run = true;
-                L.smem = block_smem(c, e);
-                for (int g = L.g0; g < L.g1; g++) in_run[g] = L.g0;
-                c = e;
-            } else {
-                L.g0 = lay.colour_groups[c];
-                L.g1 = lay.colour_groups[c + 1];
-                L.run = false;
-                L.smem = block_smem(c, c + 1);
-                c++;
-            }
+            L.g0 = lay.colour_groups[c];
+            L.g1 = lay.colour_groups[c + 1];
+            L.early_x = c > 0 ? 1 : 0;
+            L.smem = ((size_t)lay.colour_slots[c] * 32 * (4 + sizeof(VT)) + 32 * 2 * (size_t)bs + 15) / 16 * 16;
             if (L.g1 > L.g0) F.launches.push_back(L);
         }
-        // dependencies of run groups on groups of the same run
-        for (int g = 0; g < ng; g++) {
-            if (in_run[g] >= 0)
-                for (int k = lay.dep_ptr[g]; k < lay.dep_ptr[g + 1]; k++)
-                    if (lay.dep_idx[k] >= in_run[g]) didx.push_back(lay.dep_idx[k]);
-            dptr[g + 1] = (int)didx.size();
-        }
-        F.dep_ptr.alloc(dptr.size());
-        F.dep_ptr.upload(dptr.data(), dptr.size(), s);
-        F.dep_idx.alloc(std::max<size_t>(didx.size(), 1));
-        F.dep_idx.upload(didx.data(), didx.size(), s);
-        F.flags.alloc(std::max(ng, 1));
-        SENK_CUDA(cudaMemsetAsync(F.flags.p, 0, F.flags.bytes(), s));
-        const int ctrl0[4] = {0, 1, 0, 0};  // unused, epoch, abort, CTAs finished
-        F.ctrl.alloc(4);
-        F.ctrl.upload(ctrl0, 4, s);
     } else {
         F.dep_ptr.alloc(lay.dep_ptr.size());
         F.dep_ptr.upload(lay.dep_ptr.data(), lay.dep_ptr.size(), s);
@@ -395,7 +350,7 @@ void launch_wf(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaSt
 }
 
 // Compact chains, one launch per colour (k_sweep_cc), chained by programmatic
-// dependent launch; runs of small colours share one flag-synchronised launch.
+// dependent launch.
 template <typename VT, typename XT, int BS, bool UPPER>
 void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
@@ -410,11 +365,10 @@ void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaSt
         at[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        auto kern = L.run ? k_sweep_cc<VT, XT, BS, UPPER, true> : k_sweep_cc<VT, XT, BS, UPPER, false>;
-        SENK_CUDA(cudaLaunchKernelEx(&cfg, kern, (const WfGroup *)F.wgroups.p, L.g0, (const int2 *)F.wchains.p,
-                                     (const unsigned char *)F.wcounts.p, (const VT *)F.val.p, (const int *)F.col.p,
-                                     (const VT *)F.dinv.p, x, y, gate, status, (int)L.early_x,
-                                     (const int *)F.dep_ptr.p, (const int *)F.dep_idx.p, F.flags.p, F.ctrl.p));
+        SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cc<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p, L.g0,
+                                     (const int2 *)F.wchains.p, (const unsigned char *)F.wcounts.p,
+                                     (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate,
+                                     status, L.early_x));
     }
 }
 
@@ -423,11 +377,8 @@ void shape_cc(SweepFactor<VT> &F)
 {
     size_t most = 0;
     for (const auto &L : F.launches) most = std::max(most, L.smem);
-    const int bytes = (int)std::max<size_t>(most, 48 * 1024);
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   bytes));
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   bytes));
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)std::max<size_t>(most, 48 * 1024)));
 }
 
 // Launch shape of a dataflow sweep: as many warps per CTA (up to 8) as the

@@ -240,7 +240,7 @@ def compare_gcr(net: Net, mb: Member, m: int = 20, eps: float = 1e-8, max_outer:
                           true_res=true_res(sysm.get_x()), wall_ms=1e3 * (time.perf_counter() - t0),
                           fallback_cycle=lib().senk_system_learned_fallback(sysm._h))
     if fixed_cycles:
-        net.attach(sysm, 1e300)  # no fall-back while comparing a fixed number of cycles
+        net.attach(sysm, 1.0)  # fall back only on a cycle without any progress
         out["learned"]["res_after_cycles"] = after_cycles()
     Net.detach(sysm)
     sysm.close()

@@ -87,6 +87,13 @@ def _declare(L):
     d("senk_amc_ilu_gmres_d", [_P] * 10 + [_I, _P, _P, _D, _I, _I, _I, _D, Op, Rp])
     d("senk_abmc_ilu_gmres_d", [_P] * 10 + [_I, _I, _P, _P, _D, _I, _I, _I, _D, Op, Rp])
     d("senk_abmc_ilu_gmres_s", [_P] * 10 + [_I, _I, _P, _P, _Fl, _I, _I, _I, _Fl, Op, Rp])
+    d("senk_gmres_s", [_P, _P, _P, _P, _P, _Fl, _I, _I, _I, _Fl, Op, Rp])
+    d("senk_amc_ilu_gmres_s", [_P] * 10 + [_I, _P, _P, _Fl, _I, _I, _I, _Fl, Op, Rp])
+    fd = [_Fl, _I, _I, _I, _Fl]
+    d("senk_gcr_s", [_P] * 5 + fd + [Op, Rp])
+    d("senk_ilu_gcr_s", [_P] * 11 + fd + [Op, Rp])
+    d("senk_bicgstab_s", [_P] * 5 + [_Fl, _I, _I, _Fl, Op, Rp])
+    d("senk_ilu_bicgstab_s", [_P] * 11 + [_Fl, _I, _I, _Fl, Op, Rp])
     d("senk_system_create", [C.POINTER(_P), C.POINTER(SystemDesc), Op])
     d("senk_system_destroy", [_P])
     d("senk_system_stream", [_P], _P)

@@ -31,11 +31,13 @@ def _arr(a, dtype):
 
 
 def Gmresm(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, **opt) -> Result:
-    """senk::solver::Gmresm<double> (include/senk_gmres.hpp:33-95)."""
+    """senk::solver::Gmresm<T> (include/senk_gmres.hpp:33-95); T from x."""
+    T = _T(x)
+    fn = "senk_gmres_s" if T == np.float32 else "senk_gmres_d"
     r = Result()
-    check("senk_gmres_d", lib().senk_gmres_d(ptr(_arr(val, np.float64)), ptr(_arr(cind, np.int32)),
-                                             ptr(_arr(rptr, np.int32)), ptr(_arr(b, np.float64)), ptr(x),
-                                             nrm_b, outer, m, N, epsilon, C.byref(_opts(**opt)), C.byref(r)))
+    check(fn, getattr(lib(), fn)(ptr(_arr(val, T)), ptr(_arr(cind, np.int32)), ptr(_arr(rptr, np.int32)),
+                                 ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N, epsilon, C.byref(_opts(**opt)),
+                                 C.byref(r)))
     return r
 
 
@@ -54,14 +56,15 @@ def IluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm
 
 def AmcIluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cptr, cnum, b, x, nrm_b, outer, m, N,
                  epsilon, **opt) -> Result:
-    """senk::solver::AmcIluGmresm<double> (include/senk_gmres.hpp:293-367)."""
+    """senk::solver::AmcIluGmresm<T> (include/senk_gmres.hpp:293-367); T from x."""
+    T = _T(x)
+    fn = "senk_amc_ilu_gmres_s" if T == np.float32 else "senk_amc_ilu_gmres_d"
     r = Result()
-    keep = [_arr(val, np.float64), _arr(cind, np.int32), _arr(rptr, np.int32), _arr(lval, np.float64),
-            _arr(lcind, np.int32), _arr(lrptr, np.int32), _arr(uval, np.float64), _arr(ucind, np.int32),
+    keep = [_arr(val, T), _arr(cind, np.int32), _arr(rptr, np.int32), _arr(lval, T),
+            _arr(lcind, np.int32), _arr(lrptr, np.int32), _arr(uval, T), _arr(ucind, np.int32),
             _arr(urptr, np.int32), _arr(cptr, np.int32)]
-    check("senk_amc_ilu_gmres_d",
-          lib().senk_amc_ilu_gmres_d(*[ptr(a) for a in keep], cnum, ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer,
-                                     m, N, epsilon, C.byref(_opts(**opt)), C.byref(r)))
+    check(fn, getattr(lib(), fn)(*[ptr(a) for a in keep], cnum, ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N,
+                                 epsilon, C.byref(_opts(**opt)), C.byref(r)))
     return r
 
 
@@ -140,18 +143,24 @@ def AbmcIlubGmresm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr
                  ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N, epsilon, bnl, bnw, C.byref(_opts(**opt)))
 
 
+def _sfx(T):
+    return "_s" if T == np.float32 else "_d"
+
+
 def Gcrm(val, cind, rptr, b, x, nrm_b, outer, m, N, epsilon, **opt) -> Result:
-    """senk::solver::Gcrm<double> (include/senk_gcr.hpp:30-91)."""
-    k = _csr_args(np.float64, val, cind, rptr)
-    return _call("senk_gcr_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N, epsilon,
+    """senk::solver::Gcrm<T> (include/senk_gcr.hpp:30-91); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr)
+    return _call("senk_gcr" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N, epsilon,
                  C.byref(_opts(**opt)))
 
 
 def IluGcrm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, outer, m, N, epsilon,
             **opt) -> Result:
-    """senk::solver::IluGcrm<double> (include/senk_gcr.hpp:93-161)."""
-    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
-    return _call("senk_ilu_gcr_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+    """senk::solver::IluGcrm<T> (include/senk_gcr.hpp:93-161); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_ilu_gcr" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N,
                  epsilon, C.byref(_opts(**opt)))
 
 
@@ -164,17 +173,19 @@ def IlubGcrm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x
 
 
 def Bicgstab(val, cind, rptr, b, x, nrm_b, max_iter, N, epsilon, **opt) -> Result:
-    """senk::solver::Bicgstab<double> (include/senk_bicgstab.hpp:29-105)."""
-    k = _csr_args(np.float64, val, cind, rptr)
-    return _call("senk_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter, N,
+    """senk::solver::Bicgstab<T> (include/senk_bicgstab.hpp:29-105); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr)
+    return _call("senk_bicgstab" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, max_iter, N,
                  epsilon, C.byref(_opts(**opt)))
 
 
 def IluBicgstab(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b, max_iter, N, epsilon,
                 **opt) -> Result:
-    """senk::solver::IluBicgstab<double> (include/senk_bicgstab.hpp:107-196)."""
-    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
-    return _call("senk_ilu_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter, N,
+    """senk::solver::IluBicgstab<T> (include/senk_bicgstab.hpp:107-196); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_ilu_bicgstab" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, max_iter, N,
                  epsilon, C.byref(_opts(**opt)))
 
 
