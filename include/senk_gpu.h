@@ -71,15 +71,20 @@ typedef struct {
     int sweep;        /* SENK_SWEEP_* */
 } senk_options;
 
-/* How the ILU sweeps of AMC/ABMC factors are scheduled. Chains (ABMC blocks;
- * single rows for AMC) are taken 32 to a group from one colour. */
-#define SENK_SWEEP_AUTO 0     /* compact chain layout, one launch per colour, one
-                                 warp per group (the faster schedule as measured) */
-#define SENK_SWEEP_COLOURS 1  /* row-slot layout, one launch per colour, one CTA
-                                 per group */
+/* How the ILU sweeps are scheduled. Chains (ABMC blocks; single rows for AMC
+ * and the natural order's level sets) are taken 32 to a group from one colour
+ * (level set). */
+#define SENK_SWEEP_AUTO 0     /* the fastest as measured: systems whose vector fits
+                                 in shared memory (up to 192 KB) sweep both factors
+                                 in one CTA; larger ones take SENK_SWEEP_COLOURS */
+#define SENK_SWEEP_COLOURS 1  /* row-slot layout, one launch per colour (level set),
+                                 one CTA per group */
 #define SENK_SWEEP_DATAFLOW 2 /* compact chain layout, one launch per sweep: each
                                  warp takes a group, waits on the flags of the
                                  groups it reads, solves it and publishes its own */
+#define SENK_SWEEP_COMPACT 3  /* compact chain layout (chains packed per lane,
+                                 padding only to the widest chain of a group), one
+                                 launch per colour, one CTA per group */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0

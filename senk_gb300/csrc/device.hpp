@@ -169,6 +169,7 @@ struct SweepFactor {
     bool dataflow = false;         // compact: one launch per sweep (else one per colour)
     std::vector<int> colour_slots; // compact: widest block of each colour
     DevBuf<unsigned char> wcounts; // compact: per chain, external and in-chain counts of each row
+    DevBuf<int> dcolour_groups;    // compact: colour_groups on the device (small systems)
     // compact, per colour: the launches of a sweep in order
     struct Launch {
         int g0, g1;        // groups of the colour
@@ -192,6 +193,12 @@ struct IluPlan {
     int precond = SENK_PC_NONE;
     SweepFactor<VT> L, U;
     DevBuf<int> status;  // non-zero after a sweep whose bounded wait ran out (1: flag, 2: TMA)
+    // small systems (the vector fits in shared memory): both sweeps in one CTA
+    bool small = false;
+    int small_threads = 0;
+    void sweep_small(int which, const VT *x, VT *y, cudaStream_t s, const int *gate) const;
+    void build_small(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
+                     const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s);
 
     // sweep_mode: SENK_SWEEP_AUTO / SENK_SWEEP_DATAFLOW (one dataflow launch per
     // sweep where the schedule is colours of chains) or SENK_SWEEP_COLOURS (one
@@ -204,6 +211,10 @@ struct IluPlan {
     template <typename XT>
     void apply(const XT *x, XT *y, cudaStream_t s, const int *gate) const
     {
+        if (small) {
+            sweep_small(3, (const VT *)x, (VT *)y, s, gate);
+            return;
+        }
         sweep(L, x, y, s, gate);
         sweep(U, (const XT *)y, y, s, gate);
     }

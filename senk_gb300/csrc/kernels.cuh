@@ -815,6 +815,78 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
     if (live) y[row] = tsh[l][q];
 }
 
+// ------------------------------------------------- small systems, one CTA
+// One triangular factor in the compact chain layout, for k_ilu_small.
+template <typename VT>
+struct SmallFactor {
+    const WfGroup *groups;
+    const int2 *chains;
+    const VT *val;
+    const int *col;
+    const VT *dinv;         // U: inverted diagonal per row
+    const int *cgroups;     // group range of each colour (level set), processing order
+    int ncolours;
+};
+
+// Sweeps one factor inside k_ilu_small: colour by colour, one thread per chain
+// (its rows in solve order, each row's external then in-chain entries in the
+// reference's order), the vector in shared memory; a barrier between colours.
+template <typename VT, typename XT, int BS, bool UPPER>
+__device__ __forceinline__ void small_sweep(const SmallFactor<VT> &F, XT *ysh)
+{
+    for (int c = 0; c < F.ncolours; c++) {
+        const int g0 = __ldg(F.cgroups + c), g1 = __ldg(F.cgroups + c + 1);
+        for (int t = threadIdx.x; t < (g1 - g0) * 32; t += blockDim.x) {
+            const int g = g0 + (t >> 5), lane = t & 31;
+            const WfGroup d = F.groups[g];
+            if (lane >= d.nchains) continue;
+            const int2 ch = __ldg(F.chains + (size_t)g * 32 + lane);
+            const int r0 = ch.x, E = ch.y & 0xffff, I = (int)((unsigned)ch.y >> 16);
+            const int *ew = F.col + d.off + lane;
+            const VT *ev = F.val + d.off + lane;
+            const int *iw = ew + d.emax * 32;
+            const VT *iv = ev + d.emax * 32;
+            int e = 0, k = 0;
+            int we = e < E ? __ldg(ew) : 0;
+            int wi = k < I ? __ldg(iw) : 0;
+#pragma unroll
+            for (int s = 0; s < BS; s++) {
+                const int r = UPPER ? BS - 1 - s : s;
+                XT tt = ysh[r0 + r];
+                while (e < E && (int)((unsigned)we >> kColBits) == r) {
+                    tt -= (XT)__ldg(ev + e * 32) * ysh[we & kColMask];
+                    e++;
+                    if (e < E) we = __ldg(ew + e * 32);
+                }
+                while (k < I && (wi >> 8) == r) {
+                    tt -= (XT)__ldg(iv + k * 32) * ysh[r0 + (wi & 255)];
+                    k++;
+                    if (k < I) wi = __ldg(iw + k * 32);
+                }
+                if (UPPER) tt *= (XT)__ldg(F.dinv + r0 + r);
+                ysh[r0 + r] = tt;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Both triangular sweeps of one ILU application y = U^-1 L^-1 x for a system
+// whose vector fits in shared memory: one CTA, no other launch; x == y allowed.
+template <typename VT, typename XT, int BS>
+__global__ void __launch_bounds__(1024)
+k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *y, int n, const int *gate)
+{
+    extern __shared__ __align__(16) unsigned char sms[];
+    XT *ysh = reinterpret_cast<XT *>(sms);
+    if (gated(gate)) return;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) ysh[i] = x[i];
+    __syncthreads();
+    if (which & 1) small_sweep<VT, XT, BS, false>(Lf, ysh);
+    if (which & 2) small_sweep<VT, XT, BS, true>(Uf, ysh);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = ysh[i];
+}
+
 // ------------------------------------------------------ dataflow sweeps
 // One launch per triangular sweep, one group of up to 32 chains per warp.
 //

@@ -190,21 +190,32 @@ constexpr size_t kMaxStagedBytes = 160 * 1024;
 // Largest dynamic shared memory of one dataflow CTA.
 constexpr size_t kMaxWfSmem = 200 * 1024;
 
+// Largest vector the single-CTA sweeps of small systems keep in shared memory.
+constexpr size_t kSmallBytes = 192 * 1024;
+
+template <typename VT, int BS>
+void allow_small()
+{
+    SENK_CUDA(cudaFuncSetAttribute(k_ilu_small<VT, VT, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kSmallBytes));
+}
+
 // Compact chain layout (wf_layout.hpp) uploaded for k_sweep_wf. Returns false
 // (and builds nothing) when a group's block would not fit one warp's shared
 // memory; the caller then takes the row-slot layout.
 template <typename VT>
 bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
                      const std::vector<Group> &colours, int bs, const std::vector<int> &colour_of, bool dataflow,
-                     cudaStream_t s)
+                     cudaStream_t s, const std::vector<int> *rowmap = nullptr)
 {
     std::vector<WfColour> cr;
     for (const Group &g : colours) cr.push_back({g.p0, g.p1});
     WfLayout<VT> lay;
     if (!make_wf_layout(lay, upper, N, val, cind, rptr, cr, bs, colour_of.data(),
-                        dataflow ? kMaxWfSmem : kMaxStagedBytes))
+                        dataflow ? kMaxWfSmem : kMaxStagedBytes, rowmap ? rowmap->data() : nullptr))
         return false;
     const int ng = (int)lay.groups.size();
+    F.launches.clear();
     F.upper = upper;
     F.mapped = false;
     F.bs = bs;
@@ -231,6 +242,8 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.wchains.upload(lay.chains.data(), lay.chains.size(), s);
     F.wcounts.alloc(std::max<size_t>(lay.counts.size(), 16));
     F.wcounts.upload(lay.counts.data(), lay.counts.size(), s);
+    F.dcolour_groups.alloc(lay.colour_groups.size());
+    F.dcolour_groups.upload(lay.colour_groups.data(), lay.colour_groups.size(), s);
     if (!dataflow) {
         // one launch per colour; x is read early from the second colour on
         const int nc = (int)lay.colour_groups.size() - 1;
@@ -473,13 +486,96 @@ void allow_all_smem()
 
 }  // namespace
 
+template <typename VT, int BS>
+void launch_small(const IluPlan<VT> &P, int which, const VT *x, VT *y, cudaStream_t s, const int *gate)
+{
+    auto mk = [](const SweepFactor<VT> &F) {
+        return SmallFactor<VT>{(const WfGroup *)F.wgroups.p, (const int2 *)F.wchains.p, (const VT *)F.val.p,
+                               (const int *)F.col.p, (const VT *)F.dinv.p, (const int *)F.dcolour_groups.p,
+                               (int)F.colour_groups.size() - 1};
+    };
+    k_ilu_small<VT, VT, BS><<<1, P.small_threads, (size_t)P.n * sizeof(VT), s>>>(mk(P.L), mk(P.U), which, x, y, P.n,
+                                                                                 gate);
+    SENK_LAUNCH_CHECK();
+}
+
+template <typename VT>
+void IluPlan<VT>::sweep_small(int which, const VT *x, VT *y, cudaStream_t s, const int *gate) const
+{
+    switch (L.bs) {
+    case 1: launch_small<VT, 1>(*this, which, x, y, s, gate); break;
+    case 2: launch_small<VT, 2>(*this, which, x, y, s, gate); break;
+    case 4: launch_small<VT, 4>(*this, which, x, y, s, gate); break;
+    case 8: launch_small<VT, 8>(*this, which, x, y, s, gate); break;
+    case 16: launch_small<VT, 16>(*this, which, x, y, s, gate); break;
+    case 32: launch_small<VT, 32>(*this, which, x, y, s, gate); break;
+    default: throw ArgError("unsupported chain length");
+    }
+}
+
+// Compact layouts of both factors for k_ilu_small (natural order: level sets,
+// one row per chain; AMC/ABMC: the colours). Leaves `small` false when a
+// factor does not fit the compact layout, so the caller takes the other paths.
+template <typename VT>
+void IluPlan<VT>::build_small(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval,
+                              const int *ucind, const int *urptr, int pckind, const int *cptr, int cnum, int bsize,
+                              cudaStream_t s)
+{
+    small = false;
+    std::vector<Group> gl, gu;
+    std::vector<int> col_l(N), col_u(N), rml, rmu;
+    int bs = 1;
+    if (pckind == SENK_PC_ILU) {
+        level_schedule(N, lcind, lrptr, false, rml, gl);
+        level_schedule(N, ucind, urptr, true, rmu, gu);
+        for (size_t k = 0; k < gl.size(); k++)
+            for (int p = gl[k].p0; p < gl[k].p1; p++) col_l[rml[p]] = (int)k;
+        for (size_t k = 0; k < gu.size(); k++)
+            for (int p = gu[k].p0; p < gu[k].p1; p++) col_u[rmu[p]] = (int)k;
+    } else {
+        SENK_REQUIRE(pckind == SENK_PC_ILU_AMC || pckind == SENK_PC_ILU_ABMC, "unknown preconditioner kind");
+        bs = pckind == SENK_PC_ILU_AMC ? 1 : bsize;
+        SENK_REQUIRE(bs == 1 || bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32,
+                     "ABMC block size must be 1, 2, 4, 8, 16 or 32 on the GPU path (got " + std::to_string(bs) + ")");
+        SENK_REQUIRE(cptr && cnum > 0, "colour pointer missing");
+        SENK_REQUIRE(cptr[0] == 0 && (long long)cptr[cnum] * bs == N, "colour pointer does not cover N rows");
+        for (int k = 0; k < cnum; k++) {
+            SENK_REQUIRE(cptr[k + 1] >= cptr[k], "colour pointer not monotone");
+            gl.push_back({cptr[k] * bs, cptr[k + 1] * bs});
+            for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) {
+                col_l[p] = k;
+                col_u[p] = cnum - 1 - k;
+            }
+        }
+        for (int k = cnum - 1; k >= 0; k--) gu.push_back(gl[k]);
+    }
+    if (!build_factor_wf(L, false, N, lval, lcind, lrptr, gl, bs, col_l, false, s, rml.empty() ? nullptr : &rml))
+        return;
+    if (!build_factor_wf(U, true, N, uval, ucind, urptr, gu, bs, col_u, false, s, rmu.empty() ? nullptr : &rmu))
+        return;
+    int most = 32;
+    for (const SweepFactor<VT> *F : {&L, &U})
+        for (size_t c = 0; c + 1 < F->colour_groups.size(); c++)
+            most = std::max(most, (F->colour_groups[c + 1] - F->colour_groups[c]) * 32);
+    small_threads = std::min(1024, (most + 31) / 32 * 32);
+    switch (bs) {
+    case 1: allow_small<VT, 1>(); break;
+    case 2: allow_small<VT, 2>(); break;
+    case 4: allow_small<VT, 4>(); break;
+    case 8: allow_small<VT, 8>(); break;
+    case 16: allow_small<VT, 16>(); break;
+    case 32: allow_small<VT, 32>(); break;
+    }
+    small = true;
+}
+
 template <typename VT>
 void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval,
                         const int *ucind, const int *urptr, int pckind, const int *cptr, int cnum, int bsize,
                         cudaStream_t s, int sweep_mode)
 {
     SENK_REQUIRE(sweep_mode == SENK_SWEEP_AUTO || sweep_mode == SENK_SWEEP_COLOURS ||
-                     sweep_mode == SENK_SWEEP_DATAFLOW,
+                     sweep_mode == SENK_SWEEP_DATAFLOW || sweep_mode == SENK_SWEEP_COMPACT,
                  "unknown sweep mode");
     SENK_REQUIRE(N > 0, "N must be positive");
     SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
@@ -488,6 +584,14 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
     status.alloc(1);
     SENK_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
     allow_all_smem<VT, VT>();
+    // Small systems, default schedule: both sweeps in one CTA with the vector in
+    // shared memory (one launch per application instead of one per colour or
+    // level set).
+    small = sweep_mode == SENK_SWEEP_AUTO && (size_t)N * sizeof(VT) <= kSmallBytes;
+    if (small) {
+        build_small(N, lval, lcind, lrptr, uval, ucind, urptr, pckind, cptr, cnum, bsize, s);
+        if (small) return;
+    }
     if (pckind == SENK_PC_ILU) {
         std::vector<int> rm;
         std::vector<Group> gr;
@@ -511,11 +615,12 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    // Compact chains, one launch per colour (AUTO) or one dataflow launch per
-    // sweep (DATAFLOW); SENK_SWEEP_COLOURS keeps the row-slot layout with one
-    // CTA per group. A factor whose widest group does not fit shared memory
-    // falls back to row slots.
-    const bool compact = sweep_mode != SENK_SWEEP_COLOURS;
+    // Row slots, one launch per colour (AUTO: measured fastest on the 128^3
+    // system, FP32 application 0.193 ms against 0.224 ms on compact chains;
+    // COLOURS); compact chains, one launch per colour (COMPACT) or one dataflow
+    // launch per sweep (DATAFLOW). A factor whose widest group does not fit
+    // shared memory falls back to row slots.
+    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW;
     const bool df = sweep_mode == SENK_SWEEP_DATAFLOW;
     if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s)))
         build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
@@ -533,6 +638,10 @@ template <typename VT>
 template <typename XT>
 void IluPlan<VT>::sweep(const SweepFactor<VT> &F, const XT *x, XT *y, cudaStream_t s, const int *gate) const
 {
+    if (small) {
+        sweep_small(F.upper ? 2 : 1, (const VT *)x, (VT *)y, s, gate);
+        return;
+    }
     if (F.upper) sweep_groups<VT, XT, true>(F, status.p, x, y, s, gate);
     else sweep_groups<VT, XT, false>(F, status.p, x, y, s, gate);
 }

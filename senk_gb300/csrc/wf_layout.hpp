@@ -75,18 +75,22 @@ struct WfLayout {
 // `max_smem` bytes of shared memory per warp.
 template <typename VT>
 bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const int *cind, const int *rptr,
-                    const std::vector<WfColour> &colours, int bs, const int *colour_of, size_t max_smem)
+                    const std::vector<WfColour> &colours, int bs, const int *colour_of, size_t max_smem,
+                    const int *rowmap = nullptr)
 {
     if (N > kColMask) throw std::invalid_argument("N too large for the compact sweep layout (2^27 rows)");
     if (bs < 1 || bs > 32 || N % bs) throw std::invalid_argument("chain length must divide N and be at most 32");
-    const int nb = N / bs;  // chains; chain b holds rows [b*bs, b*bs + bs)
+    if (rowmap && bs != 1) throw std::invalid_argument("a row map takes chains of one row");
+    const int nb = N / bs;  // chains; chain b holds rows [b*bs, b*bs + bs), or row rowmap[b]
+    auto first_row = [&](int b) { return rowmap ? rowmap[b] : b * bs; };
     std::vector<int> E(nb), I(nb);
     int bad = -1;
 #pragma omp parallel for schedule(static)
     for (int b = 0; b < nb; b++) {
         int ne = 0, ni = 0;
         bool ok = true;
-        const int cs = b * bs, ce = cs + bs;
+        const int cs = first_row(b), ce = cs + bs;
+        if (cs < 0 || cs >= N) ok = false;
         for (int row = cs; row < ce && ok; row++) {
             int j0 = rptr[row];
             const int j1 = rptr[row + 1];
@@ -142,7 +146,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
                     const int b = ch[q0 + q];
                     d.emax = std::max(d.emax, E[b]);
                     d.imax = std::max(d.imax, I[b]);
-                    chv.push_back(make_int2(b * bs, E[b] | (I[b] << 16)));
+                    chv.push_back(make_int2(first_row(b), E[b] | (I[b] << 16)));
                 } else {
                     chv.push_back(make_int2(0, 0));
                 }

@@ -30,14 +30,15 @@ def main(argv=None):
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--reps", type=int, default=50)
-    ap.add_argument("--sweep", default="auto", choices=["auto", "colours", "dataflow"])
+    ap.add_argument("--sweep", default="auto", choices=["auto", "colours", "dataflow", "compact"])
     args = ap.parse_args(argv)
     A = P.convdiff3d(args.n, 0.5)
     nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
     Ar = S.Reordering(A, LP, RP)
     Lf, Uf, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
     dt = np.float32 if args.dtype == "f32" else np.float64
-    sweep = {"auto": L.SWEEP_AUTO, "colours": L.SWEEP_COLOURS, "dataflow": L.SWEEP_DATAFLOW}[args.sweep]
+    sweep = {"auto": L.SWEEP_AUTO, "colours": L.SWEEP_COLOURS, "dataflow": L.SWEEP_DATAFLOW,
+             "compact": L.SWEEP_COMPACT}[args.sweep]
     sy = System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, dtype=dt, m_max=1, sweep=sweep)
     ms, by = sy.time_op(OPS[args.op], args.reps)
     sy.close()

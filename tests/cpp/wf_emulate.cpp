@@ -17,7 +17,7 @@ namespace {
 
 template <typename VT>
 int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, const int *cptr, int cnum, int bs,
-            const VT *x, VT *y, char *err, int errlen)
+            const VT *x, VT *y, char *err, int errlen, const int *rowmap = nullptr)
 {
     auto fail = [&](const std::string &m) {
         std::snprintf(err, errlen, "%s", m.c_str());
@@ -26,13 +26,21 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
     try {
         std::vector<WfColour> colours;
         std::vector<int> colour_of(N);
-        for (int k = 0; k < cnum; k++) {
-            const int c = upper ? cnum - 1 - k : k;
-            colours.push_back({cptr[c] * bs, cptr[c + 1] * bs});
-            for (int p = cptr[c] * bs; p < cptr[c + 1] * bs; p++) colour_of[p] = k;
+        if (rowmap) {  // level sets in processing order: cptr holds their position ranges
+            for (int k = 0; k < cnum; k++) {
+                colours.push_back({cptr[k], cptr[k + 1]});
+                for (int p = cptr[k]; p < cptr[k + 1]; p++) colour_of[rowmap[p]] = k;
+            }
+        } else {
+            for (int k = 0; k < cnum; k++) {
+                const int c = upper ? cnum - 1 - k : k;
+                colours.push_back({cptr[c] * bs, cptr[c + 1] * bs});
+                for (int p = cptr[c] * bs; p < cptr[c + 1] * bs; p++) colour_of[p] = k;
+            }
         }
         WfLayout<VT> L;
-        if (!make_wf_layout(L, upper != 0, N, val, cind, rptr, colours, bs, colour_of.data(), (size_t)1 << 30))
+        if (!make_wf_layout(L, upper != 0, N, val, cind, rptr, colours, bs, colour_of.data(), (size_t)1 << 30,
+                            rowmap))
             return fail("layout does not fit");
         const int ng = (int)L.groups.size();
         const size_t nslots = L.col.size();
@@ -191,6 +199,13 @@ extern "C" int wf_emulate_d(int N, const double *val, const int *cind, const int
                             int cnum, int bs, const double *x, double *y, char *err, int errlen)
 {
     return emulate<double>(N, val, cind, rptr, upper, cptr, cnum, bs, x, y, err, errlen);
+}
+
+extern "C" int wf_emulate_levels_d(int N, const double *val, const int *cind, const int *rptr, int upper,
+                                   const int *levptr, int nlev, const int *rowmap, const double *x, double *y,
+                                   char *err, int errlen)
+{
+    return emulate<double>(N, val, cind, rptr, upper, levptr, nlev, 1, x, y, err, errlen, rowmap);
 }
 
 extern "C" int wf_emulate_s(int N, const float *val, const int *cind, const int *rptr, int upper, const int *cptr,

@@ -167,7 +167,7 @@ class Plan:
 SWEEPS = [("natural", 16), ("amc", 16), ("abmc", 16), ("abmc", 8), ("abmc", 32), ("abmc", 4), ("abmc", 2)]
 
 
-@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS])
+@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT])
 @pytest.mark.parametrize("case", ["poisson128", "convdiff24", "vardiff16"])
 @pytest.mark.parametrize("sched,bsize", SWEEPS)
 def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
@@ -200,7 +200,7 @@ def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
     assert rel(host(x2), want) <= 1e-12
 
 
-@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS])
+@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT])
 @pytest.mark.parametrize("sched,bsize", [("abmc", 16), ("natural", 16), ("amc", 16), ("abmc", 4)])
 def test_ilu_sweeps_f32(torch, port, sched, bsize, sweep):
     A = P.convdiff3d(24, 0.5)
@@ -232,15 +232,15 @@ def test_ilu_sweep_golden(torch, small):
 
 
 def test_ilu_sweep_at_benchmark_size(torch, port):
-    """The dataflow sweeps on the 64^3 convection-diffusion system (65,536
-    chains, 11 colours) against the oracle, FP64 and FP32, several applications
-    in a row."""
+    """The 64^3 convection-diffusion system (16,384 chains, 11 colours) against
+    the oracle under the default, dataflow and compact schedules, FP64 and FP32,
+    several applications in a row."""
     A = P.convdiff3d(64, 0.5)
     Ar, L_, U_, sc, nc, kind, bs = _factors(A, "abmc", 16)
     v = np.random.default_rng(9).uniform(-1, 1, A.n)
     want = port.sptrsv(U_, port.sptrsv(L_, v, False), True)
     for T, tol, sweep in ((np.float64, 1e-12, L.SWEEP_AUTO), (np.float32, 1e-5, L.SWEEP_AUTO),
-                          (np.float64, 1e-12, L.SWEEP_DATAFLOW)):
+                          (np.float64, 1e-12, L.SWEEP_DATAFLOW), (np.float32, 1e-5, L.SWEEP_COMPACT)):
         pl = Plan(L_, U_, kind, sc, nc, bs, T, sweep=sweep)
         L.check("plan", pl.code)
         xd = dev(torch, v.astype(T))

@@ -130,7 +130,7 @@ def test_nonconvergence_reports_outer_times_m(c1):
     assert not r.converged and r.iters == 20 and r.cycles == 2
 
 
-@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_COLOURS, L.SWEEP_DATAFLOW])
+@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_COLOURS, L.SWEEP_DATAFLOW, L.SWEEP_COMPACT])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_c1_abmc_sweep_schedules(port, golden, c1, sweep, dtype):
     """Every schedule of the ABMC sweeps (compact chains per colour, row slots

@@ -27,6 +27,9 @@ def emu(tmp_path_factory):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     lib = C.CDLL(out)
+    lib.wf_emulate_levels_d.restype = C.c_int
+    lib.wf_emulate_levels_d.argtypes = [C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                                        C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
     for name in ("wf_emulate_d", "wf_emulate_s"):
         f = getattr(lib, name)
         f.restype = C.c_int
@@ -77,3 +80,39 @@ def test_emulated_dataflow_sweep_matches_the_oracle(emu, port, kind, n, bs):
     t32 = _run(emu, U32, True, sc, nc, bs, _run(emu, L32, False, sc, nc, bs, v32))
     want32 = port.ilu_apply(L32, U32, v32, dtype=np.float32)
     assert np.max(np.abs(t32 - want32)) <= 1e-5 * np.max(np.abs(want32))
+
+
+def _levels(F, upper):
+    """Level sets of a triangular factor (the natural order's schedule): rows in
+    processing order and the position range of each level."""
+    n = F.n
+    lev = np.zeros(n, np.int64)
+    rng = range(n - 1, -1, -1) if upper else range(n)
+    for i in rng:
+        js = F.cind[F.rptr[i] + (1 if upper else 0):F.rptr[i + 1]]
+        if js.size:
+            lev[i] = lev[js].max() + 1
+    order = np.argsort(lev, kind="stable").astype(np.int32)
+    ptr = np.concatenate([[0], np.cumsum(np.bincount(lev))]).astype(np.int32)
+    return order, ptr
+
+
+@pytest.mark.parametrize("n", [16, 40])
+def test_emulated_level_set_layout_matches_the_oracle(emu, port, n):
+    """The natural order's level sets as chains of one row (row map), as the
+    single-CTA sweep of small systems uses them."""
+    A = P.poisson2d(n)
+    L_, U_, _ = S.Split(S.Ilu0(A), "L-DU", True)
+    v = np.random.default_rng(3).uniform(-1, 1, A.n)
+    out = v
+    for F, upper in ((L_, False), (U_, True)):
+        order, ptr = _levels(F, upper)
+        y = np.zeros(A.n)
+        err = C.create_string_buffer(256)
+        keep = [np.ascontiguousarray(a) for a in (F.val, F.cind, F.rptr, ptr, order, out)]
+        rc = emu.wf_emulate_levels_d(A.n, _p(keep[0]), _p(keep[1]), _p(keep[2]), int(upper), _p(keep[3]),
+                                     len(ptr) - 1, _p(keep[4]), _p(keep[5]), _p(y), err, 256)
+        assert rc == 0, err.value.decode()
+        out = y
+    want = port.sptrsv(U_, port.sptrsv(L_, v, False), True)
+    assert np.max(np.abs(out - want)) <= 1e-14 * np.max(np.abs(want))
