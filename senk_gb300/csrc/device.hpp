@@ -170,6 +170,8 @@ struct SweepFactor {
     std::vector<int> colour_slots; // compact: widest block of each colour
     DevBuf<unsigned char> wcounts; // compact: per chain, external and in-chain counts of each row
     DevBuf<int> dcolour_groups;    // compact: colour_groups on the device (small systems)
+    DevBuf<VT> cdinv;              // compact U: inverted diagonal per chain (small systems)
+    size_t level_bytes = 0;        // compact, chains of one row: most bytes one colour stages
     // compact, per colour: the launches of a sweep in order
     struct Launch {
         int g0, g1;        // groups of the colour
@@ -196,6 +198,7 @@ struct IluPlan {
     // small systems (the vector fits in shared memory): both sweeps in one CTA
     bool small = false;
     int small_threads = 0;
+    size_t small_buf = 0;          // bytes of each of the two staging buffers
     void sweep_small(int which, const VT *x, VT *y, cudaStream_t s, const int *gate) const;
     void build_small(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
                      const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s);

@@ -816,74 +816,127 @@ k_sweep(const GroupDesc *__restrict__ groups, int g_begin, const unsigned char *
 }
 
 // ------------------------------------------------- small systems, one CTA
-// One triangular factor in the compact chain layout, for k_ilu_small.
+// One triangular factor in the compact chain layout, chains of one row (level
+// sets of the natural order, or AMC colours), for k_ilu_small.
 template <typename VT>
 struct SmallFactor {
     const WfGroup *groups;
     const int2 *chains;
     const VT *val;
     const int *col;
-    const VT *dinv;         // U: inverted diagonal per row
+    const VT *cdinv;        // U: inverted diagonal per chain
     const int *cgroups;     // group range of each colour (level set), processing order
     int ncolours;
 };
 
-// Sweeps one factor inside k_ilu_small: colour by colour, one thread per chain
-// (its rows in solve order, each row's external then in-chain entries in the
-// reference's order), the vector in shared memory; a barrier between colours.
-template <typename VT, typename XT, int BS, bool UPPER>
-__device__ __forceinline__ void small_sweep(const SmallFactor<VT> &F, XT *ysh)
+// Stages the data of one level (colour) into buf with bulk copies counted on
+// bar: group descriptors, chain descriptors, the groups' blocks (columns, then
+// values) and, for U, the chains' inverted diagonals. One thread. Returns the
+// bytes expected.
+template <typename VT>
+__device__ __forceinline__ void small_stage(const SmallFactor<VT> &F, bool upper, int c, unsigned char *buf,
+                                            unsigned long long *bar)
 {
-    for (int c = 0; c < F.ncolours; c++) {
-        const int g0 = __ldg(F.cgroups + c), g1 = __ldg(F.cgroups + c + 1);
-        for (int t = threadIdx.x; t < (g1 - g0) * 32; t += blockDim.x) {
-            const int g = g0 + (t >> 5), lane = t & 31;
-            const WfGroup d = F.groups[g];
-            if (lane >= d.nchains) continue;
-            const int2 ch = __ldg(F.chains + (size_t)g * 32 + lane);
-            const int r0 = ch.x, E = ch.y & 0xffff, I = (int)((unsigned)ch.y >> 16);
-            const int *ew = F.col + d.off + lane;
-            const VT *ev = F.val + d.off + lane;
-            const int *iw = ew + d.emax * 32;
-            const VT *iv = ev + d.emax * 32;
-            int e = 0, k = 0;
-            int we = e < E ? __ldg(ew) : 0;
-            int wi = k < I ? __ldg(iw) : 0;
-#pragma unroll
-            for (int s = 0; s < BS; s++) {
-                const int r = UPPER ? BS - 1 - s : s;
-                XT tt = ysh[r0 + r];
-                while (e < E && (int)((unsigned)we >> kColBits) == r) {
-                    tt -= (XT)__ldg(ev + e * 32) * ysh[we & kColMask];
-                    e++;
-                    if (e < E) we = __ldg(ew + e * 32);
-                }
-                while (k < I && (wi >> 8) == r) {
-                    tt -= (XT)__ldg(iv + k * 32) * ysh[r0 + (wi & 255)];
-                    k++;
-                    if (k < I) wi = __ldg(iw + k * 32);
-                }
-                if (UPPER) tt *= (XT)__ldg(F.dinv + r0 + r);
-                ysh[r0 + r] = tt;
-            }
-        }
-        __syncthreads();
+    const int g0 = __ldg(F.cgroups + c), g1 = __ldg(F.cgroups + c + 1), G = g1 - g0;
+    unsigned bytes = 0;
+    int e0 = 0, ne = 0;
+    if (G > 0) {
+        const WfGroup first = F.groups[g0], last = F.groups[g1 - 1];
+        e0 = first.off;
+        ne = last.off + (last.emax + last.imax) * 32 - e0;
+        bytes = (unsigned)G * 16u + (unsigned)G * 256u + (unsigned)ne * (4u + (unsigned)sizeof(VT)) +
+                (upper ? (unsigned)G * 32u * (unsigned)sizeof(VT) : 0u);
     }
+    // earlier generic accesses to this buffer come before the async writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, bytes);
+    if (G == 0) return;
+    unsigned char *p = buf;
+    bulk_g2s(p, F.groups + g0, (unsigned)G * 16u, bar);
+    p += G * 16;
+    bulk_g2s(p, F.chains + (size_t)g0 * 32, (unsigned)G * 256u, bar);
+    p += G * 256;
+    if (ne > 0) {
+        bulk_g2s(p, F.col + e0, (unsigned)ne * 4u, bar);
+        p += (size_t)ne * 4;
+        bulk_g2s(p, F.val + e0, (unsigned)ne * (unsigned)sizeof(VT), bar);
+        p += (size_t)ne * sizeof(VT);
+    }
+    if (upper) bulk_g2s(p, F.cdinv + (size_t)g0 * 32, (unsigned)G * 32u * (unsigned)sizeof(VT), bar);
 }
 
 // Both triangular sweeps of one ILU application y = U^-1 L^-1 x for a system
-// whose vector fits in shared memory: one CTA, no other launch; x == y allowed.
-template <typename VT, typename XT, int BS>
+// whose vector fits in shared memory, in one CTA (which: bit 0 L, bit 1 U;
+// x == y allowed). The levels (colours) run in order with a barrier between
+// them, one thread per row; each level's data is staged by TMA into one of two
+// buffers while the level before it is solved. A TMA wait that runs out sets
+// *status = 2 and the kernel leaves after waiting once more.
+template <typename VT, typename XT>
 __global__ void __launch_bounds__(1024)
-k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *y, int n, const int *gate)
+k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *y, int n, const int *gate,
+            int *status, int buf_bytes)
 {
-    extern __shared__ __align__(16) unsigned char sms[];
-    XT *ysh = reinterpret_cast<XT *>(sms);
+    extern __shared__ __align__(128) unsigned char sms[];
+    __shared__ __align__(8) unsigned long long bar[2];
     if (gated(gate)) return;
+    XT *ysh = reinterpret_cast<XT *>(sms);
+    unsigned char *bufs = sms + ((size_t)n * sizeof(XT) + 127) / 128 * 128;
+    const int nl = (which & 1) ? Lf.ncolours : 0, nu = (which & 2) ? Uf.ncolours : 0, steps = nl + nu;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        if (steps > 0) {
+            if (nl) small_stage(Lf, false, 0, bufs, &bar[0]);
+            else small_stage(Uf, true, 0, bufs, &bar[0]);
+        }
+    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) ysh[i] = x[i];
     __syncthreads();
-    if (which & 1) small_sweep<VT, XT, BS, false>(Lf, ysh);
-    if (which & 2) small_sweep<VT, XT, BS, true>(Uf, ysh);
+    for (int k = 0; k < steps; k++) {
+        const int b = k & 1;
+        if (threadIdx.x == 0 && k + 1 < steps) {
+            const int k1 = k + 1;
+            unsigned char *nb = bufs + (size_t)(b ^ 1) * buf_bytes;
+            if (k1 < nl) small_stage(Lf, false, k1, nb, &bar[b ^ 1]);
+            else small_stage(Uf, true, k1 - nl, nb, &bar[b ^ 1]);
+        }
+        const bool upper = k >= nl;
+        const SmallFactor<VT> &F = upper ? Uf : Lf;
+        const int c = upper ? k - nl : k;
+        const bool ok = mbar_wait_bounded(&bar[b], (unsigned)(k >> 1) & 1u, kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicExch(status, 2);
+                // copies still in flight: this step's and the next one's
+                if (!ok) mbar_wait_bounded(&bar[b], (unsigned)(k >> 1) & 1u, kWaitLimit);
+                if (k + 1 < steps) mbar_wait_bounded(&bar[b ^ 1], (unsigned)((k + 1) >> 1) & 1u, kWaitLimit);
+            }
+            return;
+        }
+        const int G = __ldg(F.cgroups + c + 1) - __ldg(F.cgroups + c);
+        const unsigned char *sb = bufs + (size_t)b * buf_bytes;
+        const WfGroup *sd = reinterpret_cast<const WfGroup *>(sb);
+        const int2 *sc = reinterpret_cast<const int2 *>(sb + G * 16);
+        const int e0 = G > 0 ? sd[0].off : 0;
+        const WfGroup last = G > 0 ? sd[G - 1] : WfGroup{0, 0, 0, 0};
+        const int ne = last.off + (last.emax + last.imax) * 32 - e0;
+        const int *scol = reinterpret_cast<const int *>(sb + G * 16 + G * 256);
+        const VT *sval = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * 4);
+        const VT *sdinv = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * (4 + sizeof(VT)));
+        for (int t = threadIdx.x; t < G * 32; t += blockDim.x) {
+            const int gi = t >> 5, lane = t & 31;
+            const WfGroup d = sd[gi];
+            if (lane >= d.nchains) continue;
+            const int2 ch = sc[t];
+            const int row = ch.x, E = ch.y & 0xffff;
+            const int base = d.off - e0 + lane;
+            XT tt = ysh[row];
+            for (int e = 0; e < E; e++) tt -= (XT)sval[base + e * 32] * ysh[scol[base + e * 32] & kColMask];
+            if (upper) tt *= (XT)sdinv[t];
+            ysh[row] = tt;
+        }
+        __syncthreads();
+    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = ysh[i];
 }
 
@@ -977,17 +1030,25 @@ __device__ __forceinline__ void wf_solve_group(const WfGroup &d, int E, int I, c
         }
     }
     if (cur >= 0) tsh[cur * 32 + lane] = t;
-    const int *iw = cw + d.emax * 32;
-    const VT *iv = vw + d.emax * 32;
+    // this chain's in-chain entries follow those of the lanes before it
+    int ibase = I;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, ibase, o);
+        if (lane >= o) ibase += v;
+    }
+    ibase -= I;
+    const int *iw = cw + d.emax * 32 + ibase;
+    const VT *iv = vw + d.emax * 32 + ibase;
     int e = 0;
 #pragma unroll
     for (int s = 0; s < BS; s++) {
         const int r = UPPER ? BS - 1 - s : s;
         XT tt = tsh[r * 32 + lane];
         while (e < I) {
-            const int w = iw[e * 32 + lane];
+            const int w = iw[e];
             if ((w >> 8) != r) break;
-            tt -= (XT)iv[e * 32 + lane] * tsh[(w & 255) * 32 + lane];
+            tt -= (XT)iv[e] * tsh[(w & 255) * 32 + lane];
             e++;
         }
         if (UPPER) tt *= dsh[r * 32 + lane];
@@ -1119,8 +1180,12 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 {
     extern __shared__ __align__(128) unsigned char ccs[];
     __shared__ __align__(8) unsigned long long bar;
-    __shared__ XT tsh[BS][32];
-    __shared__ XT dsh[UPPER ? BS : 1][32];
+    // rows of chain q at tsh[q][r]: stride BS + 1 is odd, so both the
+    // row-per-warp accesses (lane = chain) and the row-per-lane ones (16 lanes
+    // of one chain) fall in different banks
+    __shared__ XT tsh[32][BS + 1];
+    __shared__ XT dsh[UPPER ? 32 : 1][BS + 1];
+    __shared__ int ibase[32];
     const int g = g0 + blockIdx.x;
     const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
     const WfGroup d = groups[g];
@@ -1143,7 +1208,17 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
     const bool live = q < d.nchains;
     const int2 ch = live ? __ldg(chains + (size_t)g * 32 + q) : make_int2(0, 0);
     const int row = ch.x + l;
-    if (UPPER) dsh[l][q] = live ? (XT)__ldg(dinv + row) : XT(0);
+    if (UPPER) dsh[q][l] = live ? (XT)__ldg(dinv + row) : XT(0);
+    if (l == 0) {  // where each chain's in-chain entries start in the block
+        const int I = (int)((unsigned)ch.y >> 16);
+        int v = I;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (q >= o) v += u;
+        }
+        ibase[q] = v - I;
+    }
     XT t = XT(0);
     if (early_x && live) t = x[row];
     if (!early_x) pdl_launch_dependents();
@@ -1160,17 +1235,35 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         if (!early_x && live) t = x[row];
         // row l's external entries; in lane q's stream rows come in solve order
         const unsigned char *cq = cnt + q * 2 * BS;
-        int eo = 0;
+        int eo = 0, ne = 0;
+        if constexpr (BS >= 8) {
+            // the chain's counts as 16-byte words (2 BS bytes per chain, 16-byte aligned)
+            const uint4 *c4 = reinterpret_cast<const uint4 *>(cq);
 #pragma unroll
-        for (int r = 0; r < BS; r++)
-            if (UPPER ? r > l : r < l) eo += cq[r];
-        const int ne = cq[l];
+            for (int w = 0; w < (BS + 15) / 16; w++) {
+                const uint4 v = c4[w];
+                const unsigned words[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int b = 0; b < 16; b++) {
+                    const int r = w * 16 + b;
+                    if (r >= BS) break;
+                    const int c = (int)((words[b >> 2] >> (8 * (b & 3))) & 255u);
+                    if (r == l) ne = c;
+                    if (UPPER ? r > l : r < l) eo += c;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+                if (UPPER ? r > l : r < l) eo += cq[r];
+            ne = cq[l];
+        }
 #pragma unroll 4
         for (int k = 0; k < ne; k++) {
             const int at = (eo + k) * 32 + q;
             t -= (XT)vw[at] * __ldg(y + (cw[at] & kColMask));
         }
-        tsh[l][q] = t;
+        tsh[q][l] = t;
         __syncthreads();
         // In-chain recurrence, BS lanes per chain (lane = row), 32 / BS chains
         // per warp, all warps busy: the rows are finished in solve order; the
@@ -1183,21 +1276,21 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
             constexpr int CPW = 32 / BS;  // chains per warp
             const int lane = threadIdx.x & 31;
             const int qc = l * CPW + lane / BS, rr = lane % BS;
-            const int *iw = cw + d.emax * 32;
-            const VT *iv = vw + d.emax * 32;
+            const int *iw = cw + d.emax * 32 + ibase[qc];
+            const VT *iv = vw + d.emax * 32 + ibase[qc];
             const unsigned char *cc = cnt + qc * 2 * BS;
             int io = 0;
 #pragma unroll
             for (int r = 0; r < BS; r++)
                 if (UPPER ? r > rr : r < rr) io += cc[BS + r];
             int left = cc[BS + rr];
-            XT tt = tsh[rr][qc];
-            const XT di = UPPER ? dsh[rr][qc] : XT(1);
+            XT tt = tsh[qc][rr];
+            const XT di = UPPER ? dsh[qc][rr] : XT(1);
             int c0 = -1, c1 = -1;
             XT v0 = XT(0), v1 = XT(0);
             int at = io;
-            if (left > 0) { c0 = iw[at * 32 + qc] & 255; v0 = (XT)iv[at * 32 + qc]; at++; }
-            if (left > 1) { c1 = iw[at * 32 + qc] & 255; v1 = (XT)iv[at * 32 + qc]; at++; }
+            if (left > 0) { c0 = iw[at] & 255; v0 = (XT)iv[at]; at++; }
+            if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
 #pragma unroll
             for (int s = 0; s < BS; s++) {
                 const int c = UPPER ? BS - 1 - s : s;
@@ -1209,13 +1302,13 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
                     c0 = c1;
                     v0 = v1;
                     c1 = -1;
-                    if (left > 1) { c1 = iw[at * 32 + qc] & 255; v1 = (XT)iv[at * 32 + qc]; at++; }
+                    if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
                 }
             }
-            tsh[rr][qc] = tt;
+            tsh[qc][rr] = tt;
         }
         __syncthreads();
-        if (live) y[row] = tsh[l][q];
+        if (live) y[row] = tsh[q][l];
     }
 }
 

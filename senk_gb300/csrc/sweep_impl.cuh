@@ -190,15 +190,11 @@ constexpr size_t kMaxStagedBytes = 160 * 1024;
 // Largest dynamic shared memory of one dataflow CTA.
 constexpr size_t kMaxWfSmem = 200 * 1024;
 
-// Largest vector the single-CTA sweeps of small systems keep in shared memory.
+// Largest vector the single-CTA sweeps of small systems keep in shared memory,
+// and the most dynamic shared memory of that kernel (vector + two staging
+// buffers).
 constexpr size_t kSmallBytes = 192 * 1024;
-
-template <typename VT, int BS>
-void allow_small()
-{
-    SENK_CUDA(cudaFuncSetAttribute(k_ilu_small<VT, VT, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kSmallBytes));
-}
+constexpr size_t kSmallSmem = 220 * 1024;
 
 // Compact chain layout (wf_layout.hpp) uploaded for k_sweep_wf. Returns false
 // (and builds nothing) when a group's block would not fit one warp's shared
@@ -244,6 +240,20 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.wcounts.upload(lay.counts.data(), lay.counts.size(), s);
     F.dcolour_groups.alloc(lay.colour_groups.size());
     F.dcolour_groups.upload(lay.colour_groups.data(), lay.colour_groups.size(), s);
+    if (upper) {
+        F.cdinv.alloc(std::max<size_t>(lay.cdinv.size(), 1));
+        F.cdinv.upload(lay.cdinv.data(), lay.cdinv.size(), s);
+    }
+    F.level_bytes = 0;
+    for (size_t c = 0; c + 1 < lay.colour_groups.size(); c++) {
+        const int G = lay.colour_groups[c + 1] - lay.colour_groups[c];
+        long long ne = 0;
+        for (int g = lay.colour_groups[c]; g < lay.colour_groups[c + 1]; g++)
+            ne += (long long)(lay.groups[g].emax + lay.groups[g].imax) * 32;
+        const size_t b = (size_t)G * 16 + (size_t)G * 256 + (size_t)ne * (4 + sizeof(VT)) +
+                         (upper ? (size_t)G * 32 * bs * sizeof(VT) : 0);
+        F.level_bytes = std::max(F.level_bytes, b);
+    }
     if (!dataflow) {
         // one launch per colour; x is read early from the second colour on
         const int nc = (int)lay.colour_groups.size() - 1;
@@ -486,31 +496,17 @@ void allow_all_smem()
 
 }  // namespace
 
-template <typename VT, int BS>
-void launch_small(const IluPlan<VT> &P, int which, const VT *x, VT *y, cudaStream_t s, const int *gate)
-{
-    auto mk = [](const SweepFactor<VT> &F) {
-        return SmallFactor<VT>{(const WfGroup *)F.wgroups.p, (const int2 *)F.wchains.p, (const VT *)F.val.p,
-                               (const int *)F.col.p, (const VT *)F.dinv.p, (const int *)F.dcolour_groups.p,
-                               (int)F.colour_groups.size() - 1};
-    };
-    k_ilu_small<VT, VT, BS><<<1, P.small_threads, (size_t)P.n * sizeof(VT), s>>>(mk(P.L), mk(P.U), which, x, y, P.n,
-                                                                                 gate);
-    SENK_LAUNCH_CHECK();
-}
-
 template <typename VT>
 void IluPlan<VT>::sweep_small(int which, const VT *x, VT *y, cudaStream_t s, const int *gate) const
 {
-    switch (L.bs) {
-    case 1: launch_small<VT, 1>(*this, which, x, y, s, gate); break;
-    case 2: launch_small<VT, 2>(*this, which, x, y, s, gate); break;
-    case 4: launch_small<VT, 4>(*this, which, x, y, s, gate); break;
-    case 8: launch_small<VT, 8>(*this, which, x, y, s, gate); break;
-    case 16: launch_small<VT, 16>(*this, which, x, y, s, gate); break;
-    case 32: launch_small<VT, 32>(*this, which, x, y, s, gate); break;
-    default: throw ArgError("unsupported chain length");
-    }
+    auto mk = [](const SweepFactor<VT> &F) {
+        return SmallFactor<VT>{(const WfGroup *)F.wgroups.p, (const int2 *)F.wchains.p, (const VT *)F.val.p,
+                               (const int *)F.col.p, (const VT *)F.cdinv.p, (const int *)F.dcolour_groups.p,
+                               (int)F.colour_groups.size() - 1};
+    };
+    const size_t smem = ((size_t)n * sizeof(VT) + 127) / 128 * 128 + 2 * small_buf;
+    k_ilu_small<VT, VT><<<1, small_threads, smem, s>>>(mk(L), mk(U), which, x, y, n, gate, status.p, (int)small_buf);
+    SENK_LAUNCH_CHECK();
 }
 
 // Compact layouts of both factors for k_ilu_small (natural order: level sets,
@@ -533,10 +529,7 @@ void IluPlan<VT>::build_small(int N, const VT *lval, const int *lcind, const int
         for (size_t k = 0; k < gu.size(); k++)
             for (int p = gu[k].p0; p < gu[k].p1; p++) col_u[rmu[p]] = (int)k;
     } else {
-        SENK_REQUIRE(pckind == SENK_PC_ILU_AMC || pckind == SENK_PC_ILU_ABMC, "unknown preconditioner kind");
-        bs = pckind == SENK_PC_ILU_AMC ? 1 : bsize;
-        SENK_REQUIRE(bs == 1 || bs == 2 || bs == 4 || bs == 8 || bs == 16 || bs == 32,
-                     "ABMC block size must be 1, 2, 4, 8, 16 or 32 on the GPU path (got " + std::to_string(bs) + ")");
+        if (pckind != SENK_PC_ILU_AMC) return;  // chains of several rows: the per-colour launches
         SENK_REQUIRE(cptr && cnum > 0, "colour pointer missing");
         SENK_REQUIRE(cptr[0] == 0 && (long long)cptr[cnum] * bs == N, "colour pointer does not cover N rows");
         for (int k = 0; k < cnum; k++) {
@@ -558,14 +551,10 @@ void IluPlan<VT>::build_small(int N, const VT *lval, const int *lcind, const int
         for (size_t c = 0; c + 1 < F->colour_groups.size(); c++)
             most = std::max(most, (F->colour_groups[c + 1] - F->colour_groups[c]) * 32);
     small_threads = std::min(1024, (most + 31) / 32 * 32);
-    switch (bs) {
-    case 1: allow_small<VT, 1>(); break;
-    case 2: allow_small<VT, 2>(); break;
-    case 4: allow_small<VT, 4>(); break;
-    case 8: allow_small<VT, 8>(); break;
-    case 16: allow_small<VT, 16>(); break;
-    case 32: allow_small<VT, 32>(); break;
-    }
+    small_buf = (std::max(L.level_bytes, U.level_bytes) + 127) / 128 * 128;
+    const size_t smem = ((size_t)N * sizeof(VT) + 127) / 128 * 128 + 2 * small_buf;
+    if (smem > kSmallSmem) return;  // a level too large to stage next to the vector
+    SENK_CUDA(cudaFuncSetAttribute(k_ilu_small<VT, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     small = true;
 }
 

@@ -7,8 +7,11 @@
 // each colour are sorted by their entry counts (external first, then in-chain,
 // both descending) and taken 32 at a time into groups, lane q = chain q. Group
 // block at `off`: external entry k of lane q at off + k*32 + q for
-// k < E_q <= emax, then in-chain entry k at off + (emax + k)*32 + q for
-// k < I_q <= imax. Both parts list rows in solve order (ascending for L,
+// k < E_q <= emax (slot-major, so a warp taking one entry of every chain
+// reads 32 consecutive words); then the in-chain entries chain after chain,
+// entry k of lane q at off + emax*32 + ibase_q + k with ibase_q the sum of
+// I over the lanes before q (a chain's rows, handled by consecutive lanes,
+// read consecutive words). Both parts list rows in solve order (ascending for L,
 // descending for U) and each row's entries in the reference's subtraction
 // order (include/senk_sparse.hpp:132-167: ascending columns for L, descending
 // for U, the U diagonal kept apart as dinv). Column words: external
@@ -62,6 +65,7 @@ struct WfLayout {
     std::vector<VT> val;          // block values
     std::vector<int> col;         // block column words
     std::vector<VT> dinv;         // U: inverted diagonal per row
+    std::vector<VT> cdinv;        // U: the same per chain, chain after chain (32 x bs per group)
     std::vector<int> dep_ptr, dep_idx;  // groups each group reads from (all earlier)
     std::vector<int> colour_groups;     // group range of each colour (size colours + 1)
     std::vector<int> colour_slots;      // widest block of each colour
@@ -169,6 +173,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
     out.val.assign((size_t)off, VT(0));
     out.col.assign((size_t)off, 0);
     out.counts.assign((size_t)ng * 32 * 2 * bs, 0);
+    out.cdinv.assign(upper ? (size_t)ng * 32 * bs : 0, VT(0));
     out.dinv.assign(upper ? N : 0, VT(0));
     std::vector<int> owner(N, -1);  // group of each row
     long long stored = 0;
@@ -178,6 +183,8 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
         for (int q = 0; q < d.nchains; q++) {
             const int r0 = chv[(size_t)g * 32 + q].x;
             int ke = 0, ki = 0;
+            int ibase = 0;
+            for (int q2 = 0; q2 < q; q2++) ibase += (int)((unsigned)chv[(size_t)g * 32 + q2].y >> 16);
             for (int st = 0; st < bs; st++) {
                 const int l = upper ? bs - 1 - st : st;  // rows in solve order
                 const int row = r0 + l;
@@ -187,7 +194,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
                     const int c = cind[j];
                     if (c >= r0 && c < r0 + bs) {
                         cnt[bs + l]++;
-                        const long long at = d.off + (long long)(d.emax + ki++) * 32 + q;
+                        const long long at = d.off + (long long)d.emax * 32 + ibase + ki++;
                         out.col[at] = (l << 8) | (c - r0);
                         out.val[at] = val[j];
                     } else {
@@ -200,6 +207,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
                 };
                 if (upper) {
                     out.dinv[row] = val[rptr[row]];
+                    out.cdinv[((size_t)g * 32 + q) * bs + l] = val[rptr[row]];
                     for (int j = rptr[row + 1] - 1; j >= rptr[row] + 1; j--) put(j);
                 } else {
                     for (int j = rptr[row]; j < rptr[row + 1]; j++) put(j);

@@ -121,22 +121,25 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                     t -= vw[at] * yy[c];
                 }
                 if (cur >= 0) tsh[cur] = t;
+                // in-chain entries of this lane start after those of the lanes before it
+                int ibase = 0;
+                for (int q2 = 0; q2 < lane; q2++) ibase += (int)((unsigned)L.chains[(size_t)g * 32 + q2].y >> 16);
                 std::vector<VT> tsh_par(tsh);
                 if (par_check) {
                     // lane rr keeps its next two in-chain entries; step s finishes
                     // column c and every lane whose next entry is c uses it
                     std::vector<int> left(bs), at(bs), c0(bs, -1), c1(bs, -1);
                     std::vector<VT> v0(bs, 0), v1(bs, 0);
-                    const int *iw = cw + (size_t)d.emax * 32;
-                    const VT *iv = vw + (size_t)d.emax * 32;
+                    const int *iw = cw + (size_t)d.emax * 32 + ibase;
+                    const VT *iv = vw + (size_t)d.emax * 32 + ibase;
                     for (int rr = 0; rr < bs; rr++) {
                         int io = 0;
                         for (int r = 0; r < bs; r++)
                             if (upper ? r > rr : r < rr) io += cq[bs + r];
                         left[rr] = cq[bs + rr];
                         at[rr] = io;
-                        if (left[rr] > 0) { c0[rr] = iw[(size_t)at[rr] * 32 + lane] & 255; v0[rr] = iv[(size_t)at[rr] * 32 + lane]; at[rr]++; }
-                        if (left[rr] > 1) { c1[rr] = iw[(size_t)at[rr] * 32 + lane] & 255; v1[rr] = iv[(size_t)at[rr] * 32 + lane]; at[rr]++; }
+                        if (left[rr] > 0) { c0[rr] = iw[at[rr]] & 255; v0[rr] = iv[at[rr]]; at[rr]++; }
+                        if (left[rr] > 1) { c1[rr] = iw[at[rr]] & 255; v1[rr] = iv[at[rr]]; at[rr]++; }
                     }
                     for (int s = 0; s < bs; s++) {
                         const int c = upper ? bs - 1 - s : s;
@@ -150,9 +153,9 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                             v0[rr] = v1[rr];
                             c1[rr] = -1;
                             if (left[rr] > 1) {
-                                if ((size_t)at[rr] >= (size_t)d.imax) return fail("in-chain window beyond the block");
-                                c1[rr] = iw[(size_t)at[rr] * 32 + lane] & 255;
-                                v1[rr] = iv[(size_t)at[rr] * 32 + lane];
+                                if (at[rr] >= I) return fail("in-chain window beyond the chain's entries");
+                                c1[rr] = iw[at[rr]] & 255;
+                                v1[rr] = iv[at[rr]];
                                 at[rr]++;
                             }
                         }
@@ -165,7 +168,7 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
                     const int r = upper ? bs - 1 - s : s;
                     VT tt = tsh[r];
                     while (e < I) {
-                        const size_t at = (size_t)(d.emax + e) * 32 + lane;
+                        const size_t at = (size_t)d.emax * 32 + ibase + e;
                         if (at >= (size_t)slots * 32) return fail("in-chain slot out of block");
                         const int w = cw[at];
                         if ((w >> 8) != r) break;
