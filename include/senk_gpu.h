@@ -74,9 +74,11 @@ typedef struct {
 /* How the ILU sweeps are scheduled. Chains (ABMC blocks; single rows for AMC
  * and the natural order's level sets) are taken 32 to a group from one colour
  * (level set). */
-#define SENK_SWEEP_AUTO 0     /* the fastest as measured: systems whose vector fits
-                                 in shared memory (up to 192 KB) sweep both factors
-                                 in one CTA; larger ones take SENK_SWEEP_COLOURS */
+#define SENK_SWEEP_AUTO 0     /* the fastest as measured: natural-order or AMC
+                                 systems whose vector fits in shared memory (up to
+                                 192 KB) sweep both factors in one CTA; otherwise
+                                 FP32 factors take SENK_SWEEP_COMPACT and FP64
+                                 factors SENK_SWEEP_COLOURS */
 #define SENK_SWEEP_COLOURS 1  /* row-slot layout, one launch per colour (level set),
                                  one CTA per group */
 #define SENK_SWEEP_DATAFLOW 2 /* compact chain layout, one launch per sweep: each

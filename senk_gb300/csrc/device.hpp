@@ -198,7 +198,8 @@ struct IluPlan {
     // small systems (the vector fits in shared memory): both sweeps in one CTA
     bool small = false;
     int small_threads = 0;
-    size_t small_buf = 0;          // bytes of each of the two staging buffers
+    size_t small_buf = 0;          // bytes of each staging buffer
+    int small_nbuf = 2;            // staging buffers (levels staged ahead + 1)
     void sweep_small(int which, const VT *x, VT *y, cudaStream_t s, const int *gate) const;
     void build_small(int N, const VT *lval, const int *lcind, const int *lrptr, const VT *uval, const int *ucind,
                      const int *urptr, int precond, const int *cptr, int cnum, int bsize, cudaStream_t s);

@@ -868,48 +868,50 @@ __device__ __forceinline__ void small_stage(const SmallFactor<VT> &F, bool upper
 // Both triangular sweeps of one ILU application y = U^-1 L^-1 x for a system
 // whose vector fits in shared memory, in one CTA (which: bit 0 L, bit 1 U;
 // x == y allowed). The levels (colours) run in order with a barrier between
-// them, one thread per row; each level's data is staged by TMA into one of two
-// buffers while the level before it is solved. A TMA wait that runs out sets
-// *status = 2 and the kernel leaves after waiting once more.
+// them, one thread per row; each level's data is staged by TMA into one of
+// nbuf buffers (2 to 8), nbuf - 1 levels ahead of the level being solved. A
+// TMA wait that runs out sets *status = 2 and the kernel leaves after waiting
+// once more for every copy it has issued.
+constexpr int kSmallMaxBufs = 8;
+
 template <typename VT, typename XT>
 __global__ void __launch_bounds__(1024)
 k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *y, int n, const int *gate,
-            int *status, int buf_bytes)
+            int *status, int buf_bytes, int nbuf)
 {
     extern __shared__ __align__(128) unsigned char sms[];
-    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ __align__(8) unsigned long long bar[kSmallMaxBufs];
     if (gated(gate)) return;
     XT *ysh = reinterpret_cast<XT *>(sms);
     unsigned char *bufs = sms + ((size_t)n * sizeof(XT) + 127) / 128 * 128;
     const int nl = (which & 1) ? Lf.ncolours : 0, nu = (which & 2) ? Uf.ncolours : 0, steps = nl + nu;
+    // step j uses buffer j % nbuf, its (j / nbuf)-th use: phase parity (j / nbuf) & 1
+    auto stage = [&](int j) {
+        unsigned char *buf = bufs + (size_t)(j % nbuf) * buf_bytes;
+        if (j < nl) small_stage(Lf, false, j, buf, &bar[j % nbuf]);
+        else small_stage(Uf, true, j - nl, buf, &bar[j % nbuf]);
+    };
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        if (steps > 0) {
-            if (nl) small_stage(Lf, false, 0, bufs, &bar[0]);
-            else small_stage(Uf, true, 0, bufs, &bar[0]);
-        }
+        for (int b = 0; b < nbuf; b++) mbar_init(&bar[b], 1);
+        for (int j = 0; j < nbuf - 1 && j < steps; j++) stage(j);
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) ysh[i] = x[i];
     __syncthreads();
     for (int k = 0; k < steps; k++) {
-        const int b = k & 1;
-        if (threadIdx.x == 0 && k + 1 < steps) {
-            const int k1 = k + 1;
-            unsigned char *nb = bufs + (size_t)(b ^ 1) * buf_bytes;
-            if (k1 < nl) small_stage(Lf, false, k1, nb, &bar[b ^ 1]);
-            else small_stage(Uf, true, k1 - nl, nb, &bar[b ^ 1]);
-        }
+        const int b = k % nbuf;
+        // the buffer of step k - 1 is free again (the barrier at its end)
+        if (threadIdx.x == 0 && k + nbuf - 1 < steps) stage(k + nbuf - 1);
         const bool upper = k >= nl;
         const SmallFactor<VT> &F = upper ? Uf : Lf;
         const int c = upper ? k - nl : k;
-        const bool ok = mbar_wait_bounded(&bar[b], (unsigned)(k >> 1) & 1u, kWaitLimit);
+        const unsigned par = (unsigned)(k / nbuf) & 1u;
+        const bool ok = mbar_wait_bounded(&bar[b], par, kWaitLimit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
                 atomicExch(status, 2);
-                // copies still in flight: this step's and the next one's
-                if (!ok) mbar_wait_bounded(&bar[b], (unsigned)(k >> 1) & 1u, kWaitLimit);
-                if (k + 1 < steps) mbar_wait_bounded(&bar[b ^ 1], (unsigned)((k + 1) >> 1) & 1u, kWaitLimit);
+                // every copy still in flight: steps k .. k + nbuf - 1
+                for (int j = k; j < steps && j < k + nbuf; j++)
+                    mbar_wait_bounded(&bar[j % nbuf], (unsigned)(j / nbuf) & 1u, kWaitLimit);
             }
             return;
         }

@@ -504,8 +504,9 @@ void IluPlan<VT>::sweep_small(int which, const VT *x, VT *y, cudaStream_t s, con
                                (const int *)F.col.p, (const VT *)F.cdinv.p, (const int *)F.dcolour_groups.p,
                                (int)F.colour_groups.size() - 1};
     };
-    const size_t smem = ((size_t)n * sizeof(VT) + 127) / 128 * 128 + 2 * small_buf;
-    k_ilu_small<VT, VT><<<1, small_threads, smem, s>>>(mk(L), mk(U), which, x, y, n, gate, status.p, (int)small_buf);
+    const size_t smem = ((size_t)n * sizeof(VT) + 127) / 128 * 128 + (size_t)small_nbuf * small_buf;
+    k_ilu_small<VT, VT><<<1, small_threads, smem, s>>>(mk(L), mk(U), which, x, y, n, gate, status.p, (int)small_buf,
+                                                       small_nbuf);
     SENK_LAUNCH_CHECK();
 }
 
@@ -552,8 +553,10 @@ void IluPlan<VT>::build_small(int N, const VT *lval, const int *lcind, const int
             most = std::max(most, (F->colour_groups[c + 1] - F->colour_groups[c]) * 32);
     small_threads = std::min(1024, (most + 31) / 32 * 32);
     small_buf = (std::max(L.level_bytes, U.level_bytes) + 127) / 128 * 128;
-    const size_t smem = ((size_t)N * sizeof(VT) + 127) / 128 * 128 + 2 * small_buf;
-    if (smem > kSmallSmem) return;  // a level too large to stage next to the vector
+    const size_t vec = ((size_t)N * sizeof(VT) + 127) / 128 * 128;
+    if (vec + 2 * small_buf > kSmallSmem) return;  // a level too large to stage next to the vector
+    small_nbuf = (int)std::min<size_t>(kSmallMaxBufs, (kSmallSmem - vec) / std::max<size_t>(small_buf, 128));
+    const size_t smem = vec + (size_t)small_nbuf * small_buf;
     SENK_CUDA(cudaFuncSetAttribute(k_ilu_small<VT, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     small = true;
 }
@@ -604,12 +607,15 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    // Row slots, one launch per colour (AUTO: measured fastest on the 128^3
-    // system, FP32 application 0.193 ms against 0.224 ms on compact chains;
-    // COLOURS); compact chains, one launch per colour (COMPACT) or one dataflow
-    // launch per sweep (DATAFLOW). A factor whose widest group does not fit
-    // shared memory falls back to row slots.
-    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW;
+    // AUTO, as measured on the 128^3 system: FP32 factors on compact chains,
+    // one launch per colour (application 0.176 ms against 0.194 ms on row
+    // slots, and 1.34x instead of 2.1x the algorithmic DRAM bytes), FP64
+    // factors on row slots (0.301 ms against 0.344 ms). COLOURS: row slots;
+    // COMPACT: compact chains per colour; DATAFLOW: compact chains, one launch
+    // per sweep. A factor whose widest group does not fit shared memory falls
+    // back to row slots.
+    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW ||
+                         (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == 4);
     const bool df = sweep_mode == SENK_SWEEP_DATAFLOW;
     if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s)))
         build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
