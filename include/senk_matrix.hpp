@@ -121,7 +121,16 @@ int Csr2Sell(T *val, int *cind, int *rptr, T **s_val, int **s_cind, int **s_len,
  * CSR -> BCSR with bnl x bnw blocks (senk_matrix.hpp:144-211). A block row holds,
  * in ascending order, every block column touched by one of its rows; block
  * values are column-major (bval[blk*bnl*bnw + c*bnl + r]) and zero where the CSR
- * has no entry. Exits when N is not a multiple of bnl and bnw.
+ * has no entry. Columns must ascend within each row. Exits when N is not a
+ * multiple of bnl and bnw.
+ *
+ * An empty row takes one entry: the reference's row cursor starts at rptr[row]
+ * and is only found finished after it has copied the entry there, which is the
+ * first entry of the next non-empty row (senk_matrix.hpp:159-177, 196-203). An
+ * L factor's row 0, and in ABMC order the first row of many blocks, so carries a
+ * value on or near the diagonal, and the ILUB sweeps read it. Kept, since the
+ * sweeps' results depend on it. Where no entry follows (trailing empty rows) the
+ * reference reads past the arrays; here such a row stays empty.
  */
 template <typename T>
 void Csr2Bcsr(T *val, int *cind, int *rptr, T **bval, int **bcind, int **brptr, int N, int bnl, int bnw)
@@ -130,7 +139,11 @@ void Csr2Bcsr(T *val, int *cind, int *rptr, T **bval, int **bcind, int **brptr, 
         std::printf("Error: Csr2Bcsr\n");
         std::exit(EXIT_FAILURE);
     }
-    const int nbr = N / bnl;
+    const int nbr = N / bnl, nnz = rptr[N];
+    // entries [rptr[row], row_end(row)) of a row, the one borrowed entry included
+    auto row_end = [&](int row) {
+        return rptr[row + 1] > rptr[row] ? rptr[row + 1] : std::min(rptr[row] + 1, nnz);
+    };
     *brptr = utils::SafeMalloc<int>(nbr + 1);
     (*brptr)[0] = 0;
     std::vector<int> cols;
@@ -138,7 +151,7 @@ void Csr2Bcsr(T *val, int *cind, int *rptr, T **bval, int **bcind, int **brptr, 
     for (int br = 0; br < nbr; br++) {
         cols.clear();
         for (int r = br * bnl; r < (br + 1) * bnl; r++)
-            for (int j = rptr[r]; j < rptr[r + 1]; j++) cols.push_back(cind[j] / bnw);
+            for (int j = rptr[r]; j < row_end(r); j++) cols.push_back(cind[j] / bnw);
         std::sort(cols.begin(), cols.end());
         cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
         bc.insert(bc.end(), cols.begin(), cols.end());
@@ -152,7 +165,7 @@ void Csr2Bcsr(T *val, int *cind, int *rptr, T **bval, int **bcind, int **brptr, 
         for (int r = 0; r < bnl; r++) {
             const int row = br * bnl + r;
             int blk = (*brptr)[br];
-            for (int j = rptr[row]; j < rptr[row + 1]; j++) {
+            for (int j = rptr[row]; j < row_end(row); j++) {
                 while ((*bcind)[blk] != cind[j] / bnw) blk++;
                 (*bval)[(size_t)blk * bnl * bnw + (cind[j] % bnw) * bnl + r] = val[j];
             }

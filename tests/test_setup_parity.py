@@ -97,3 +97,27 @@ def test_golden_c1_setup(golden):
     Ar = S.Reordering(A, LP, RP)
     L, U, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
     assert sha(L.val) == g["L_sha"] and sha(U.val) == g["U_sha"]
+
+
+@pytest.mark.parametrize("bnl,bnw", [(1, 1), (2, 1), (2, 2), (3, 3), (4, 1), (4, 2), (8, 1), (8, 2)])
+def test_csr2bcsr_of_factors_matches_oracle(port, bnl, bnw):
+    # L rows without lower entries (row 0, and the first rows of ABMC blocks)
+    # take the next row's first entry, as in the reference
+    A = P.convdiff3d(12, 0.5)
+    nc, sc, LP, RP = port.abmc_permutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    L, U, _ = S.Split(S.Ilu0(S.Reordering(A, LP, RP)), "L-DU", True)
+    assert np.count_nonzero(np.diff(L.rptr) == 0) > 1
+    for F in (L, U):
+        a, o = S.Csr2Bcsr(F, bnl, bnw), port.csr2bcsr(F, bnl, bnw)
+        assert all(eq(x, y) for x, y in zip(a, o))
+    assert S.Csr2Bcsr(L, bnl, bnw)[0][0] != 0.0
+
+
+def test_csr2bcsr_of_factors_matches_reference(port, ref):
+    A = P.convdiff3d(8, 0.5)
+    nc, sc, LP, RP = port.abmc_permutation(A.cind, A.rptr, A.n, 8, False, "connect")
+    L, U, _ = S.Split(S.Ilu0(S.Reordering(A, LP, RP)), "L-DU", True)
+    for bnl, bnw in ((8, 1), (2, 2), (4, 2)):
+        for F in (L, U):
+            a, r = S.Csr2Bcsr(F, bnl, bnw), ref.csr2bcsr(F, bnl, bnw)
+            assert all(eq(x, y) for x, y in zip(a, r))
