@@ -87,6 +87,11 @@ typedef struct {
 #define SENK_SWEEP_COMPACT 3  /* compact chain layout (chains packed per lane,
                                  padding only to the widest chain of a group), one
                                  launch per colour, one CTA per group */
+#define SENK_SWEEP_PERSISTENT 4 /* compact chain layout, one cooperative launch per
+                                 sweep: the CTAs take the groups of a colour in
+                                 turn, a grid barrier separates the colours, and
+                                 each group's block is staged while the group
+                                 before it is solved */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0
@@ -376,6 +381,8 @@ int senk_system_bicgstab(senk_system *sys, double nrm_b, int max_iter, double ep
 #define SENK_OP_SWEEP_L 2   /* the L sweep alone */
 #define SENK_OP_SWEEP_U 3   /* the U sweep alone (in place) */
 #define SENK_OP_DOT 4       /* one dot product of two vectors */
+#define SENK_OP_MULTIDOT 5  /* the Arnoldi step's dot products: 16 basis vectors with w */
+#define SENK_OP_UPDATE 6    /* the Arnoldi step's update w -= V c over 16 basis vectors, with ||w|| */
 #define SENK_OP_INNER 16    /* added to an op: the FP32 copy of a mixed system */
 int senk_system_time_op(senk_system *sys, int op, int reps, double *ms_per_rep, long long *bytes_per_rep);
 
@@ -475,8 +482,10 @@ int senk_ilu_plan_sweep(senk_ilu_plan *plan, int upper, const void *x, void *y, 
 int senk_ilu_plan_status(senk_ilu_plan *plan, void *stream);
 /* For tests of the error path: makes `group` of the dataflow sweep (upper = 0:
  * L, 1: U) wait on its own flag, which is never set before the group runs, so
- * its bounded wait runs out (about a second) on the next sweep. The plan keeps
- * this defect; destroy it afterwards. */
+ * its bounded wait runs out (about a second) on the next sweep. For the
+ * cooperative sweep (SENK_SWEEP_PERSISTENT; `group` ignored) the first grid
+ * barrier of the next sweep waits for more arrivals than there are CTAs. The
+ * plan keeps this defect; destroy it afterwards. */
 int senk_ilu_plan_test_stall(senk_ilu_plan *plan, int upper, int group);
 int senk_ilu_plan_destroy(senk_ilu_plan *plan);
 

@@ -169,7 +169,8 @@ struct SweepFactor {
     bool dataflow = false;         // compact: one launch per sweep (else one per colour)
     std::vector<int> colour_slots; // compact: widest block of each colour
     DevBuf<unsigned char> wcounts; // compact: per chain, external and in-chain counts of each row
-    DevBuf<int> dcolour_groups;    // compact: colour_groups on the device (small systems)
+    DevBuf<int> dcolour_groups;    // compact: colour_groups on the device
+    DevBuf<int4> levels;           // compact, per colour: {first group, groups, first slot, slots}
     DevBuf<VT> cdinv;              // compact U: inverted diagonal per chain (small systems)
     size_t level_bytes = 0;        // compact, chains of one row: most bytes one colour stages
     // compact, per colour: the launches of a sweep in order
@@ -186,6 +187,11 @@ struct SweepFactor {
     int slots_max = 0;             // widest group block (slots of 32 entries)
     int wf_warps = 0, wf_grid = 0; // warps per CTA, CTAs
     size_t wf_smem = 0;            // dynamic shared memory per CTA
+    // compact, one cooperative launch per sweep (k_sweep_cp): CTAs, bytes of
+    // each of its two staging buffers (ctrl holds its barrier words)
+    bool persistent = false;
+    int cp_grid = 0;
+    size_t cp_buf = 0;
 };
 
 // A split ILU factorisation with its sweep schedule.

@@ -85,6 +85,36 @@ k_spmv_csr(const MT *__restrict__ val, const int *__restrict__ cind, const int *
     }
 }
 
+// Row sum of one SELL-32 row (lane r of the slice at element offset o, w
+// columns): sum over k of val * x[col] in column order. The entries are taken
+// eight at a time with every load of a batch issued before the first product
+// (values and columns, then the x gathers), so a stencil row of seven entries
+// costs two dependent memory latencies instead of one per entry.
+template <typename MT, typename XT, typename A>
+__device__ __forceinline__ A sell_row_sum(const MT *__restrict__ val, const int *__restrict__ col,
+                                          const XT *__restrict__ x, int o, int w, int r)
+{
+    constexpr int B = 8;
+    A sum = 0;
+    for (int k = 0; k < w; k += B) {
+        MT v[B];
+        int c[B];
+        XT xv[B];
+#pragma unroll
+        for (int u = 0; u < B; u++) {
+            const int i0 = o + (k + u) * 32 + r;
+            v[u] = k + u < w ? ld_stream(val + i0) : MT(0);
+            c[u] = k + u < w ? ld_stream(col + i0) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < B; u++) xv[u] = k + u < w ? __ldg(x + c[u]) : XT(0);
+#pragma unroll
+        for (int u = 0; u < B; u++)
+            if (k + u < w) sum += (A)v[u] * (A)xv[u];
+    }
+    return sum;
+}
+
 // SELL-C SpMV, one thread per row, C = 32 rows per slice, slice-major columns:
 // element (slice s, column k, lane r) at off[s] + k*32 + r. `perm` (optional)
 // maps slice position -> row for sigma-sorted layouts.
@@ -100,22 +130,7 @@ k_spmv_sell32(const MT *__restrict__ val, const int *__restrict__ col, const int
     if (p >= ((long long)n + 31) / 32 * 32) return;
     const int s = (int)(p >> 5), r = (int)(p & 31);
     const int o = __ldg(off + s), w = (__ldg(off + s + 1) - o) >> 5;
-    A sum = 0;
-    int k = 0;
-    for (; k + 4 <= w; k += 4) {
-        const int i0 = o + k * 32 + r;
-        const MT v0 = ld_stream(val + i0), v1 = ld_stream(val + i0 + 32), v2 = ld_stream(val + i0 + 64), v3 = ld_stream(val + i0 + 96);
-        const int c0 = ld_stream(col + i0), c1 = ld_stream(col + i0 + 32), c2 = ld_stream(col + i0 + 64), c3 = ld_stream(col + i0 + 96);
-        const XT x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-        sum += (A)v0 * (A)x0;
-        sum += (A)v1 * (A)x1;
-        sum += (A)v2 * (A)x2;
-        sum += (A)v3 * (A)x3;
-    }
-    for (; k < w; k++) {
-        const int i0 = o + k * 32 + r;
-        sum += (A)ld_stream(val + i0) * (A)__ldg(x + ld_stream(col + i0));
-    }
+    const A sum = sell_row_sum<MT, XT, A>(val, col, x, o, w, r);
     const long long row = perm ? (long long)__ldg(perm + p) : p;
     if (row < n && row >= 0) y[row] = MODE == 1 ? (XT)((A)b[row] - sum) : (XT)sum;
 }
@@ -134,11 +149,7 @@ k_residual_sell32(const T *__restrict__ val, const int *__restrict__ col, const 
     if (p < n) {
         const int s = (int)(p >> 5), lane = (int)(p & 31);
         const int o = __ldg(off + s), w = (__ldg(off + s + 1) - o) >> 5;
-        A sum = 0;
-        for (int k = 0; k < w; k++) {
-            const int i0 = o + k * 32 + lane;
-            sum += (A)ld_stream(val + i0) * (A)__ldg(x + ld_stream(col + i0));
-        }
+        const A sum = sell_row_sum<T, T, A>(val, col, x, o, w, lane);
         const T v = (T)((A)b[p] - sum);
         r[p] = v;
         nacc = (double)v * (double)v;
@@ -825,28 +836,22 @@ struct SmallFactor {
     const VT *val;
     const int *col;
     const VT *cdinv;        // U: inverted diagonal per chain
-    const int *cgroups;     // group range of each colour (level set), processing order
+    const int4 *levels;     // per colour (level set), processing order: {first group, groups, first slot, slots}
     int ncolours;
 };
 
-// Stages the data of one level (colour) into buf with bulk copies counted on
+// Stages the data of one level (colour) lv into buf with bulk copies counted on
 // bar: group descriptors, chain descriptors, the groups' blocks (columns, then
-// values) and, for U, the chains' inverted diagonals. One thread. Returns the
-// bytes expected.
+// values) and, for U, the chains' inverted diagonals. One thread; no global
+// loads, so a stage costs the issuing thread a few instructions.
 template <typename VT>
-__device__ __forceinline__ void small_stage(const SmallFactor<VT> &F, bool upper, int c, unsigned char *buf,
+__device__ __forceinline__ void small_stage(const SmallFactor<VT> &F, bool upper, int4 lv, unsigned char *buf,
                                             unsigned long long *bar)
 {
-    const int g0 = __ldg(F.cgroups + c), g1 = __ldg(F.cgroups + c + 1), G = g1 - g0;
-    unsigned bytes = 0;
-    int e0 = 0, ne = 0;
-    if (G > 0) {
-        const WfGroup first = F.groups[g0], last = F.groups[g1 - 1];
-        e0 = first.off;
-        ne = last.off + (last.emax + last.imax) * 32 - e0;
-        bytes = (unsigned)G * 16u + (unsigned)G * 256u + (unsigned)ne * (4u + (unsigned)sizeof(VT)) +
-                (upper ? (unsigned)G * 32u * (unsigned)sizeof(VT) : 0u);
-    }
+    const int g0 = lv.x, G = lv.y, e0 = lv.z, ne = lv.w;
+    const unsigned bytes = G > 0 ? (unsigned)G * 16u + (unsigned)G * 256u + (unsigned)ne * (4u + (unsigned)sizeof(VT)) +
+                                       (upper ? (unsigned)G * 32u * (unsigned)sizeof(VT) : 0u)
+                                 : 0u;
     // earlier generic accesses to this buffer come before the async writes
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(bar, bytes);
@@ -869,9 +874,11 @@ __device__ __forceinline__ void small_stage(const SmallFactor<VT> &F, bool upper
 // whose vector fits in shared memory, in one CTA (which: bit 0 L, bit 1 U;
 // x == y allowed). The levels (colours) run in order with a barrier between
 // them, one thread per row; each level's data is staged by TMA into one of
-// nbuf buffers (2 to 8), nbuf - 1 levels ahead of the level being solved. A
-// TMA wait that runs out sets *status = 2 and the kernel leaves after waiting
-// once more for every copy it has issued.
+// nbuf buffers (2 to 8), nbuf - 1 levels ahead of the level being solved.
+// Thread 0 issues the copies; the level descriptor it needs is loaded one step
+// before, so no global load lies on the path from one level to the next. A TMA
+// wait that runs out sets *status = 2 and the kernel leaves after waiting once
+// more for every copy it has issued.
 constexpr int kSmallMaxBufs = 8;
 
 template <typename VT, typename XT>
@@ -881,29 +888,36 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
 {
     extern __shared__ __align__(128) unsigned char sms[];
     __shared__ __align__(8) unsigned long long bar[kSmallMaxBufs];
+    __shared__ int4 lsh[kSmallMaxBufs];  // descriptor of the level staged in each buffer
     if (gated(gate)) return;
     XT *ysh = reinterpret_cast<XT *>(sms);
     unsigned char *bufs = sms + ((size_t)n * sizeof(XT) + 127) / 128 * 128;
     const int nl = (which & 1) ? Lf.ncolours : 0, nu = (which & 2) ? Uf.ncolours : 0, steps = nl + nu;
+    auto desc = [&](int j) { return j < nl ? __ldg(Lf.levels + j) : __ldg(Uf.levels + (j - nl)); };
     // step j uses buffer j % nbuf, its (j / nbuf)-th use: phase parity (j / nbuf) & 1
-    auto stage = [&](int j) {
-        unsigned char *buf = bufs + (size_t)(j % nbuf) * buf_bytes;
-        if (j < nl) small_stage(Lf, false, j, buf, &bar[j % nbuf]);
-        else small_stage(Uf, true, j - nl, buf, &bar[j % nbuf]);
+    auto stage = [&](int j, int4 lv) {
+        const int b = j % nbuf;
+        lsh[b] = lv;
+        unsigned char *buf = bufs + (size_t)b * buf_bytes;
+        if (j < nl) small_stage(Lf, false, lv, buf, &bar[b]);
+        else small_stage(Uf, true, lv, buf, &bar[b]);
     };
+    int4 dn = make_int4(0, 0, 0, 0);  // thread 0: descriptor of the next level to stage
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; b++) mbar_init(&bar[b], 1);
-        for (int j = 0; j < nbuf - 1 && j < steps; j++) stage(j);
+        for (int j = 0; j < nbuf - 1 && j < steps; j++) stage(j, desc(j));
+        if (nbuf - 1 < steps) dn = desc(nbuf - 1);
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) ysh[i] = x[i];
     __syncthreads();
     for (int k = 0; k < steps; k++) {
         const int b = k % nbuf;
         // the buffer of step k - 1 is free again (the barrier at its end)
-        if (threadIdx.x == 0 && k + nbuf - 1 < steps) stage(k + nbuf - 1);
+        if (threadIdx.x == 0 && k + nbuf - 1 < steps) {
+            stage(k + nbuf - 1, dn);
+            if (k + nbuf < steps) dn = desc(k + nbuf);
+        }
         const bool upper = k >= nl;
-        const SmallFactor<VT> &F = upper ? Uf : Lf;
-        const int c = upper ? k - nl : k;
         const unsigned par = (unsigned)(k / nbuf) & 1u;
         const bool ok = mbar_wait_bounded(&bar[b], par, kWaitLimit);
         if (__syncthreads_or(!ok)) {
@@ -915,13 +929,12 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
             }
             return;
         }
-        const int G = __ldg(F.cgroups + c + 1) - __ldg(F.cgroups + c);
+        // written by thread 0 before the barrier that ended step k - nbuf + 1 (or the first one)
+        const int4 lv = lsh[b];
+        const int G = lv.y, e0 = lv.z, ne = lv.w;
         const unsigned char *sb = bufs + (size_t)b * buf_bytes;
         const WfGroup *sd = reinterpret_cast<const WfGroup *>(sb);
         const int2 *sc = reinterpret_cast<const int2 *>(sb + G * 16);
-        const int e0 = G > 0 ? sd[0].off : 0;
-        const WfGroup last = G > 0 ? sd[G - 1] : WfGroup{0, 0, 0, 0};
-        const int ne = last.off + (last.emax + last.imax) * 32 - e0;
         const int *scol = reinterpret_cast<const int *>(sb + G * 16 + G * 256);
         const VT *sval = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * 4);
         const VT *sdinv = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * (4 + sizeof(VT)));
@@ -1160,6 +1173,94 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int g0, int ng, const int2 *__res
     }
 }
 
+// One group of the compact chain layout, staged in shared memory (cw, vw: its
+// block; cnt: its per-chain row counts), for the thread of row l of chain q
+// (t: x of that row on entry): subtracts the row's external entries, then runs
+// the in-chain recurrence; the solved rows are in tsh on return (all threads
+// past a CTA barrier). NC reads y through the non-coherent path, for kernels in
+// which y's earlier rows were written by earlier kernels.
+template <typename VT, typename XT, int BS, bool UPPER, bool NC>
+__device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
+                                         XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, XT t,
+                                         const XT *y, int l, int q)
+{
+    // row l's external entries; in lane q's stream rows come in solve order
+    const unsigned char *cq = cnt + q * 2 * BS;
+    int eo = 0, ne = 0;
+    if constexpr (BS >= 8) {
+        // the chain's counts as 16-byte words (2 BS bytes per chain, 16-byte aligned)
+        const uint4 *c4 = reinterpret_cast<const uint4 *>(cq);
+#pragma unroll
+        for (int w = 0; w < (BS + 15) / 16; w++) {
+            const uint4 v = c4[w];
+            const unsigned words[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int b = 0; b < 16; b++) {
+                const int r = w * 16 + b;
+                if (r >= BS) break;
+                const int c = (int)((words[b >> 2] >> (8 * (b & 3))) & 255u);
+                if (r == l) ne = c;
+                if (UPPER ? r > l : r < l) eo += c;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < BS; r++)
+            if (UPPER ? r > l : r < l) eo += cq[r];
+        ne = cq[l];
+    }
+#pragma unroll 4
+    for (int k = 0; k < ne; k++) {
+        const int at = (eo + k) * 32 + q;
+        t -= (XT)vw[at] * (NC ? __ldg(y + (cw[at] & kColMask)) : y[cw[at] & kColMask]);
+    }
+    tsh[q][l] = t;
+    __syncthreads();
+    // In-chain recurrence, BS lanes per chain (lane = row), 32 / BS chains
+    // per warp, all warps busy: the rows are finished in solve order; the
+    // lane of the row finished at step s (U: after its inverted diagonal)
+    // broadcasts it by a shuffle within the chain's lanes, and every lane
+    // whose next in-chain entry is that column subtracts it. A lane's
+    // entries come in the same order as the steps (the reference's column
+    // order), two of them held in registers and refilled from the block.
+    if (BS > 1 || UPPER) {
+        constexpr int CPW = 32 / BS;  // chains per warp
+        const int lane = threadIdx.x & 31;
+        const int qc = l * CPW + lane / BS, rr = lane % BS;
+        const int *iw = cw + d.emax * 32 + ibase[qc];
+        const VT *iv = vw + d.emax * 32 + ibase[qc];
+        const unsigned char *cc = cnt + qc * 2 * BS;
+        int io = 0;
+#pragma unroll
+        for (int r = 0; r < BS; r++)
+            if (UPPER ? r > rr : r < rr) io += cc[BS + r];
+        int left = cc[BS + rr];
+        XT tt = tsh[qc][rr];
+        const XT di = UPPER ? dsh[qc][rr] : XT(1);
+        int c0 = -1, c1 = -1;
+        XT v0 = XT(0), v1 = XT(0);
+        int at = io;
+        if (left > 0) { c0 = iw[at] & 255; v0 = (XT)iv[at]; at++; }
+        if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
+#pragma unroll
+        for (int s = 0; s < BS; s++) {
+            const int c = UPPER ? BS - 1 - s : s;
+            if (UPPER && rr == c) tt *= di;
+            const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
+            if (c0 == c) {
+                tt -= v0 * yc;
+                left--;
+                c0 = c1;
+                v0 = v1;
+                c1 = -1;
+                if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
+            }
+        }
+        tsh[qc][rr] = tt;
+    }
+    __syncthreads();
+}
+
 // One colour per launch on the compact chain layout, one CTA of BS warps per
 // group: warp l takes row l of every chain (lane q = chain q) and subtracts
 // that row's external entries, read from the staged block at lane q's offset
@@ -1233,85 +1334,168 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         return;
     }
     if (gated(gate)) return;
-    {
-        if (!early_x && live) t = x[row];
-        // row l's external entries; in lane q's stream rows come in solve order
-        const unsigned char *cq = cnt + q * 2 * BS;
-        int eo = 0, ne = 0;
-        if constexpr (BS >= 8) {
-            // the chain's counts as 16-byte words (2 BS bytes per chain, 16-byte aligned)
-            const uint4 *c4 = reinterpret_cast<const uint4 *>(cq);
-#pragma unroll
-            for (int w = 0; w < (BS + 15) / 16; w++) {
-                const uint4 v = c4[w];
-                const unsigned words[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                for (int b = 0; b < 16; b++) {
-                    const int r = w * 16 + b;
-                    if (r >= BS) break;
-                    const int c = (int)((words[b >> 2] >> (8 * (b & 3))) & 255u);
-                    if (r == l) ne = c;
-                    if (UPPER ? r > l : r < l) eo += c;
-                }
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-                if (UPPER ? r > l : r < l) eo += cq[r];
-            ne = cq[l];
-        }
-#pragma unroll 4
-        for (int k = 0; k < ne; k++) {
-            const int at = (eo + k) * 32 + q;
-            t -= (XT)vw[at] * __ldg(y + (cw[at] & kColMask));
-        }
-        tsh[q][l] = t;
-        __syncthreads();
-        // In-chain recurrence, BS lanes per chain (lane = row), 32 / BS chains
-        // per warp, all warps busy: the rows are finished in solve order; the
-        // lane of the row finished at step s (U: after its inverted diagonal)
-        // broadcasts it by a shuffle within the chain's lanes, and every lane
-        // whose next in-chain entry is that column subtracts it. A lane's
-        // entries come in the same order as the steps (the reference's column
-        // order), two of them held in registers and refilled from the block.
-        if (BS > 1 || UPPER) {
-            constexpr int CPW = 32 / BS;  // chains per warp
-            const int lane = threadIdx.x & 31;
-            const int qc = l * CPW + lane / BS, rr = lane % BS;
-            const int *iw = cw + d.emax * 32 + ibase[qc];
-            const VT *iv = vw + d.emax * 32 + ibase[qc];
-            const unsigned char *cc = cnt + qc * 2 * BS;
-            int io = 0;
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-                if (UPPER ? r > rr : r < rr) io += cc[BS + r];
-            int left = cc[BS + rr];
-            XT tt = tsh[qc][rr];
-            const XT di = UPPER ? dsh[qc][rr] : XT(1);
-            int c0 = -1, c1 = -1;
-            XT v0 = XT(0), v1 = XT(0);
-            int at = io;
-            if (left > 0) { c0 = iw[at] & 255; v0 = (XT)iv[at]; at++; }
-            if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
-#pragma unroll
-            for (int s = 0; s < BS; s++) {
-                const int c = UPPER ? BS - 1 - s : s;
-                if (UPPER && rr == c) tt *= di;
-                const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
-                if (c0 == c) {
-                    tt -= v0 * yc;
-                    left--;
-                    c0 = c1;
-                    v0 = v1;
-                    c1 = -1;
-                    if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
-                }
-            }
-            tsh[qc][rr] = tt;
-        }
-        __syncthreads();
-        if (live) y[row] = tsh[q][l];
+    if (!early_x && live) t = x[row];
+    cc_solve<VT, XT, BS, UPPER, true>(d, cw, vw, cnt, tsh, dsh, ibase, t, y, l, q);
+    if (live) y[row] = tsh[q][l];
+}
+
+// All colours of one sweep in one cooperative launch, on the compact chain
+// layout: CTA b takes groups b, b + gridDim.x, ... of each colour (the group
+// body of k_sweep_cc), and a grid barrier separates the colours. Each group's
+// block and row counts are staged by TMA into one of two buffers while the
+// group before it is solved, across the barrier too (the blocks are read-only).
+// Rows of earlier colours were written in this launch, so y (and x, which may
+// be y) are read through the coherent path: the acquire at the barrier drops
+// L1 lines cached before it.
+//
+// ctrl = {arrivals, departures, abort}. Barrier k waits for k * gridDim.x
+// arrivals. A barrier wait that runs out of polls sets abort and *status = 1, a
+// TMA wait that runs out abort and *status = 2; after an abort every CTA stops
+// taking groups, waits (bounded) for its copies in flight and leaves, and the
+// last CTA to leave resets ctrl for the next launch.
+template <typename VT, typename XT, int BS, bool UPPER>
+__global__ void __launch_bounds__(BS * 32)
+k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, int ncolours,
+           const int2 *__restrict__ chains, const unsigned char *__restrict__ counts, const VT *__restrict__ val,
+           const int *__restrict__ col, const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate,
+           int *status, int *ctrl, unsigned buf_bytes)
+{
+    extern __shared__ __align__(128) unsigned char cps[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ XT tsh[32][BS + 1];
+    __shared__ XT dsh[UPPER ? 32 : 1][BS + 1];
+    __shared__ int ibase[32];
+    __shared__ int s_ok;
+    constexpr unsigned nbytes = 32u * 2u * BS;
+    const int l = threadIdx.x >> 5, q = threadIdx.x & 31;
+    if (gated(gate)) return;  // every CTA alike, before any control word is touched
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
     }
+    __syncthreads();
+    auto stage = [&](int g, int k) {  // thread 0: group g's block and counts into buffer k
+        const WfGroup d = groups[g];
+        const int slots = d.emax + d.imax;
+        const unsigned cbytes = (unsigned)slots * 32u * 4u, vbytes = (unsigned)slots * 32u * (unsigned)sizeof(VT);
+        unsigned char *b = cps + (size_t)k * buf_bytes;
+        // the generic reads of this buffer (two groups back) come before the async writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&bar[k], cbytes + vbytes + nbytes);
+        if (slots > 0) {
+            bulk_g2s(b, col + d.off, cbytes, &bar[k]);
+            bulk_g2s(b + cbytes, val + d.off, vbytes, &bar[k]);
+        }
+        bulk_g2s(b + cbytes + vbytes, counts + (size_t)g * nbytes, nbytes, &bar[k]);
+    };
+    // this CTA's first group in colour c or a later one (-1: none); its colour in *cc
+    auto first_from = [&](int c, int *cc) {
+        for (; c < ncolours; c++) {
+            const int g = __ldg(cgroups + c) + (int)blockIdx.x;
+            if (g < __ldg(cgroups + c + 1)) {
+                *cc = c;
+                return g;
+            }
+        }
+        return -1;
+    };
+    // per buffer b: bit b of ph = parity of its next completion, bit b of pend = a copy in flight
+    unsigned ph = 0u, pend = 0u;
+    int k = 0, cdummy = 0;
+    {
+        const int g = first_from(0, &cdummy);
+        if (g >= 0) {
+            if (threadIdx.x == 0) stage(g, 0);
+            pend = 1u;
+        }
+    }
+    bool ok = true;
+    for (int c = 0; c < ncolours && ok; c++) {
+        const int ge = __ldg(cgroups + c + 1);
+        for (int g = __ldg(cgroups + c) + (int)blockIdx.x; g < ge; g += (int)gridDim.x) {
+            int cn = c, gn = g + (int)gridDim.x;
+            if (gn >= ge) gn = first_from(c + 1, &cn);
+            const bool arrived = mbar_wait_bounded(&bar[k], (ph >> k) & 1u, kWaitLimit);
+            if (__syncthreads_or(!arrived)) {
+                if (threadIdx.x == 0) {
+                    atomicExch(status, 2);
+                    atomicExch(ctrl + 2, 1);
+                }
+                ok = false;
+                break;
+            }
+            ph ^= 1u << k;
+            pend &= ~(1u << k);
+            if (gn >= 0) {
+                if (threadIdx.x == 0) stage(gn, k ^ 1);
+                pend |= 1u << (k ^ 1);
+            }
+            const WfGroup d = groups[g];
+            const int slots = d.emax + d.imax;
+            const unsigned char *b = cps + (size_t)k * buf_bytes;
+            const int *cw = reinterpret_cast<const int *>(b);
+            const VT *vw = reinterpret_cast<const VT *>(b + (size_t)slots * 32 * 4);
+            const unsigned char *cnt = b + (size_t)slots * 32 * (4 + sizeof(VT));
+            const bool live = q < d.nchains;
+            const int2 ch = live ? __ldg(chains + (size_t)g * 32 + q) : make_int2(0, 0);
+            const int row = ch.x + l;
+            if (UPPER) dsh[q][l] = live ? (XT)__ldg(dinv + row) : XT(0);
+            if (l == 0) {
+                const int I = (int)((unsigned)ch.y >> 16);
+                int v = I;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(0xffffffffu, v, o);
+                    if (q >= o) v += u;
+                }
+                ibase[q] = v - I;
+            }
+            const XT t = live ? x[row] : XT(0);
+            cc_solve<VT, XT, BS, UPPER, false>(d, cw, vw, cnt, tsh, dsh, ibase, t, y, l, q);
+            if (live) y[row] = tsh[q][l];
+            k ^= 1;
+        }
+        if (!ok || c + 1 == ncolours) break;
+        // grid barrier: this CTA's rows of colour c are written
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(ctrl, 1);
+            const int target = (c + 1) * (int)gridDim.x;
+            int good = 1;
+            unsigned polls = 0;
+            while (ld_acquire(ctrl) < target) {
+                if (ld_acquire(ctrl + 2)) {
+                    good = 0;
+                    break;
+                }
+                if (++polls > 64u) __nanosleep(32);
+                if (polls > kFlagPolls) {
+                    atomicExch(ctrl + 2, 1);
+                    atomicExch(status, 1);
+                    good = 0;
+                    break;
+                }
+            }
+            __threadfence();
+            s_ok = good;
+        }
+        __syncthreads();
+        ok = s_ok != 0;
+    }
+    // copies still in flight (after an abort) land before the CTA leaves
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 2; b++)
+            if ((pend >> b) & 1u) mbar_wait_bounded(&bar[b], (ph >> b) & 1u, kWaitLimit);
+        __threadfence();
+        if (atomicAdd(ctrl + 1, 1) == (int)gridDim.x - 1) {
+            ctrl[0] = 0;
+            ctrl[2] = 0;
+            __threadfence();
+            atomicExch(ctrl + 1, 0);
+        }
+    }
+    __syncthreads();
 }
 
 }  // namespace senkgpu

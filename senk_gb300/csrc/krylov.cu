@@ -342,8 +342,11 @@ int System<T>::gmres(double nrm_b, int outer, int m, double eps, senk_result *re
 template <typename T>
 void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
 {
-    SENK_REQUIRE(op == SENK_OP_SPMV || op == SENK_OP_DOT || has_pc(), "system has no preconditioner");
-    ensure_gmres(std::max(m_alloc, 1));
+    SENK_REQUIRE(op == SENK_OP_SPMV || op == SENK_OP_DOT || op == SENK_OP_MULTIDOT || op == SENK_OP_UPDATE ||
+                     has_pc(),
+                 "system has no preconditioner");
+    constexpr int kBasis = 16;  // columns of the Arnoldi-step ops (the middle of a GMRES(30) cycle)
+    ensure_gmres(std::max(m_alloc, (op == SENK_OP_MULTIDOT || op == SENK_OP_UPDATE) ? kBasis : 1));
     T *v0 = V.p, *v1 = V.p + n;
     const long long vb = sizeof(T);
     long long bytes = 0;
@@ -362,6 +365,14 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
         case SENK_OP_DOT:
             launch_multidot<T, false>(dim3(red.ctas, 1), stream, v0, n, 1, v1, n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
             break;
+        case SENK_OP_MULTIDOT:
+            launch_multidot<T, false>(dim3(red.ctas, (kBasis + 7) / 8), stream, V.p, n, kBasis, V.p + (long long)kBasis * n,
+                                      n, red.part.p, red.ticket.p, coef.p, nullptr, nullptr);
+            break;
+        case SENK_OP_UPDATE:
+            launch_update<T, kEpiNone>(red.ctas, stream, V.p, n, kBasis, coef.p, V.p + (long long)kBasis * n, n,
+                                       red.part.p, red.ticket.p, nullptr, st.p, GmresEpi{}, nullptr);
+            break;
         default: throw ArgError("unknown op");
         }
     };
@@ -377,10 +388,19 @@ void System<T>::time_op(int op, int reps, double *ms_out, long long *bytes_out)
                     : (pc->U.nnz - n) * (vb + 4) + 3LL * n * vb;
         break;
     case SENK_OP_DOT: bytes = 2LL * n * vb; break;
+    case SENK_OP_MULTIDOT: bytes = (kBasis + 1LL) * n * vb; break;
+    case SENK_OP_UPDATE: bytes = (kBasis + 2LL) * n * vb; break;
     }
     // deterministic finite inputs
-    ew<T, 4>(x.p, v0, nullptr, n, T(0), T(0), nullptr, 1.0, stream, nullptr);
-    SENK_CUDA(cudaMemsetAsync(v1, 0, vb * n, stream));
+    if (op == SENK_OP_MULTIDOT || op == SENK_OP_UPDATE) {
+        SENK_CUDA(cudaMemsetAsync(V.p, 0, vb * n * (kBasis + 1), stream));
+        SENK_CUDA(cudaMemsetAsync(coef.p, 0, sizeof(double) * kBasis, stream));
+        for (int k = 0; k <= kBasis; k++)
+            ew<T, 4>(x.p, V.p + (long long)k * n, nullptr, n, T(0), T(0), nullptr, 1.0, stream, nullptr);
+    } else {
+        ew<T, 4>(x.p, v0, nullptr, n, T(0), T(0), nullptr, 1.0, stream, nullptr);
+        SENK_CUDA(cudaMemsetAsync(v1, 0, vb * n, stream));
+    }
     run();
     SENK_CUDA(cudaEventRecord(ev0, stream));
     for (int i = 0; i < reps; i++) run();

@@ -61,7 +61,14 @@ int senk_ilu_plan_test_stall(senk_ilu_plan *plan, int upper, int group)
         SENK_REQUIRE(plan && (plan->d || plan->f), "null plan or not a CSR factor plan");
         auto stall = [&](auto &P) {
             auto &F = upper ? P.U : P.L;
-            SENK_REQUIRE(F.dataflow, "the factor is not swept by the dataflow schedule");
+            if (F.persistent) {
+                SENK_REQUIRE(F.colour_groups.size() > 2, "the sweep has no grid barrier (one colour)");
+                // arrivals start far below any barrier's target
+                const int low = -(1 << 30);
+                SENK_CUDA(cudaMemcpy(F.ctrl.p, &low, sizeof(int), cudaMemcpyHostToDevice));
+                return;
+            }
+            SENK_REQUIRE(F.dataflow, "the factor is not swept by the dataflow or cooperative schedule");
             SENK_REQUIRE(group >= 0 && group < F.ngroups, "group out of range");
             int ptr[2];
             SENK_CUDA(cudaMemcpy(ptr, F.dep_ptr.p + group, sizeof(ptr), cudaMemcpyDeviceToHost));

@@ -179,6 +179,7 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.widths.upload(wd.data(), wd.size(), s);
     F.dataflow = false;
     F.compact = false;
+    F.persistent = false;
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
 }
@@ -217,6 +218,7 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.bs = bs;
     F.compact = true;
     F.dataflow = dataflow;
+    F.persistent = false;
     F.ngroups = ng;
     F.slots_max = lay.slots_max;
     F.elems = (long long)lay.col.size();
@@ -240,6 +242,19 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.wcounts.upload(lay.counts.data(), lay.counts.size(), s);
     F.dcolour_groups.alloc(lay.colour_groups.size());
     F.dcolour_groups.upload(lay.colour_groups.data(), lay.colour_groups.size(), s);
+    std::vector<int4> lv;
+    for (size_t c = 0; c + 1 < lay.colour_groups.size(); c++) {
+        const int g0 = lay.colour_groups[c], g1 = lay.colour_groups[c + 1];
+        int e0 = 0, ne = 0;
+        if (g1 > g0) {
+            const WfGroup &last = lay.groups[g1 - 1];
+            e0 = lay.groups[g0].off;
+            ne = last.off + (last.emax + last.imax) * 32 - e0;
+        }
+        lv.push_back(make_int4(g0, g1 - g0, e0, ne));
+    }
+    F.levels.alloc(std::max<size_t>(lv.size(), 1));
+    F.levels.upload(lv.data(), lv.size(), s);
     if (upper) {
         F.cdinv.alloc(std::max<size_t>(lay.cdinv.size(), 1));
         F.cdinv.upload(lay.cdinv.data(), lay.cdinv.size(), s);
@@ -404,6 +419,61 @@ void shape_cc(SweepFactor<VT> &F)
                                    (int)std::max<size_t>(most, 48 * 1024)));
 }
 
+// Compact chains, all colours of the sweep in one cooperative launch
+// (k_sweep_cp); ctrl holds its barrier words.
+template <typename VT, typename XT, int BS, bool UPPER>
+void launch_cp(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
+{
+    if (F.ngroups == 0) return;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(F.cp_grid);
+    cfg.blockDim = dim3(BS * 32);
+    cfg.dynamicSmemBytes = 2 * F.cp_buf;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cp<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p,
+                                 (const int *)F.dcolour_groups.p, (int)F.colour_groups.size() - 1,
+                                 (const int2 *)F.wchains.p, (const unsigned char *)F.wcounts.p, (const VT *)F.val.p,
+                                 (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate, status, F.ctrl.p,
+                                 (unsigned)F.cp_buf));
+}
+
+// Shape of the cooperative sweep: two staging buffers of the widest group's
+// block, as many CTAs as are resident at once but no more than the largest
+// colour's groups. Leaves `persistent` false (per-colour launches) when the
+// buffers do not fit or the device cannot launch cooperatively.
+template <typename VT, int BS, bool UPPER>
+void shape_cp(SweepFactor<VT> &F)
+{
+    F.persistent = false;
+    int coop = 0, dev = 0;
+    SENK_CUDA(cudaGetDevice(&dev));
+    SENK_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop || F.ngroups == 0) return;
+    size_t buf = 0;
+    for (const auto &L : F.launches) buf = std::max(buf, L.smem);
+    buf = (buf + 127) / 128 * 128;
+    if (2 * buf > kMaxWfSmem) return;
+    auto kern = k_sweep_cp<VT, VT, BS, UPPER>;
+    SENK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)std::max<size_t>(2 * buf, 48 * 1024)));
+    int per_sm = 0;
+    SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 2 * buf));
+    if (per_sm < 1) return;
+    int widest = 0;
+    for (size_t c = 0; c + 1 < F.colour_groups.size(); c++)
+        widest = std::max(widest, F.colour_groups[c + 1] - F.colour_groups[c]);
+    F.cp_buf = buf;
+    F.cp_grid = std::max(1, std::min(widest, per_sm * sm_count()));
+    if (F.ctrl.n < 4) F.ctrl.alloc(4);
+    SENK_CUDA(cudaMemset(F.ctrl.p, 0, 4 * sizeof(int)));
+    F.persistent = true;
+}
+
 // Launch shape of a dataflow sweep: as many warps per CTA (up to 8) as the
 // shared memory allows, and as many CTAs as are resident at once (every warp
 // loops over groups, so the grid need not cover them).
@@ -428,8 +498,12 @@ void shape_wf(SweepFactor<VT> &F)
 template <typename VT, bool UPPER, int BS>
 void shape_compact_bs(SweepFactor<VT> &F)
 {
-    if (F.dataflow) shape_wf<VT, BS, UPPER>(F);
-    else shape_cc<VT, BS, UPPER>(F);
+    if (F.dataflow) {
+        shape_wf<VT, BS, UPPER>(F);
+        return;
+    }
+    shape_cc<VT, BS, UPPER>(F);
+    if (F.persistent) shape_cp<VT, BS, UPPER>(F);
 }
 
 template <typename VT, bool UPPER>
@@ -454,6 +528,7 @@ void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cud
 #define SENK_COMPACT_CASE(BS)                                                      \
     case BS:                                                                       \
         if (F.dataflow) launch_wf<VT, XT, BS, UPPER>(F, status, x, y, s, gate);    \
+        else if (F.persistent) launch_cp<VT, XT, BS, UPPER>(F, status, x, y, s, gate); \
         else launch_cc<VT, XT, BS, UPPER>(F, status, x, y, s, gate);               \
         break;
         switch (F.bs) {
@@ -501,7 +576,7 @@ void IluPlan<VT>::sweep_small(int which, const VT *x, VT *y, cudaStream_t s, con
 {
     auto mk = [](const SweepFactor<VT> &F) {
         return SmallFactor<VT>{(const WfGroup *)F.wgroups.p, (const int2 *)F.wchains.p, (const VT *)F.val.p,
-                               (const int *)F.col.p, (const VT *)F.cdinv.p, (const int *)F.dcolour_groups.p,
+                               (const int *)F.col.p, (const VT *)F.cdinv.p, (const int4 *)F.levels.p,
                                (int)F.colour_groups.size() - 1};
     };
     const size_t smem = ((size_t)n * sizeof(VT) + 127) / 128 * 128 + (size_t)small_nbuf * small_buf;
@@ -567,7 +642,8 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
                         cudaStream_t s, int sweep_mode)
 {
     SENK_REQUIRE(sweep_mode == SENK_SWEEP_AUTO || sweep_mode == SENK_SWEEP_COLOURS ||
-                     sweep_mode == SENK_SWEEP_DATAFLOW || sweep_mode == SENK_SWEEP_COMPACT,
+                     sweep_mode == SENK_SWEEP_DATAFLOW || sweep_mode == SENK_SWEEP_COMPACT ||
+                     sweep_mode == SENK_SWEEP_PERSISTENT,
                  "unknown sweep mode");
     SENK_REQUIRE(N > 0, "N must be positive");
     SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
@@ -614,19 +690,24 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
     // COMPACT: compact chains per colour; DATAFLOW: compact chains, one launch
     // per sweep. A factor whose widest group does not fit shared memory falls
     // back to row slots.
-    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW ||
+    const bool persistent = sweep_mode == SENK_SWEEP_PERSISTENT;
+    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW || persistent ||
                          (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == 4);
     const bool df = sweep_mode == SENK_SWEEP_DATAFLOW;
     if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s)))
         build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
-    else
+    else {
+        L.persistent = persistent;
         shape_wf_bs<VT, false>(L);
+    }
     // For U, "earlier" means a later colour: flip the colour numbers.
     for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
     if (!(compact && build_factor_wf(U, true, N, uval, ucind, urptr, bwd, bs, colour_of, df, s)))
         build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
-    else
+    else {
+        U.persistent = persistent;
         shape_wf_bs<VT, true>(U);
+    }
 }
 
 template <typename VT>
@@ -662,7 +743,7 @@ void IluPlan<VT>::check_status(cudaStream_t s) const
     SENK_CUDA(cudaStreamSynchronize(s));
     throw CudaError{cudaErrorLaunchTimeout,
                     h == 2 ? "ILU sweep: a TMA copy of a factor block did not complete"
-                           : "ILU sweep: a wait for an earlier group's rows ran out",
+                           : "ILU sweep: a wait for an earlier group's or colour's rows ran out",
                     __FILE__, __LINE__};
 }
 

@@ -196,6 +196,96 @@ int emulate(int N, const VT *val, const int *cind, const int *rptr, int upper, c
     }
 }
 
+// The schedule of the cooperative sweep (k_sweep_cp) on `grid` CTAs, repeated
+// on the CPU: each CTA's walk over the colours (first_from / next group), the
+// group it stages into each of its two buffers and when it consumes it, with
+// the staged bytes checked against the buffer size the host computes (the
+// widest colour's block plus the row counts, rounded to 128 bytes) and the
+// copy addresses and sizes against TMA's 16-byte rule. Every group must be
+// solved exactly once, by the CTA the kernel assigns, after that CTA's groups
+// of the colours before its own (the grid barriers order the other CTAs').
+template <typename VT>
+int cp_schedule(int N, const VT *val, const int *cind, const int *rptr, int upper, const int *cptr, int cnum, int bs,
+                int grid, char *err, int errlen)
+{
+    auto fail = [&](const std::string &m) {
+        std::snprintf(err, errlen, "%s", m.c_str());
+        return 1;
+    };
+    try {
+        std::vector<WfColour> colours;
+        std::vector<int> colour_of(N);
+        for (int k = 0; k < cnum; k++) {
+            const int c = upper ? cnum - 1 - k : k;
+            colours.push_back({cptr[c] * bs, cptr[c + 1] * bs});
+            for (int p = cptr[c] * bs; p < cptr[c + 1] * bs; p++) colour_of[p] = k;
+        }
+        WfLayout<VT> L;
+        if (!make_wf_layout(L, upper != 0, N, val, cind, rptr, colours, bs, colour_of.data(), (size_t)160 * 1024))
+            return fail("layout does not fit");
+        const std::vector<int> &cg = L.colour_groups;
+        const int nc = (int)cg.size() - 1;
+        size_t buf = 0;  // as the host: per colour, widest block + counts, 16-byte rounded; then 128
+        for (int c = 0; c < nc; c++)
+            buf = std::max(buf, ((size_t)L.colour_slots[c] * 32 * (4 + sizeof(VT)) + 32 * 2 * (size_t)bs + 15) / 16 * 16);
+        buf = (buf + 127) / 128 * 128;
+        const size_t nbytes = 32 * 2 * (size_t)bs;
+        if (buf % 16 || nbytes % 16) return fail("buffer or count block not a multiple of 16 bytes");
+        std::vector<int> solved((size_t)cg[nc], 0);
+        int widest = 0;
+        for (int c = 0; c < nc; c++) widest = std::max(widest, cg[c + 1] - cg[c]);
+        if (grid > widest) return fail("grid wider than the widest colour");
+        for (int b = 0; b < grid; b++) {
+            auto first_from = [&](int c, int *cc) {
+                for (; c < nc; c++)
+                    if (cg[c] + b < cg[c + 1]) {
+                        *cc = c;
+                        return cg[c] + b;
+                    }
+                return -1;
+            };
+            int staged[2] = {-1, -1};
+            auto stage = [&](int g, int k) {
+                if (staged[k] >= 0) return fail("buffer restaged before its group was solved");
+                const WfGroup &d = L.groups[g];
+                const size_t slots = (size_t)d.emax + d.imax;
+                const size_t cb = slots * 32 * 4, vb = slots * 32 * sizeof(VT);
+                if (cb + vb + nbytes > buf) return fail("group block larger than the staging buffer");
+                if ((size_t)d.off % 32 || cb % 16 || vb % 16) return fail("copy not 16-byte aligned");
+                if ((size_t)d.off + slots * 32 > L.col.size()) return fail("block past the factor");
+                if ((size_t)(g + 1) * nbytes > L.counts.size()) return fail("counts past the array");
+                staged[k] = g;
+                return 0;
+            };
+            int k = 0, cd = 0;
+            int g0 = first_from(0, &cd);
+            if (g0 < 0) return fail("a CTA without a group");
+            if (stage(g0, 0)) return 1;
+            for (int c = 0; c < nc; c++) {
+                const int ge = cg[c + 1];
+                for (int g = cg[c] + b; g < ge; g += grid) {
+                    int cn = c, gn = g + grid;
+                    if (gn >= ge) gn = first_from(c + 1, &cn);
+                    if (staged[k] != g) return fail("solved group is not the one staged in its buffer");
+                    staged[k] = -1;
+                    if (gn >= 0 && stage(gn, k ^ 1)) return 1;
+                    for (int cc = 0; cc < c; cc++)
+                        for (int h = cg[cc]; h < cg[cc + 1]; h++)
+                            if (!solved[h] && (h - cg[cc]) % grid == b) return fail("earlier colour not finished");
+                    solved[g]++;
+                    k ^= 1;
+                }
+            }
+            if (staged[0] >= 0 || staged[1] >= 0) return fail("a staged group was never solved");
+        }
+        for (size_t g = 0; g < solved.size(); g++)
+            if (solved[g] != 1) return fail("group " + std::to_string(g) + " solved " + std::to_string(solved[g]) + " times");
+        return 0;
+    } catch (const std::exception &ex) {
+        return fail(ex.what());
+    }
+}
+
 }  // namespace
 
 extern "C" int wf_emulate_d(int N, const double *val, const int *cind, const int *rptr, int upper, const int *cptr,
@@ -215,4 +305,16 @@ extern "C" int wf_emulate_s(int N, const float *val, const int *cind, const int 
                             int cnum, int bs, const float *x, float *y, char *err, int errlen)
 {
     return emulate<float>(N, val, cind, rptr, upper, cptr, cnum, bs, x, y, err, errlen);
+}
+
+extern "C" int wf_cp_schedule_s(int N, const float *val, const int *cind, const int *rptr, int upper, const int *cptr,
+                                int cnum, int bs, int grid, char *err, int errlen)
+{
+    return cp_schedule<float>(N, val, cind, rptr, upper, cptr, cnum, bs, grid, err, errlen);
+}
+
+extern "C" int wf_cp_schedule_d(int N, const double *val, const int *cind, const int *rptr, int upper,
+                                const int *cptr, int cnum, int bs, int grid, char *err, int errlen)
+{
+    return cp_schedule<double>(N, val, cind, rptr, upper, cptr, cnum, bs, grid, err, errlen);
 }

@@ -167,7 +167,8 @@ class Plan:
 SWEEPS = [("natural", 16), ("amc", 16), ("abmc", 16), ("abmc", 8), ("abmc", 32), ("abmc", 4), ("abmc", 2)]
 
 
-@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT])
+@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT,
+                                   L.SWEEP_PERSISTENT])
 @pytest.mark.parametrize("case", ["poisson128", "convdiff24", "vardiff16"])
 @pytest.mark.parametrize("sched,bsize", SWEEPS)
 def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
@@ -200,7 +201,8 @@ def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
     assert rel(host(x2), want) <= 1e-12
 
 
-@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT])
+@pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT,
+                                   L.SWEEP_PERSISTENT])
 @pytest.mark.parametrize("sched,bsize", [("abmc", 16), ("natural", 16), ("amc", 16), ("abmc", 4)])
 def test_ilu_sweeps_f32(torch, port, sched, bsize, sweep):
     A = P.convdiff3d(24, 0.5)
@@ -233,14 +235,15 @@ def test_ilu_sweep_golden(torch, small):
 
 def test_ilu_sweep_at_benchmark_size(torch, port):
     """The 64^3 convection-diffusion system (16,384 chains, 11 colours) against
-    the oracle under the default, dataflow and compact schedules, FP64 and FP32,
-    several applications in a row."""
+    the oracle under the default, dataflow, compact and cooperative schedules,
+    FP64 and FP32, several applications in a row."""
     A = P.convdiff3d(64, 0.5)
     Ar, L_, U_, sc, nc, kind, bs = _factors(A, "abmc", 16)
     v = np.random.default_rng(9).uniform(-1, 1, A.n)
     want = port.sptrsv(U_, port.sptrsv(L_, v, False), True)
     for T, tol, sweep in ((np.float64, 1e-12, L.SWEEP_AUTO), (np.float32, 1e-5, L.SWEEP_AUTO),
-                          (np.float64, 1e-12, L.SWEEP_DATAFLOW), (np.float32, 1e-5, L.SWEEP_COMPACT)):
+                          (np.float64, 1e-12, L.SWEEP_DATAFLOW), (np.float32, 1e-5, L.SWEEP_COMPACT),
+                          (np.float64, 1e-12, L.SWEEP_PERSISTENT), (np.float32, 1e-5, L.SWEEP_PERSISTENT)):
         pl = Plan(L_, U_, kind, sc, nc, bs, T, sweep=sweep)
         L.check("plan", pl.code)
         xd = dev(torch, v.astype(T))
@@ -278,6 +281,28 @@ def test_dataflow_wait_that_runs_out_is_reported(torch):
     L.check("plan", pl2.code)
     L.check("apply", L.lib().senk_ilu_plan_apply(pl2.h, xd.data_ptr(), yd.data_ptr(), None))
     L.check("status", L.lib().senk_ilu_plan_status(pl2.h, None))
+
+
+def test_cooperative_barrier_wait_that_runs_out_is_reported(torch, port):
+    """The cooperative sweep's first grid barrier made to wait for more arrivals
+    than there are CTAs: every CTA gives up after its bounded wait, the call
+    reports the failure, the device stays usable, and the plan's next sweep (the
+    launch that gave up reset the barrier words) is correct."""
+    A = P.convdiff3d(24, 0.5)
+    Ar, L_, U_, sc, nc, kind, bs = _factors(A, "abmc", 16)
+    pl = Plan(L_, U_, kind, sc, nc, bs, sweep=L.SWEEP_PERSISTENT)
+    L.check("plan", pl.code)
+    L.check("stall", L.lib().senk_ilu_plan_test_stall(pl.h, 1, 0))
+    v = np.random.default_rng(8).uniform(-1, 1, A.n)
+    xd = dev(torch, v)
+    yd = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    L.check("apply", L.lib().senk_ilu_plan_apply(pl.h, xd.data_ptr(), yd.data_ptr(), None))
+    assert L.lib().senk_ilu_plan_status(pl.h, None) == L.ERR_CUDA
+    assert "wait" in L.lib().senk_last_error().decode()
+    L.check("apply", L.lib().senk_ilu_plan_apply(pl.h, xd.data_ptr(), yd.data_ptr(), None))
+    L.check("status", L.lib().senk_ilu_plan_status(pl.h, None))
+    torch.cuda.synchronize()
+    assert rel(host(yd), port.sptrsv(U_, port.sptrsv(L_, v, False), True)) <= 1e-12
 
 
 def test_plan_rejects_bad_schedules():

@@ -30,6 +30,11 @@ def emu(tmp_path_factory):
     lib.wf_emulate_levels_d.restype = C.c_int
     lib.wf_emulate_levels_d.argtypes = [C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                                                                         C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
+    for name in ("wf_cp_schedule_s", "wf_cp_schedule_d"):
+        f = getattr(lib, name)
+        f.restype = C.c_int
+        f.argtypes = [C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_char_p,
+                                                      C.c_int]
     for name in ("wf_emulate_d", "wf_emulate_s"):
         f = getattr(lib, name)
         f.restype = C.c_int
@@ -116,3 +121,21 @@ def test_emulated_level_set_layout_matches_the_oracle(emu, port, n):
         out = y
     want = port.sptrsv(U_, port.sptrsv(L_, v, False), True)
     assert np.max(np.abs(out - want)) <= 1e-14 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("n,bs,grid", [(24, 16, 7), (24, 16, 1), (32, 4, 150), (16, 1, 13), (64, 16, 456)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_cooperative_schedule(emu, n, bs, grid, dtype):
+    """k_sweep_cp's walk on `grid` CTAs (capped at the widest colour, as the
+    host does): staging buffers, copy alignment, each group solved once after
+    the colours before it."""
+    A = P.convdiff3d(n, 0.5)
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, bs, False, "connect")
+    L_, U_, _ = S.Split(S.Ilu0(S.Reordering(A, LP, RP)), "L-DU", True)
+    widest = int(np.max(np.diff(np.asarray(sc)) + 31) // 32)
+    f = emu.wf_cp_schedule_s if dtype == np.float32 else emu.wf_cp_schedule_d
+    for F, upper in ((L_, 0), (U_, 1)):
+        keep = [np.ascontiguousarray(a) for a in (F.val.astype(dtype), F.cind, F.rptr, np.asarray(sc, np.int32))]
+        err = C.create_string_buffer(256)
+        rc = f(F.n, _p(keep[0]), _p(keep[1]), _p(keep[2]), upper, _p(keep[3]), nc, bs, min(grid, widest), err, 256)
+        assert rc == 0, err.value.decode()
