@@ -96,6 +96,32 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Barrier `id` (1..15) over the first `nthreads` threads of the CTA (a multiple
+// of 32); returns whether any of them passed v = true.
+__device__ __forceinline__ bool named_bar_or(int id, int nthreads, bool v)
+{
+    int r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.s32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.s32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((int)v), "r"(id), "r"(nthreads)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void named_bar(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // One bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16);
 // completion is counted on `bar`.
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
@@ -158,6 +184,51 @@ __device__ __forceinline__ T block_sum(T v, T *sh)
     }
     __syncthreads();
     return r;
+}
+
+// Sum of the grid's partials p[0..P), by every thread of the (last) CTA; the
+// total is returned in thread 0, as block_sum. Thread t adds p[t],
+// p[t + blockDim.x], ... into eight independent sums, so its loads are in
+// flight together instead of one memory latency apart. The order of the
+// additions depends only on P and the block size.
+__device__ __forceinline__ double cta_sum_partials(const double *p, int P, double *sh)
+{
+    double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int S = blockDim.x;
+    int i = threadIdx.x;
+    for (; i + 7 * S < P; i += 8 * S) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] += __ldcg(p + i + u * S);
+    }
+    for (; i < P; i += S) a[0] += __ldcg(p + i);
+    return block_sum(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])), sh);
+}
+
+// Per-column totals of the grid's partials part[k * P + p] (k < nv), by every
+// thread of the (last) CTA: one column uses the whole CTA (cta_sum_partials),
+// several take a warp each, every lane with eight independent sums.
+// store(k, total) runs once per column. Fixed order for given P, nv and block.
+template <typename F>
+__device__ __forceinline__ void cta_sum_columns(const double *part, int P, int nv, double *sh, F store)
+{
+    if (nv == 1) {
+        const double s = cta_sum_partials(part, P, sh);
+        if (threadIdx.x == 0) store(0, s);
+        return;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = wid; k < nv; k += nw) {
+        const double *p = part + (long long)k * P;
+        double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        int i = lane;
+        for (; i + 7 * 32 < P; i += 256) {
+#pragma unroll
+            for (int u = 0; u < 8; u++) a[u] += __ldcg(p + i + 32 * u);
+        }
+        for (; i < P; i += 32) a[0] += __ldcg(p + i);
+        const double s = warp_sum(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])));
+        if (lane == 0) store(k, s);
+    }
 }
 
 // "Last CTA finishes" protocol for grid-wide reductions without a second launch.

@@ -25,7 +25,8 @@
 namespace senkgpu {
 
 // 64-bit hash of a list of byte ranges: each 1 MiB chunk is hashed on its own
-// (multiply-xorshift over 8-byte words, in parallel over chunks), then the
+// (multiply-xorshift over 8-byte words in four independent lanes, so a core
+// keeps four multiplies in flight; chunks in parallel), then the lanes and the
 // chunk hashes are combined in order, so the result does not depend on the
 // number of threads.
 inline uint64_t content_hash(const std::vector<std::pair<const void *, size_t>> &ranges)
@@ -47,16 +48,30 @@ inline uint64_t content_hash(const std::vector<std::pair<const void *, size_t>> 
         const Piece pc = pieces[i];
         uint64_t x = 0x243F6A8885A308D3ull ^ pc.n;
         if (pc.p) {
+            uint64_t l[4] = {x, x ^ 0xA4093822299F31D0ull, x ^ 0x082EFA98EC4E6C89ull, x ^ 0x452821E638D01377ull};
             size_t k = 0;
+            for (; k + 32 <= pc.n; k += 32) {
+                uint64_t w[4];
+                std::memcpy(w, pc.p + k, 32);
+                for (int q = 0; q < 4; q++) {
+                    l[q] = (l[q] ^ w[q]) * 0x9E3779B97F4A7C15ull;
+                    l[q] ^= l[q] >> 29;
+                }
+            }
             for (; k + 8 <= pc.n; k += 8) {
                 uint64_t w;
                 std::memcpy(&w, pc.p + k, 8);
-                x = (x ^ w) * 0x9E3779B97F4A7C15ull;
-                x ^= x >> 29;
+                l[0] = (l[0] ^ w) * 0x9E3779B97F4A7C15ull;
+                l[0] ^= l[0] >> 29;
             }
             uint64_t w = 0;
             std::memcpy(&w, pc.p + k, pc.n - k);
-            x = (x ^ w) * 0x9E3779B97F4A7C15ull;
+            x = l[0] ^ w;
+            for (int q = 1; q < 4; q++) {
+                x = (x ^ l[q]) * 0x9E3779B97F4A7C15ull;
+                x ^= x >> 32;
+            }
+            x = x * 0x9E3779B97F4A7C15ull;
             x ^= x >> 32;
         }
         h[i] = x;

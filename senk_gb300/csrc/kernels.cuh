@@ -71,11 +71,8 @@ k_spmv_csr(const MT *__restrict__ val, const int *__restrict__ cind, const int *
         double t = block_sum(nacc, sh);
         if (threadIdx.x == 0) part[blockIdx.x] = t;
         if (last_cta_arrives(ticket, gridDim.x)) {
-            double s = 0;
-            if (threadIdx.x < 32) {
-                for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) s += part[i];
-                s = warp_sum(s);
-            }
+            __shared__ double shp[32];
+            const double s = cta_sum_partials(part, gridDim.x, shp);
             if (threadIdx.x == 0) {
                 double r = sqrt(s);
                 *norm_out = r;
@@ -158,9 +155,7 @@ k_residual_sell32(const T *__restrict__ val, const int *__restrict__ col, const 
     const double t = block_sum(nacc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double s = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += part[i];
-        s = block_sum(s, sh);
+        const double s = cta_sum_partials(part, gridDim.x, sh);
         if (threadIdx.x == 0) {
             const double nr = sqrt(s);
             *norm_out = nr;
@@ -332,16 +327,11 @@ k_multidot(const XT *__restrict__ V, long long ldv, int nv, const XT *__restrict
     }
     const unsigned total = gridDim.x * gridDim.y;
     if (last_cta_arrives(ticket, total)) {
-        const int P = gridDim.x;
-        for (int k = wid; k < nv; k += blockDim.x >> 5) {
-            double s = 0;
-            for (int p = lane; p < P; p += 32) s += part[(long long)k * P + p];
-            s = warp_sum(s);
-            if (lane == 0) {
-                coef[k] = s;
-                if (hcol) hcol[k] = ACCUM ? hcol[k] + s : s;
-            }
-        }
+        __shared__ double shp[32];
+        cta_sum_columns(part, gridDim.x, nv, shp, [&](int k, double s) {
+            coef[k] = s;
+            if (hcol) hcol[k] = ACCUM ? hcol[k] + s : s;
+        });
     }
 }
 
@@ -411,16 +401,11 @@ k_multidot_v(const XT *__restrict__ V, long long ldv, int nv, const XT *__restri
     }
     const unsigned total = gridDim.x * gridDim.y;
     if (last_cta_arrives(ticket, total)) {
-        const int P = gridDim.x;
-        for (int k = wid; k < nv; k += blockDim.x >> 5) {
-            double s = 0;
-            for (int p = lane; p < P; p += 32) s += part[(long long)k * P + p];
-            s = warp_sum(s);
-            if (lane == 0) {
-                coef[k] = s;
-                if (hcol) hcol[k] = ACCUM ? hcol[k] + s : s;
-            }
-        }
+        __shared__ double shp[32];
+        cta_sum_columns(part, gridDim.x, nv, shp, [&](int k, double s) {
+            coef[k] = s;
+            if (hcol) hcol[k] = ACCUM ? hcol[k] + s : s;
+        });
     }
 }
 
@@ -517,11 +502,8 @@ k_update(const XT *__restrict__ V, long long ldv, int nv, const double *__restri
     double t = block_sum((double)nacc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double s = 0;
-        if (threadIdx.x < 32) {
-            for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) s += part[i];
-            s = warp_sum(s);
-        }
+        __shared__ double shp[32];
+        const double s = cta_sum_partials(part, gridDim.x, shp);
         if (threadIdx.x == 0) {
             const double hn = sqrt(s);
             if (norm_out) *norm_out = hn;
@@ -573,11 +555,8 @@ k_update_v(const XT *__restrict__ V, long long ldv, int nv, const double *__rest
     double t = block_sum((double)nacc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double s = 0;
-        if (threadIdx.x < 32) {
-            for (int i2 = threadIdx.x; i2 < (int)gridDim.x; i2 += 32) s += part[i2];
-            s = warp_sum(s);
-        }
+        __shared__ double shp[32];
+        const double s = cta_sum_partials(part, gridDim.x, shp);
         if (threadIdx.x == 0) {
             const double hn = sqrt(s);
             if (norm_out) *norm_out = hn;
@@ -872,13 +851,15 @@ __device__ __forceinline__ void small_stage(const SmallFactor<VT> &F, bool upper
 
 // Both triangular sweeps of one ILU application y = U^-1 L^-1 x for a system
 // whose vector fits in shared memory, in one CTA (which: bit 0 L, bit 1 U;
-// x == y allowed). The levels (colours) run in order with a barrier between
-// them, one thread per row; each level's data is staged by TMA into one of
-// nbuf buffers (2 to 8), nbuf - 1 levels ahead of the level being solved.
-// Thread 0 issues the copies; the level descriptor it needs is loaded one step
-// before, so no global load lies on the path from one level to the next. A TMA
-// wait that runs out sets *status = 2 and the kernel leaves after waiting once
-// more for every copy it has issued.
+// x == y allowed). The levels (colours) run in order, one consumer thread per
+// row, with a barrier among the consumers between levels. The last warp stages:
+// its first lane copies each level's data by TMA into one of nbuf buffers (2 to
+// 8) as soon as the consumers have released that buffer (full / empty
+// mbarriers per buffer), so up to nbuf levels are in flight ahead of the one
+// being solved and no staging work lies on the consumers' path. A wait that
+// runs out sets *status = 2 and a shared abort flag; the other side stops at
+// its next wait, and the stager waits (bounded) for every copy it issued
+// before it leaves.
 constexpr int kSmallMaxBufs = 8;
 
 template <typename VT, typename XT>
@@ -887,49 +868,71 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
             int *status, int buf_bytes, int nbuf)
 {
     extern __shared__ __align__(128) unsigned char sms[];
-    __shared__ __align__(8) unsigned long long bar[kSmallMaxBufs];
+    __shared__ __align__(8) unsigned long long full[kSmallMaxBufs], empty[kSmallMaxBufs];
     __shared__ int4 lsh[kSmallMaxBufs];  // descriptor of the level staged in each buffer
+    __shared__ int abort_flag;
     if (gated(gate)) return;
     XT *ysh = reinterpret_cast<XT *>(sms);
     unsigned char *bufs = sms + ((size_t)n * sizeof(XT) + 127) / 128 * 128;
     const int nl = (which & 1) ? Lf.ncolours : 0, nu = (which & 2) ? Uf.ncolours : 0, steps = nl + nu;
-    auto desc = [&](int j) { return j < nl ? __ldg(Lf.levels + j) : __ldg(Uf.levels + (j - nl)); };
-    // step j uses buffer j % nbuf, its (j / nbuf)-th use: phase parity (j / nbuf) & 1
-    auto stage = [&](int j, int4 lv) {
-        const int b = j % nbuf;
-        lsh[b] = lv;
-        unsigned char *buf = bufs + (size_t)b * buf_bytes;
-        if (j < nl) small_stage(Lf, false, lv, buf, &bar[b]);
-        else small_stage(Uf, true, lv, buf, &bar[b]);
-    };
-    int4 dn = make_int4(0, 0, 0, 0);  // thread 0: descriptor of the next level to stage
+    const int ncons = (int)blockDim.x - 32;  // consumer threads; the last warp stages
     if (threadIdx.x == 0) {
-        for (int b = 0; b < nbuf; b++) mbar_init(&bar[b], 1);
-        for (int j = 0; j < nbuf - 1 && j < steps; j++) stage(j, desc(j));
-        if (nbuf - 1 < steps) dn = desc(nbuf - 1);
+        for (int b = 0; b < nbuf; b++) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], 1);
+        }
+        abort_flag = 0;
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) ysh[i] = x[i];
     __syncthreads();
-    for (int k = 0; k < steps; k++) {
-        const int b = k % nbuf;
-        // the buffer of step k - 1 is free again (the barrier at its end)
-        if (threadIdx.x == 0 && k + nbuf - 1 < steps) {
-            stage(k + nbuf - 1, dn);
-            if (k + nbuf < steps) dn = desc(k + nbuf);
+    if ((int)threadIdx.x >= ncons) {
+        if ((int)threadIdx.x != ncons) return;
+        // stager: step j fills buffer b = j % nbuf for its (j / nbuf)-th time
+        int issued = 0;
+        unsigned epar = 0u;  // bit b: parity of buffer b's next release
+        for (int j = 0, b = 0; j < steps; j++, b = b + 1 == nbuf ? 0 : b + 1) {
+            if (j >= nbuf) {  // released by the consumers after step j - nbuf
+                const unsigned par = (epar >> b) & 1u;
+                epar ^= 1u << b;
+                bool got = false;
+                for (unsigned i = 0; i < kWaitLimit && !got; i++) {
+                    got = mbar_try_wait(&empty[b], par);
+                    if (!got && *(volatile int *)&abort_flag) break;
+                }
+                if (!got) {
+                    if (!*(volatile int *)&abort_flag) {
+                        atomicExch(status, 2);
+                        *(volatile int *)&abort_flag = 1;
+                    }
+                    break;
+                }
+            }
+            const int4 lv = j < nl ? __ldg(Lf.levels + j) : __ldg(Uf.levels + (j - nl));
+            lsh[b] = lv;
+            unsigned char *buf = bufs + (size_t)b * buf_bytes;
+            if (j < nl) small_stage(Lf, false, lv, buf, &full[b]);
+            else small_stage(Uf, true, lv, buf, &full[b]);
+            issued = j + 1;
         }
+        // the last use of each buffer: complete (consumed or not) before the CTA leaves
+        for (int j = issued > nbuf ? issued - nbuf : 0; j < issued; j++)
+            mbar_wait_bounded(&full[j % nbuf], (unsigned)(j / nbuf) & 1u, kWaitLimit);
+        return;
+    }
+    unsigned fpar = 0u;  // bit b: parity of buffer b's next fill
+    for (int k = 0, b = 0; k < steps; k++, b = b + 1 == nbuf ? 0 : b + 1) {
         const bool upper = k >= nl;
-        const unsigned par = (unsigned)(k / nbuf) & 1u;
-        const bool ok = mbar_wait_bounded(&bar[b], par, kWaitLimit);
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
+        bool ok = mbar_wait_bounded(&full[b], (fpar >> b) & 1u, kWaitLimit);
+        fpar ^= 1u << b;
+        if (ok && *(volatile int *)&abort_flag) ok = false;
+        if (named_bar_or(1, ncons, !ok)) {
+            if (threadIdx.x == 0 && !*(volatile int *)&abort_flag) {
                 atomicExch(status, 2);
-                // every copy still in flight: steps k .. k + nbuf - 1
-                for (int j = k; j < steps && j < k + nbuf; j++)
-                    mbar_wait_bounded(&bar[j % nbuf], (unsigned)(j / nbuf) & 1u, kWaitLimit);
+                *(volatile int *)&abort_flag = 1;
             }
             return;
         }
-        // written by thread 0 before the barrier that ended step k - nbuf + 1 (or the first one)
+        // written by the stager before the copies it counted on full[b]
         const int4 lv = lsh[b];
         const int G = lv.y, e0 = lv.z, ne = lv.w;
         const unsigned char *sb = bufs + (size_t)b * buf_bytes;
@@ -938,7 +941,7 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
         const int *scol = reinterpret_cast<const int *>(sb + G * 16 + G * 256);
         const VT *sval = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * 4);
         const VT *sdinv = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * (4 + sizeof(VT)));
-        for (int t = threadIdx.x; t < G * 32; t += blockDim.x) {
+        for (int t = threadIdx.x; t < G * 32; t += ncons) {
             const int gi = t >> 5, lane = t & 31;
             const WfGroup d = sd[gi];
             if (lane >= d.nchains) continue;
@@ -950,9 +953,10 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
             if (upper) tt *= (XT)sdinv[t];
             ysh[row] = tt;
         }
-        __syncthreads();
+        named_bar(1, ncons);  // the level's rows are final and buffer b is free
+        if (threadIdx.x == 0) mbar_arrive(&empty[b]);
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = ysh[i];
+    for (int i = threadIdx.x; i < n; i += ncons) y[i] = ysh[i];
 }
 
 // ------------------------------------------------------ dataflow sweeps
@@ -995,6 +999,11 @@ __device__ __forceinline__ int ld_acquire(const int *p)
 __device__ __forceinline__ void st_release(int *p, int v)
 {
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void red_release_add(int *p, int v)
+{
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 template <typename T>
@@ -1456,20 +1465,21 @@ k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, 
             k ^= 1;
         }
         if (!ok || c + 1 == ncolours) break;
-        // grid barrier: this CTA's rows of colour c are written
+        // grid barrier: this CTA's rows of colour c are written (ordered before
+        // thread 0's release by the CTA barrier); the acquire that sees the
+        // last arrival orders the next colour's reads after every CTA's rows
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(ctrl, 1);
+            red_release_add(ctrl, 1);
             const int target = (c + 1) * (int)gridDim.x;
             int good = 1;
             unsigned polls = 0;
             while (ld_acquire(ctrl) < target) {
-                if (ld_acquire(ctrl + 2)) {
+                if ((++polls & 63u) == 0 && *(volatile const int *)(ctrl + 2)) {
                     good = 0;
                     break;
                 }
-                if (++polls > 64u) __nanosleep(32);
+                if (polls > 1024u) __nanosleep(32);
                 if (polls > kFlagPolls) {
                     atomicExch(ctrl + 2, 1);
                     atomicExch(status, 1);
@@ -1477,7 +1487,6 @@ k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, 
                     break;
                 }
             }
-            __threadfence();
             s_ok = good;
         }
         __syncthreads();

@@ -124,9 +124,7 @@ k_bicg_xr(KrylovState *st, T *x, const T *Kp, const T *Ks, const T *AKs, const T
     const double t = block_sum(nacc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double sum = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) sum += part[i];
-        sum = block_sum(sum, sh);
+        const double sum = cta_sum_partials(part, gridDim.x, sh);
         if (threadIdx.x == 0) {
             const double nr = sqrt(sum);
             st->s[kOmega] = omega;

@@ -59,9 +59,7 @@ __global__ void __launch_bounds__(kThreads) k_rms(const T *r, long long n, doubl
     s = block_sum(s, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double t = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += part[i];
-        t = block_sum(t, sh);
+        const double t = cta_sum_partials(part, gridDim.x, sh);
         if (threadIdx.x == 0) {
             const double rms = sqrt(t / (double)n);
             out[0] = (float)rms;
@@ -156,9 +154,7 @@ k_target(const T *e, const T *ilu, const float *rms, float d, float *t, long lon
     s = block_sum(s, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double u = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) u += part[i];
-        u = block_sum(u, sh);
+        const double u = cta_sum_partials(part, gridDim.x, sh);
         if (threadIdx.x == 0) acc[0] = u;
     }
 }
@@ -287,13 +283,8 @@ k_step_alpha(const double *r, const double *au, const double *y, long long n, do
         part[gridDim.x + blockIdx.x] = b;
     }
     if (last_cta_arrives(ticket, gridDim.x)) {
-        double ta = 0, tb = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-            ta += part[i];
-            tb += part[gridDim.x + i];
-        }
-        ta = block_sum(ta, sh);
-        tb = block_sum(tb, sh);
+        const double ta = cta_sum_partials(part, gridDim.x, sh);
+        const double tb = cta_sum_partials(part + gridDim.x, gridDim.x, sh);
         if (threadIdx.x == 0) *alpha = tb > 0 ? ta / tb : 0.0;
     }
 }

@@ -580,8 +580,9 @@ void IluPlan<VT>::sweep_small(int which, const VT *x, VT *y, cudaStream_t s, con
                                (int)F.colour_groups.size() - 1};
     };
     const size_t smem = ((size_t)n * sizeof(VT) + 127) / 128 * 128 + (size_t)small_nbuf * small_buf;
-    k_ilu_small<VT, VT><<<1, small_threads, smem, s>>>(mk(L), mk(U), which, x, y, n, gate, status.p, (int)small_buf,
-                                                       small_nbuf);
+    // small_threads consumers and one staging warp
+    k_ilu_small<VT, VT><<<1, small_threads + 32, smem, s>>>(mk(L), mk(U), which, x, y, n, gate, status.p,
+                                                            (int)small_buf, small_nbuf);
     SENK_LAUNCH_CHECK();
 }
 
@@ -626,7 +627,7 @@ void IluPlan<VT>::build_small(int N, const VT *lval, const int *lcind, const int
     for (const SweepFactor<VT> *F : {&L, &U})
         for (size_t c = 0; c + 1 < F->colour_groups.size(); c++)
             most = std::max(most, (F->colour_groups[c + 1] - F->colour_groups[c]) * 32);
-    small_threads = std::min(1024, (most + 31) / 32 * 32);
+    small_threads = std::min(992, (most + 31) / 32 * 32);
     small_buf = (std::max(L.level_bytes, U.level_bytes) + 127) / 128 * 128;
     const size_t vec = ((size_t)N * sizeof(VT) + 127) / 128 * 128;
     if (vec + 2 * small_buf > kSmallSmem) return;  // a level too large to stage next to the vector
