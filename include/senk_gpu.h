@@ -87,11 +87,13 @@ typedef struct {
 #define SENK_SWEEP_COMPACT 3  /* compact chain layout (chains packed per lane,
                                  padding only to the widest chain of a group), one
                                  launch per colour, one CTA per group */
-#define SENK_SWEEP_PERSISTENT 4 /* compact chain layout, one cooperative launch per
-                                 sweep: the CTAs take the groups of a colour in
-                                 turn, a grid barrier separates the colours, and
-                                 each group's block is staged while the group
-                                 before it is solved */
+#define SENK_SWEEP_PERSISTENT 4 /* compact chain layout; every run of consecutive
+                                 colours whose groups fit one wave of co-resident
+                                 CTAs sweeps in one cooperative launch (the CTAs
+                                 take the groups of a colour in turn, a grid
+                                 barrier separates the colours, each group's block
+                                 is staged while the group before it is solved);
+                                 wider colours keep one launch each */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0
@@ -484,7 +486,8 @@ int senk_ilu_plan_status(senk_ilu_plan *plan, void *stream);
  * L, 1: U) wait on its own flag, which is never set before the group runs, so
  * its bounded wait runs out (about a second) on the next sweep. For the
  * cooperative sweep (SENK_SWEEP_PERSISTENT; `group` ignored) the first grid
- * barrier of the next sweep waits for more arrivals than there are CTAs. The
+ * barrier of the sweep's first cooperative launch waits for more arrivals than
+ * there are CTAs. The
  * plan keeps this defect; destroy it afterwards. */
 int senk_ilu_plan_test_stall(senk_ilu_plan *plan, int upper, int group);
 int senk_ilu_plan_destroy(senk_ilu_plan *plan);
@@ -586,6 +589,33 @@ int senk_setup_ilup(double **val, int **cind, int **rptr, int N, int p);
 int senk_setup_alloc_level_zero(double **val, int **cind, int **rptr, int N, int p);
 /* senk::matrix::RemoveOffDiagonal<double> (include/senk_matrix.hpp:668-689) */
 int senk_setup_remove_off_diagonal(double **val, int **cind, int **rptr, int N, int bnum);
+/* senk::io::ReadMatrixMarket (include/senk_io.hpp:41-103): CSR of the file's
+ * entries (a symmetric file's stored triangle; *symmetric = 1), rows sorted by
+ * column; SENK_ERR_ARG (with the reason) for a file the reader rejects. */
+int senk_io_read_matrix_market(const char *filename, double **val, int **cind, int **rptr, int *N, int *M,
+                               int *symmetric, int remove_zeros);
+/* senk::matrix::Expand<double> (include/senk_matrix.hpp:336-370): the full
+ * matrix from its stored triangle, key "L" or "U" */
+int senk_setup_expand(const double *tval, const int *tcind, const int *trptr, double **val, int **cind,
+                      int **rptr, int N, const char *key);
+
+/* ============================================= device diagonal scaling ==
+ * The reference's GetDiag / Scaling (include/senk_matrix.hpp:391-416) on a CSR
+ * matrix in device memory, and the symmetric scaling its driver applies
+ * (main.cpp:65-73: d_i = 1 / sqrt|a_ii|, a_ij <- d_i a_ij d_j). Each value is
+ * (ld[i] * a_ij) * rd[j], two roundings in the reference's order, so results
+ * equal the host functions' bit for bit. A row without a diagonal entry gets
+ * diag 0 (the reference leaves it unset). Asynchronous on `stream`. */
+int senk_dev_get_diag_d(const double *val, const int *cind, const int *rptr, double *diag, int N, void *stream);
+int senk_dev_get_diag_s(const float *val, const int *cind, const int *rptr, float *diag, int N, void *stream);
+int senk_dev_scaling_d(double *val, const int *cind, const int *rptr, const double *ld, const double *rd, int N,
+                       void *stream);
+int senk_dev_scaling_s(float *val, const int *cind, const int *rptr, const float *ld, const float *rd, int N,
+                       void *stream);
+/* GetDiag, d = 1 / sqrt|d|, Scaling(d, d); `d` (N entries, device) receives the
+ * scaling factors. */
+int senk_dev_diag_scaling_d(double *val, const int *cind, const int *rptr, double *d, int N, void *stream);
+int senk_dev_diag_scaling_s(float *val, const int *cind, const int *rptr, float *d, int N, void *stream);
 
 #ifdef __cplusplus
 }

@@ -248,6 +248,58 @@ class _Lib:
         D = _take(self, d, N, np.float64) if d else None
         return L, U, D
 
+    def get_diag(self, A):
+        if self.prefix == "oracle_":
+            f = self.fn("get_diag", [_P, _P, _P, _P, _I])
+            d = np.zeros(A.n)
+            f(_ptr(np.ascontiguousarray(A.val, np.float64)), _ptr(_i32(A.cind)), _ptr(_i32(A.rptr)), _ptr(d), A.n)
+            return d
+        f = self.fn("get_diag", [_P, _P, _P, _P, _I])
+        dp = _P()
+        f(_ptr(np.ascontiguousarray(A.val, np.float64)), _ptr(_i32(A.cind)), _ptr(_i32(A.rptr)), C.byref(dp), A.n)
+        return _take(self, dp.value, A.n, np.float64)
+
+    def scaling(self, A, ld, rd):
+        f = self.fn("scaling", [_P, _P, _P, _P, _P, _I])
+        val = np.array(A.val, np.float64)
+        ld, rd = np.ascontiguousarray(ld, np.float64), np.ascontiguousarray(rd, np.float64)
+        f(_ptr(val), _ptr(_i32(A.cind)), _ptr(_i32(A.rptr)), _ptr(ld), _ptr(rd), A.n)
+        return type(A)(val, A.cind.copy(), A.rptr.copy())
+
+    def expand(self, A, key="L"):
+        v, c, r = _P(), _P(), _P()
+        args = (_ptr(np.ascontiguousarray(A.val, np.float64)), _ptr(_i32(A.cind)), _ptr(_i32(A.rptr)),
+                C.byref(v), C.byref(c), C.byref(r), A.n)
+        if self.prefix == "oracle_":
+            f = self.fn("expand", [_P, _P, _P, _P, _P, _P, _I, C.c_char], _I)
+            if f(*args, key.encode()) != 0:
+                raise ValueError("expand: key must be L or U")
+        else:
+            self.fn("expand", [_P, _P, _P, _P, _P, _P, _I, C.c_char_p])(*args, key.encode())
+        rp = _take(self, r.value, A.n + 1, np.int32)
+        nnz = int(rp[-1])
+        return type(A)(_take(self, v.value, nnz, np.float64), _take(self, c.value, nnz, np.int32), rp)
+
+    def read_matrix_market(self, path, remove_zeros=True):
+        """(val, cind, rptr, N, M, symmetric) of the file, or None if rejected."""
+        v, c, r = _P(), _P(), _P()
+        n, m, sym = C.c_int(0), C.c_int(0), C.c_int(0)
+        args = [str(path).encode(), C.byref(v), C.byref(c), C.byref(r), C.byref(n), C.byref(m), C.byref(sym),
+                int(remove_zeros)]
+        if self.prefix == "oracle_":
+            f = self.fn("read_matrix_market", [C.c_char_p, _P, _P, _P, _P, _P, _P, _I], _I)
+            ret = f(*args)
+        else:
+            f = self.fn("read_matrix_market", [C.c_char_p, _P, _P, _P, _P, _P, _P, _I, C.c_char_p, _I], _I)
+            self.last_stdout = C.create_string_buffer(1 << 16)
+            ret = f(*args, self.last_stdout, 1 << 16)
+        if ret != 0:
+            return None
+        rp = _take(self, r.value, n.value + 1, np.int32)
+        nnz = int(rp[-1])
+        return (_take(self, v.value, nnz, np.float64), _take(self, c.value, nnz, np.int32), rp, n.value, m.value,
+                bool(sym.value))
+
     def csr2bcsr(self, A, bnl, bnw):
         f = self.fn("csr2bcsr", [_P, _P, _P, _P, _P, _P, _I, _I, _I], _I if self.prefix == "oracle_" else None)
         bv, bc, br = _P(), _P(), _P()

@@ -215,6 +215,18 @@ void ref_amc_permutation(int *c, int *r, int *nc, int **sc, int **LP, int **RP, 
 { senk::graph::GetAMCPermutation(c, r, nc, sc, LP, RP, N, sym != 0); }
 void ref_abmc_permutation(int *c, int *r, int *nc, int **sc, int **LP, int **RP, int N, int bs, int sym, const char *method)
 { senk::graph::GetABMCPermutation(c, r, nc, sc, LP, RP, N, bs, sym != 0, method); }
+void ref_expand(double *tv, int *tc, int *tr, double **v, int **c, int **r, int N, const char *key)
+{ senk::matrix::Expand<double>(tv, tc, tr, v, c, r, N, key); }
+// senk::io::ReadMatrixMarket; its stdout lines go to `out`; returns its result
+int ref_read_matrix_market(const char *path, double **v, int **c, int **r, int *N, int *M, int *sym, int rz,
+                           char *out, int cap)
+{
+    bool ok = false;
+    senk::io::Shape shape = senk::io::Unsym;
+    capture_stdout(out, cap, [&] { ok = senk::io::ReadMatrixMarket(path, v, c, r, N, M, &shape, rz != 0); });
+    *sym = shape == senk::io::Sym ? 1 : 0;
+    return ok ? 0 : -1;
+}
 void ref_relative_residual(double *v, int *c, int *r, double *b, double *x, int N, char *out, int cap)
 { capture_stdout(out, cap, [&] { senk::test::RelativeResidualError(v, c, r, b, x, N); }); }
 

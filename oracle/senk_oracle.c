@@ -289,6 +289,101 @@ int oracle_split(const double *val, const int *cind, const int *rptr,
     return 0;
 }
 
+/* include/senk_matrix.hpp:335-371  Expand: full matrix from the stored
+ * triangle (key 'L': lower incl. diagonal stored; 'U': upper). Row i takes the
+ * lower-oriented row's entries, then the upper-oriented row's entries after
+ * its first (the diagonal). Returns -1 for another key. */
+int oracle_expand(const double *tval, const int *tcind, const int *trptr,
+                  double **val, int **cind, int **rptr, int N, char key)
+{
+    if (key != 'L' && key != 'U') return -1;
+    double *cv; int *cr, *cp;
+    oracle_csr2csc(tval, tcind, trptr, &cv, &cr, &cp, N, N);
+    const double *lv = key == 'L' ? tval : cv, *uv = key == 'L' ? cv : tval;
+    const int *lc = key == 'L' ? tcind : cr, *uc = key == 'L' ? cr : tcind;
+    const int *lr = key == 'L' ? trptr : cp, *ur = key == 'L' ? cp : trptr;
+    int nnz = trptr[N] * 2 - N;
+    *val = (double *)malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+    *cind = (int *)malloc(sizeof(int) * (nnz > 0 ? nnz : 1));
+    *rptr = (int *)malloc(sizeof(int) * (N + 1));
+    int at = 0;
+    (*rptr)[0] = 0;
+    for (int i = 0; i < N; i++) {
+        for (int j = lr[i]; j < lr[i + 1]; j++) { (*val)[at] = lv[j]; (*cind)[at] = lc[j]; at++; }
+        for (int j = ur[i] + 1; j < ur[i + 1]; j++) { (*val)[at] = uv[j]; (*cind)[at] = uc[j]; at++; }
+        (*rptr)[i + 1] = at;
+    }
+    free(cv); free(cr); free(cp);
+    return 0;
+}
+
+/* include/senk_io.hpp:41-103  ReadMatrixMarket: header with "symmetric"
+ * (*sym = 1) or "general" (0), not "complex"; '%' lines skipped up to the
+ * size line "N M PE"; PE triples "row col value" (1-based), zero values dropped
+ * when remove_zeros; CSR with rows in order and each row sorted by column
+ * (entries of equal row and column keep file order here). Returns -1 for a
+ * file the reference would reject or read out of bounds. */
+int oracle_read_matrix_market(const char *path, double **val, int **cind, int **rptr,
+                              int *N, int *M, int *sym, int remove_zeros)
+{
+    FILE *f = fopen(path, "r");
+    if (!f) return -1;
+    char line[4096];
+    if (!fgets(line, sizeof line, f) || strstr(line, "complex")) { fclose(f); return -1; }
+    if (strstr(line, "symmetric")) *sym = 1;
+    else if (strstr(line, "general")) *sym = 0;
+    else { fclose(f); return -1; }
+    long long n = -1, m = -1, pe = -1;
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '%') continue;
+        if (sscanf(line, "%lld %lld %lld", &n, &m, &pe) != 3) n = -1;
+        break;
+    }
+    if (n < 0 || m < 0 || pe < 0) { fclose(f); return -1; }
+    int *row = (int *)malloc(sizeof(int) * (pe > 0 ? pe : 1));
+    int *col = (int *)malloc(sizeof(int) * (pe > 0 ? pe : 1));
+    double *v = (double *)malloc(sizeof(double) * (pe > 0 ? pe : 1));
+    long long k = 0;
+    for (long long e = 0; e < pe; e++) {
+        long long r, c;
+        double x;
+        if (fscanf(f, "%lld %lld %lf", &r, &c, &x) != 3 || r < 1 || r > n || c < 1 || c > m) {
+            free(row); free(col); free(v); fclose(f);
+            return -1;
+        }
+        if (remove_zeros && x == 0) continue;
+        row[k] = (int)(r - 1); col[k] = (int)(c - 1); v[k] = x; k++;
+    }
+    fclose(f);
+    *N = (int)n;
+    *M = (int)m;
+    *rptr = (int *)calloc((size_t)n + 1, sizeof(int));
+    *cind = (int *)malloc(sizeof(int) * (k > 0 ? k : 1));
+    *val = (double *)malloc(sizeof(double) * (k > 0 ? k : 1));
+    for (long long e = 0; e < k; e++) (*rptr)[row[e] + 1]++;
+    for (long long i = 0; i < n; i++) (*rptr)[i + 1] += (*rptr)[i];
+    int *at = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+    memcpy(at, *rptr, sizeof(int) * ((size_t)n + 1));
+    for (long long e = 0; e < k; e++) {
+        int p = at[row[e]]++;
+        (*cind)[p] = col[e];
+        (*val)[p] = v[e];
+    }
+    /* insertion sort of each row by column (stable) */
+    for (long long i = 0; i < n; i++) {
+        for (int j = (*rptr)[i] + 1; j < (*rptr)[i + 1]; j++) {
+            int c = (*cind)[j];
+            double x = (*val)[j];
+            int q = j - 1;
+            while (q >= (*rptr)[i] && (*cind)[q] > c) { (*cind)[q + 1] = (*cind)[q]; (*val)[q + 1] = (*val)[q]; q--; }
+            (*cind)[q + 1] = c;
+            (*val)[q + 1] = x;
+        }
+    }
+    free(at); free(row); free(col); free(v);
+    return 0;
+}
+
 /* include/senk_matrix.hpp:391-404  GetDiag */
 void oracle_get_diag(const double *val, const int *cind, const int *rptr, double *diag, int N)
 {

@@ -8,6 +8,7 @@
 
 #include "../../include/senk_gpu.h"
 #include "../../include/senk_graph.hpp"
+#include "../../include/senk_io.hpp"
 #include "../../include/senk_matrix.hpp"
 
 namespace senkgpu {
@@ -115,6 +116,35 @@ int senk_setup_csr2bcsr(const double *val, const int *cind, const int *rptr, dou
     }
     senk::matrix::Csr2Bcsr<double>(const_cast<double *>(val), const_cast<int *>(cind), const_cast<int *>(rptr), bval,
                                    bcind, brptr, N, bnl, bnw);
+    return SENK_OK;
+}
+
+int senk_io_read_matrix_market(const char *filename, double **val, int **cind, int **rptr, int *N, int *M,
+                               int *symmetric, int remove_zeros)
+{
+    if (!filename || !val || !cind || !rptr || !N || !M || !symmetric) {
+        set_last_error("senk_io_read_matrix_market: null argument");
+        return SENK_ERR_ARG;
+    }
+    senk::io::Shape shape = senk::io::Unsym;
+    if (!senk::io::ReadMatrixMarket(filename, val, cind, rptr, N, M, &shape, remove_zeros != 0)) {
+        set_last_error(std::string("senk_io_read_matrix_market: cannot read ") + filename +
+                       " (message on stderr)");
+        return SENK_ERR_ARG;
+    }
+    *symmetric = shape == senk::io::Sym ? 1 : 0;
+    return SENK_OK;
+}
+
+int senk_setup_expand(const double *tval, const int *tcind, const int *trptr, double **val, int **cind,
+                      int **rptr, int N, const char *key)
+{
+    if (!key || (std::strcmp(key, "L") != 0 && std::strcmp(key, "U") != 0)) {
+        set_last_error("senk_setup_expand: key must be \"L\" or \"U\"");
+        return SENK_ERR_ARG;
+    }
+    senk::matrix::Expand<double>(const_cast<double *>(tval), const_cast<int *>(tcind), const_cast<int *>(trptr), val,
+                                 cind, rptr, N, key);
     return SENK_OK;
 }
 

@@ -178,6 +178,9 @@ struct SweepFactor {
         int g0, g1;        // groups of the colour
         int early_x;       // 1: x is read before the wait on the previous kernel
         size_t smem;       // dynamic shared memory
+        // a cooperative launch (k_sweep_cp) of colours [cbeg, cend) on `grid` CTAs
+        // instead of one colour (k_sweep_cc)
+        int coop = 0, cbeg = 0, cend = 0, grid = 0;
     };
     std::vector<Launch> launches;
     DevBuf<WfGroup> wgroups;
@@ -187,10 +190,10 @@ struct SweepFactor {
     int slots_max = 0;             // widest group block (slots of 32 entries)
     int wf_warps = 0, wf_grid = 0; // warps per CTA, CTAs
     size_t wf_smem = 0;            // dynamic shared memory per CTA
-    // compact, one cooperative launch per sweep (k_sweep_cp): CTAs, bytes of
-    // each of its two staging buffers (ctrl holds its barrier words)
+    // compact: runs of colours that fit one wave of co-resident CTAs sweep in
+    // one cooperative launch each (k_sweep_cp; bytes of each of its two staging
+    // buffers; ctrl holds its barrier words)
     bool persistent = false;
-    int cp_grid = 0;
     size_t cp_buf = 0;
 };
 

@@ -1348,8 +1348,9 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
     if (live) y[row] = tsh[q][l];
 }
 
-// All colours of one sweep in one cooperative launch, on the compact chain
-// layout: CTA b takes groups b, b + gridDim.x, ... of each colour (the group
+// Colours [cbeg, cend) of one sweep in one cooperative launch, on the
+// compact chain layout (all of them, or a run of small colours between
+// per-colour launches): CTA b takes groups b, b + gridDim.x, ... of each colour (the group
 // body of k_sweep_cc), and a grid barrier separates the colours. Each group's
 // block and row counts are staged by TMA into one of two buffers while the
 // group before it is solved, across the barrier too (the blocks are read-only).
@@ -1364,7 +1365,7 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 // last CTA to leave resets ctrl for the next launch.
 template <typename VT, typename XT, int BS, bool UPPER>
 __global__ void __launch_bounds__(BS * 32)
-k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, int ncolours,
+k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, int cbeg, int cend,
            const int2 *__restrict__ chains, const unsigned char *__restrict__ counts, const VT *__restrict__ val,
            const int *__restrict__ col, const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate,
            int *status, int *ctrl, unsigned buf_bytes)
@@ -1399,7 +1400,7 @@ k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, 
     };
     // this CTA's first group in colour c or a later one (-1: none); its colour in *cc
     auto first_from = [&](int c, int *cc) {
-        for (; c < ncolours; c++) {
+        for (; c < cend; c++) {
             const int g = __ldg(cgroups + c) + (int)blockIdx.x;
             if (g < __ldg(cgroups + c + 1)) {
                 *cc = c;
@@ -1412,14 +1413,14 @@ k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, 
     unsigned ph = 0u, pend = 0u;
     int k = 0, cdummy = 0;
     {
-        const int g = first_from(0, &cdummy);
+        const int g = first_from(cbeg, &cdummy);
         if (g >= 0) {
             if (threadIdx.x == 0) stage(g, 0);
             pend = 1u;
         }
     }
     bool ok = true;
-    for (int c = 0; c < ncolours && ok; c++) {
+    for (int c = cbeg; c < cend && ok; c++) {
         const int ge = __ldg(cgroups + c + 1);
         for (int g = __ldg(cgroups + c) + (int)blockIdx.x; g < ge; g += (int)gridDim.x) {
             int cn = c, gn = g + (int)gridDim.x;
@@ -1464,14 +1465,14 @@ k_sweep_cp(const WfGroup *__restrict__ groups, const int *__restrict__ cgroups, 
             if (live) y[row] = tsh[q][l];
             k ^= 1;
         }
-        if (!ok || c + 1 == ncolours) break;
+        if (!ok || c + 1 == cend) break;
         // grid barrier: this CTA's rows of colour c are written (ordered before
         // thread 0's release by the CTA barrier); the acquire that sees the
         // last arrival orders the next colour's reads after every CTA's rows
         __syncthreads();
         if (threadIdx.x == 0) {
             red_release_add(ctrl, 1);
-            const int target = (c + 1) * (int)gridDim.x;
+            const int target = (c - cbeg + 1) * (int)gridDim.x;
             int good = 1;
             unsigned polls = 0;
             while (ld_acquire(ctrl) < target) {

@@ -62,7 +62,9 @@ int senk_ilu_plan_test_stall(senk_ilu_plan *plan, int upper, int group)
         auto stall = [&](auto &P) {
             auto &F = upper ? P.U : P.L;
             if (F.persistent) {
-                SENK_REQUIRE(F.colour_groups.size() > 2, "the sweep has no grid barrier (one colour)");
+                bool barrier = false;
+                for (const auto &L : F.launches) barrier = barrier || (L.coop && L.cend - L.cbeg >= 2);
+                SENK_REQUIRE(barrier, "the sweep has no cooperative launch with a grid barrier");
                 // arrivals start far below any barrier's target
                 const int low = -(1 << 30);
                 SENK_CUDA(cudaMemcpy(F.ctrl.p, &low, sizeof(int), cudaMemcpyHostToDevice));

@@ -393,6 +393,24 @@ template <typename VT, typename XT, int BS, bool UPPER>
 void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
 {
     for (const auto &L : F.launches) {
+        if (L.coop) {
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(L.grid);
+            cfg.blockDim = dim3(BS * 32);
+            cfg.dynamicSmemBytes = L.smem;
+            cfg.stream = s;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeCooperative;
+            at[0].val.cooperative = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cp<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p,
+                                         (const int *)F.dcolour_groups.p, L.cbeg, L.cend, (const int2 *)F.wchains.p,
+                                         (const unsigned char *)F.wcounts.p, (const VT *)F.val.p,
+                                         (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate, status, F.ctrl.p,
+                                         (unsigned)F.cp_buf));
+            continue;
+        }
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3(L.g1 - L.g0);
         cfg.blockDim = dim3(BS * 32);
@@ -419,37 +437,16 @@ void shape_cc(SweepFactor<VT> &F)
                                    (int)std::max<size_t>(most, 48 * 1024)));
 }
 
-// Compact chains, all colours of the sweep in one cooperative launch
-// (k_sweep_cp); ctrl holds its barrier words.
-template <typename VT, typename XT, int BS, bool UPPER>
-void launch_cp(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaStream_t s, const int *gate)
-{
-    if (F.ngroups == 0) return;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(F.cp_grid);
-    cfg.blockDim = dim3(BS * 32);
-    cfg.dynamicSmemBytes = 2 * F.cp_buf;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cp<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p,
-                                 (const int *)F.dcolour_groups.p, (int)F.colour_groups.size() - 1,
-                                 (const int2 *)F.wchains.p, (const unsigned char *)F.wcounts.p, (const VT *)F.val.p,
-                                 (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate, status, F.ctrl.p,
-                                 (unsigned)F.cp_buf));
-}
-
-// Shape of the cooperative sweep: two staging buffers of the widest group's
-// block, as many CTAs as are resident at once but no more than the largest
-// colour's groups. Leaves `persistent` false (per-colour launches) when the
-// buffers do not fit or the device cannot launch cooperatively.
+// Shape of the cooperative launches: two staging buffers of the widest group's
+// block; as many CTAs fit at once as the occupancy allows. Every run of at
+// least two consecutive colours (in processing order) whose groups fit that
+// wave becomes one cooperative launch on as many CTAs as its widest colour has
+// groups; the other colours keep their own launches. Leaves the launch list
+// as it is when the buffers do not fit or the device cannot launch
+// cooperatively.
 template <typename VT, int BS, bool UPPER>
 void shape_cp(SweepFactor<VT> &F)
 {
-    F.persistent = false;
     int coop = 0, dev = 0;
     SENK_CUDA(cudaGetDevice(&dev));
     SENK_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
@@ -464,14 +461,36 @@ void shape_cp(SweepFactor<VT> &F)
     int per_sm = 0;
     SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BS * 32, 2 * buf));
     if (per_sm < 1) return;
-    int widest = 0;
-    for (size_t c = 0; c + 1 < F.colour_groups.size(); c++)
-        widest = std::max(widest, F.colour_groups[c + 1] - F.colour_groups[c]);
+    const int wave = per_sm * sm_count();
+    const int nc = (int)F.colour_groups.size() - 1;
+    auto groups_of = [&](int c) { return F.colour_groups[c + 1] - F.colour_groups[c]; };
+    std::vector<typename SweepFactor<VT>::Launch> out;
+    int c = 0;
+    while (c < nc) {
+        int e = c;
+        int widest = 0;
+        while (e < nc && groups_of(e) <= wave) widest = std::max(widest, groups_of(e++));
+        if (e - c >= 2 && widest > 0) {
+            typename SweepFactor<VT>::Launch L{};
+            L.coop = 1;
+            L.cbeg = c;
+            L.cend = e;
+            L.grid = widest;
+            L.smem = 2 * buf;
+            out.push_back(L);
+            c = e;
+            continue;
+        }
+        if (groups_of(c) > 0) {
+            for (const auto &L : F.launches)
+                if (L.g0 == F.colour_groups[c]) out.push_back(L);
+        }
+        c++;
+    }
+    F.launches = out;
     F.cp_buf = buf;
-    F.cp_grid = std::max(1, std::min(widest, per_sm * sm_count()));
     if (F.ctrl.n < 4) F.ctrl.alloc(4);
     SENK_CUDA(cudaMemset(F.ctrl.p, 0, 4 * sizeof(int)));
-    F.persistent = true;
 }
 
 // Launch shape of a dataflow sweep: as many warps per CTA (up to 8) as the
@@ -528,7 +547,6 @@ void sweep_groups(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cud
 #define SENK_COMPACT_CASE(BS)                                                      \
     case BS:                                                                       \
         if (F.dataflow) launch_wf<VT, XT, BS, UPPER>(F, status, x, y, s, gate);    \
-        else if (F.persistent) launch_cp<VT, XT, BS, UPPER>(F, status, x, y, s, gate); \
         else launch_cc<VT, XT, BS, UPPER>(F, status, x, y, s, gate);               \
         break;
         switch (F.bs) {

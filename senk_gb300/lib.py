@@ -181,6 +181,12 @@ def _declare(L):
     d("senk_setup_ilup", [PP, PP, PP, _I, _I])
     d("senk_setup_alloc_level_zero", [PP, PP, PP, _I, _I])
     d("senk_setup_remove_off_diagonal", [PP, PP, PP, _I, _I])
+    d("senk_io_read_matrix_market", [C.c_char_p, PP, PP, PP, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), _I])
+    d("senk_setup_expand", [_P, _P, _P, PP, PP, PP, _I, C.c_char_p])
+    for sfx in ("d", "s"):
+        d(f"senk_dev_get_diag_{sfx}", [_P, _P, _P, _P, _I, _P])
+        d(f"senk_dev_scaling_{sfx}", [_P, _P, _P, _P, _P, _I, _P])
+        d(f"senk_dev_diag_scaling_{sfx}", [_P, _P, _P, _P, _I, _P])
 
 
 def check(fn: str, code: int) -> int:

@@ -152,5 +152,30 @@ def RemoveOffDiagonal(A: Csr, bnum: int) -> Csr:
     return out
 
 
+def ReadMatrixMarket(path, removeZeros: bool = True):
+    """senk::io::ReadMatrixMarket: (Csr of the stored entries, M, symmetric).
+    A symmetric file gives its stored triangle; Expand(A, "L") makes the full
+    matrix, as the reference's driver does."""
+    pv, pc, pr = _P(), _P(), _P()
+    n, m, sym = C.c_int(0), C.c_int(0), C.c_int(0)
+    check("senk_io_read_matrix_market",
+          lib().senk_io_read_matrix_market(str(path).encode(), C.byref(pv), C.byref(pc), C.byref(pr), C.byref(n),
+                                           C.byref(m), C.byref(sym), int(removeZeros)))
+    rptr = _take(pr.value, n.value + 1, np.int32)
+    nnz = int(rptr[-1])
+    return Csr(_take(pv.value, nnz, np.float64), _take(pc.value, nnz, np.int32), rptr), m.value, bool(sym.value)
+
+
+def Expand(A: Csr, key: str = "L") -> Csr:
+    """senk::matrix::Expand: the full matrix from its stored triangle."""
+    pv, pc, pr = _P(), _P(), _P()
+    check("senk_setup_expand", lib().senk_setup_expand(ptr(_f64(A.val)), ptr(_i32(A.cind)), ptr(_i32(A.rptr)),
+                                                       C.byref(pv), C.byref(pc), C.byref(pr), A.n, key.encode()))
+    rptr = _take(pr.value, A.n + 1, np.int32)
+    nnz = int(rptr[-1])
+    return Csr(_take(pv.value, nnz, np.float64), _take(pc.value, nnz, np.int32), rptr)
+
+
 __all__ = ["Ilu0", "Split", "GetABMCPermutation", "GetAMCPermutation", "Reordering", "Csr2Bcsr",
-           "AllocBlockZero", "Ilup", "AllocLevelZero", "RemoveOffDiagonal", "SenkError"]
+           "AllocBlockZero", "Ilup", "AllocLevelZero", "RemoveOffDiagonal", "ReadMatrixMarket", "Expand",
+           "SenkError"]

@@ -57,7 +57,9 @@ def test_driver_runs_with_the_reference_counts(tmp_path, golden):
     assert abs(it("AbmcIluGmresm") - g["AbmcIluGmresm_m30"]["iters"]) <= 2
     assert abs(it("IlubGmresm") - g["IlubGmresm_8x1_m30"]["iters"]) <= 2
     bic = int(re.search(r"^# iter (\d+)$", sections["IluBicgstab"], re.M).group(1))
-    assert abs(bic - g["IluBicgstab"]["iters"]) <= 2
+    # BiCGStab's count moves with the association of its dot products (the
+    # reference with 8 OpenMP threads: 68 to 75 from run to run, 70 with one)
+    assert abs(bic - g["IluBicgstab"]["iters"]) <= 5
     gcr = re.findall(r"^(\d+) ([-+0-9.eE]+)$", sections["IluGcrm"], re.M)
     assert int(gcr[-1][0]) == g["IluGcrm_m20"]["iters"]
     for name in ("IluGmresm", "AbmcIluGmresm", "IlubGmresm", "IluGcrm"):

@@ -49,6 +49,13 @@ def near(it, want, tol=2):
     return abs(it - want) <= tol
 
 
+# BiCGStab's count moves with the association of its dot products: the
+# reference itself, run with 8 OpenMP threads, took between 68 and 75
+# iterations on C1 from run to run (70 with one thread). The bar covers that
+# spread instead of the ±2 of the other solvers.
+BICG_TOL = 5
+
+
 # ----------------------------------------------------------------- ILUB sweeps
 
 class IlubPlan:
@@ -157,7 +164,7 @@ def test_c1_bicgstab_unpreconditioned(port, golden, c1):
     A, b, nb = c1
     x = np.zeros(A.n)
     r = SV.Bicgstab(A.val, A.cind, A.rptr, b, x, nb, 10000, A.n, 1e-8)
-    assert r.converged and near(r.iters, golden["c1"]["Bicgstab"]["iters"])
+    assert r.converged and near(r.iters, golden["c1"]["Bicgstab"]["iters"], BICG_TOL)
     assert port.relative_residual(A, b, x) < 2e-8
 
 
@@ -167,7 +174,7 @@ def test_c1_ilu_bicgstab(port, golden, c1):
     x = np.zeros(A.n)
     r = SV.IluBicgstab(A.val, A.cind, A.rptr, L_.val, L_.cind, L_.rptr, U_.val, U_.cind, U_.rptr, b, x, nb, 10000,
                        A.n, 1e-8)
-    assert r.converged and near(r.iters, golden["c1"]["IluBicgstab"]["iters"])
+    assert r.converged and near(r.iters, golden["c1"]["IluBicgstab"]["iters"], BICG_TOL)
     assert r.res < 1e-8 and port.relative_residual(A, b, x) < 2e-8
 
 
@@ -176,7 +183,7 @@ def test_c1_ilub_bicgstab(port, golden, c1, ilub8):
     bl, bu = ilub8
     x = np.zeros(A.n)
     r = SV.IlubBicgstab(A.val, A.cind, A.rptr, *bl, *bu, b, x, nb, 10000, A.n, 1e-8, 8, 1)
-    assert r.converged and near(r.iters, golden["c1"]["IlubBicgstab_8x1"]["iters"])
+    assert r.converged and near(r.iters, golden["c1"]["IlubBicgstab_8x1"]["iters"], BICG_TOL)
     assert port.relative_residual(A, b, x) < 2e-8
 
 
@@ -189,7 +196,7 @@ def test_convdiff16_abmc_ilu_bicgstab(port, golden, small):
     r = SV.AbmcIluBicgstab(Ar.val, Ar.cind, Ar.rptr, s["L_val"], s["L_cind"], s["L_rptr"], s["U_val"], s["U_cind"],
                            s["U_rptr"], sc, len(sc) - 1, 16, b, x, float(np.linalg.norm(b)), 1000, Ar.n, 1e-8)
     # the ABMC sweep is the sequential sweep on the reordered system
-    assert r.converged and near(r.iters, golden["convdiff16"]["IluBicgstab"]["iters"])
+    assert r.converged and near(r.iters, golden["convdiff16"]["IluBicgstab"]["iters"], BICG_TOL)
     assert port.relative_residual(Ar, b, x) < 2e-8
 
 
