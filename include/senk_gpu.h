@@ -557,6 +557,29 @@ int senk_dev_ilu0_d(double *val, const int *cind, const int *rptr, int N,
 int senk_dev_ilu0_s(float *val, const int *cind, const int *rptr, int N,
                     const int *cptr, int cnum, int bsize, void *stream);
 
+/* ================================================ device ABMC ordering ==
+ * senk::graph::GetABMCPermutation(cind, rptr, ..., N, bsize, isSym = false,
+ * "simple") (include/senk_graph.hpp:291-334) on a CSR pattern in device
+ * memory; with bsize = 1 it is GetAMCPermutation(..., isSym = false)
+ * (:250-277). The outputs are the reference's, identical: *num_color,
+ * *size_color (host, malloc'd, num_color + 1 entries, in blocks; release with
+ * senk_free), LP (new -> old) and RP (old -> new) in caller-provided device
+ * arrays of N. Each colour is found by parallel rounds that give the same set
+ * as the reference's index-order greedy sweep. Fails (SENK_ERR_ARG) when N is
+ * not a multiple of bsize or a block has more than 128 neighbour blocks.
+ * Synchronous. (The reference's "connect" blocking is a sequential
+ * breadth-first search and stays on the host.) */
+int senk_dev_abmc_ordering(const int *cind, const int *rptr, int N, int bsize, int *num_color, int **size_color,
+                           int *LP, int *RP, void *stream);
+/* senk::matrix::Reordering (include/senk_matrix.hpp:703-730) on the device:
+ * out row i = row LP[i] with columns RP[c], sorted by column; oval/ocind hold
+ * nnz entries, orptr N + 1 (all device). Bit-identical to the host function.
+ * Synchronous. */
+int senk_dev_reordering_d(const double *val, const int *cind, const int *rptr, const int *LP, const int *RP, int N,
+                          double *oval, int *ocind, int *orptr, void *stream);
+int senk_dev_reordering_s(const float *val, const int *cind, const int *rptr, const int *LP, const int *RP, int N,
+                          float *oval, int *ocind, int *orptr, void *stream);
+
 /* ===================================================== host setup (CPU) ==
  * The reference's setup functions, bit-exact, for callers without C++ headers.
  * Outputs are malloc'd; release them with senk_free. */

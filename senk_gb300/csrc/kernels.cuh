@@ -311,19 +311,22 @@ k_multidot(const XT *__restrict__ V, long long ldv, int nv, const XT *__restrict
         for (int q = 0; q < CH; q++)
             if (q < nc) acc[q] += (A)ld_stream(V + (long long)(c0 + q) * ldv + i) * wi;
     }
+    // columns this CTA holds only (nc is the same in all its warps)
     __shared__ double sh[CH][kThreads / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < CH; q++) {
-        double v = warp_sum((double)acc[q]);
-        if (lane == 0) sh[q][wid] = v;
+        if (q < nc) {
+            const double v = warp_sum((double)acc[q]);
+            if (lane == 0) sh[q][wid] = v;
+        }
     }
     __syncthreads();
-    if (threadIdx.x < CH * 32) {
+    if (threadIdx.x < CH * 32 && (int)(threadIdx.x >> 5) < nc) {
         const int q = threadIdx.x >> 5;
         double v = lane < (int)(blockDim.x >> 5) ? sh[q][lane] : 0.0;
         v = warp_sum(v);
-        if (lane == 0 && q < nc) part[(long long)(c0 + q) * gridDim.x + blockIdx.x] = v;
+        if (lane == 0) part[(long long)(c0 + q) * gridDim.x + blockIdx.x] = v;
     }
     const unsigned total = gridDim.x * gridDim.y;
     if (last_cta_arrives(ticket, total)) {
@@ -385,19 +388,24 @@ k_multidot_v(const XT *__restrict__ V, long long ldv, int nv, const XT *__restri
         for (int q = 0; q < CH; q++)
             if (q < nc) acc[q] += vdot(ld_stream(Vv + q * ldvec + i), w0);
     }
+    // columns this CTA holds only (nc is the same in all its warps); each
+    // warp adds its lanes' sums in XT (FP64 shuffles and adds are slow on
+    // this GPU), then the CTA's warps and the grid's CTAs in FP64
     __shared__ double sh[CH][kThreads / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < CH; q++) {
-        double v = warp_sum((double)acc[q]);
-        if (lane == 0) sh[q][wid] = v;
+        if (q < nc) {
+            const XT v = warp_sum(acc[q]);
+            if (lane == 0) sh[q][wid] = (double)v;
+        }
     }
     __syncthreads();
-    if (threadIdx.x < CH * 32) {
+    if (threadIdx.x < CH * 32 && (int)(threadIdx.x >> 5) < nc) {
         const int q = threadIdx.x >> 5;
         double v = lane < (int)(blockDim.x >> 5) ? sh[q][lane] : 0.0;
         v = warp_sum(v);
-        if (lane == 0 && q < nc) part[(long long)(c0 + q) * gridDim.x + blockIdx.x] = v;
+        if (lane == 0) part[(long long)(c0 + q) * gridDim.x + blockIdx.x] = v;
     }
     const unsigned total = gridDim.x * gridDim.y;
     if (last_cta_arrives(ticket, total)) {
@@ -552,7 +560,15 @@ k_update_v(const XT *__restrict__ V, long long ldv, int nv, const double *__rest
         nacc += vdot(v0, v0);
     }
     __shared__ double sh[32];
-    double t = block_sum((double)nacc, sh);
+    // lanes in XT, then the warps in FP64 (as in k_multidot_v)
+    const XT wsum = warp_sum(nacc);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)wsum;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+    }
     if (threadIdx.x == 0) part[blockIdx.x] = t;
     if (last_cta_arrives(ticket, gridDim.x)) {
         __shared__ double shp[32];

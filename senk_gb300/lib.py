@@ -183,7 +183,9 @@ def _declare(L):
     d("senk_setup_remove_off_diagonal", [PP, PP, PP, _I, _I])
     d("senk_io_read_matrix_market", [C.c_char_p, PP, PP, PP, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), _I])
     d("senk_setup_expand", [_P, _P, _P, PP, PP, PP, _I, C.c_char_p])
+    d("senk_dev_abmc_ordering", [_P, _P, _I, _I, C.POINTER(_I), PP, _P, _P, _P])
     for sfx in ("d", "s"):
+        d(f"senk_dev_reordering_{sfx}", [_P, _P, _P, _P, _P, _I, _P, _P, _P, _P])
         d(f"senk_dev_get_diag_{sfx}", [_P, _P, _P, _P, _I, _P])
         d(f"senk_dev_scaling_{sfx}", [_P, _P, _P, _P, _P, _I, _P])
         d(f"senk_dev_diag_scaling_{sfx}", [_P, _P, _P, _P, _I, _P])

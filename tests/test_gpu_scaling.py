@@ -49,9 +49,9 @@ def test_device_scaling_is_bit_identical(torch, port, dtype, case):
     rng = np.random.default_rng(4)
     ld = rng.uniform(0.5, 2.0, A.n).astype(dtype)
     rd = rng.uniform(0.5, 2.0, A.n).astype(dtype)
+    ldd, rdd = _dev(torch, ld), _dev(torch, rd)  # held until the call has run
     L.check("scaling", getattr(L.lib(), f"senk_dev_scaling_{sfx}")(v.data_ptr(), c.data_ptr(), r.data_ptr(),
-                                                                    _dev(torch, ld).data_ptr(),
-                                                                    _dev(torch, rd).data_ptr(), A.n, None))
+                                                                    ldd.data_ptr(), rdd.data_ptr(), A.n, None))
     torch.cuda.synchronize()
     if dtype == np.float64:
         want = port.scaling(A, ld, rd).val
