@@ -65,21 +65,24 @@ def _trained_like_params(seed=3):
 
 
 def _grad_blocks():
-    """Parameter blocks with their bars: the layer weights come from the BF16
-    tensor-core product X^T dZ (operands rounded to BF16, as the oracle
-    reproduces, then summed in FP32 in a different order), the other blocks
-    from FP32 sums of FP32 (or once-rounded BF16) terms."""
-    out = [("W_in", M.OFF_WIN, M.OFF_BIN, GRAD_BAR_FP32), ("b_in", M.OFF_BIN, M.OFF_LAYER, GRAD_BAR_FP32)]
+    """Parameter blocks with their bars (relative max-norm error against the
+    oracle, which reproduces every BF16 rounding point). The decoder's
+    gradients are FP32 sums of FP32 terms. Every other block's gradient flows
+    back through the layers' BF16 tensor-core products (the layer weights are
+    such a product, X^T dZ, themselves), so its terms carry BF16-rounded
+    operands summed in FP32 in a different order than the oracle's. Measured
+    on this system: decoder at most 1.7e-6, the others at most 2.2e-4."""
+    out = [("W_in", M.OFF_WIN, M.OFF_BIN, GRAD_BAR_BF16_PATH), ("b_in", M.OFF_BIN, M.OFF_LAYER, GRAD_BAR_BF16_PATH)]
     for l in range(M.LAYERS):
         base = M.OFF_LAYER + l * M.LAYER_SIZE
-        out.append((f"Theta{l}", base, base + 2 * M.HID * M.HID, GRAD_BAR_BF16))
-        out.append((f"beta{l}", base + 2 * M.HID * M.HID, base + M.LAYER_SIZE, GRAD_BAR_FP32))
+        out.append((f"Theta{l}", base, base + 2 * M.HID * M.HID, GRAD_BAR_BF16_PATH))
+        out.append((f"beta{l}", base + 2 * M.HID * M.HID, base + M.LAYER_SIZE, GRAD_BAR_BF16_PATH))
     out += [("w_out", M.OFF_WOUT, M.OFF_BOUT, GRAD_BAR_FP32), ("b_out", M.OFF_BOUT, M.NPARAMS, GRAD_BAR_FP32)]
     return out
 
 
-GRAD_BAR_BF16 = 2e-2
-GRAD_BAR_FP32 = 2e-2
+GRAD_BAR_BF16_PATH = 1e-3
+GRAD_BAR_FP32 = 1e-5
 
 
 def test_network_output_loss_and_gradient_match_oracle(torch, small_member):
