@@ -54,30 +54,63 @@ k_ilub_sweep(const T *__restrict__ bval, const int *__restrict__ bcind, const in
         const int i = br * BNL;
         T t = lane < BNL ? x[i + lane] : T(0);
         const int b0 = brptr[br], b1 = brptr[br + 1];
+        // Blocks are taken kBatch at a time: their columns, values and (for
+        // columns outside this block row) y entries are all loaded before the
+        // first subtraction, which then run in the blocks' order as before.
+        constexpr int kBatch = 4;
         if (!UPPER) {
-            for (int j = b0; j < b1; j++) {
-                const int xb = bcind[j] * BNW;
+            for (int j0 = b0; j0 < b1; j0 += kBatch) {
+                int xb[kBatch];
+                T vv[kBatch][BNW], yy[kBatch][BNW];
 #pragma unroll
-                for (int l = 0; l < BNW; l++) {
-                    const int rel = xb + l - i;
-                    const T v = lane < BNL ? bval[(size_t)j * BS + l * BNL + lane] : T(0);
-                    if (rel >= 0 && rel < BNL) {
-                        const T s0 = __shfl_sync(mask, t, rel, G);
-                        const T t0 = t - v * s0;
-                        const T s1 = __shfl_sync(mask, t0, rel, G);  // y[col] after its own pair
-                        t = (lane >> 1) > (rel >> 1) ? t - v * s1 : t0;
-                    } else {
-                        t -= v * y[xb + l];
+                for (int u = 0; u < kBatch; u++) xb[u] = j0 + u < b1 ? bcind[j0 + u] * BNW : i;
+#pragma unroll
+                for (int u = 0; u < kBatch; u++)
+#pragma unroll
+                    for (int l = 0; l < BNW; l++) {
+                        const int rel = xb[u] + l - i;
+                        const bool live = j0 + u < b1;
+                        vv[u][l] = live && lane < BNL ? bval[(size_t)(j0 + u) * BS + l * BNL + lane] : T(0);
+                        yy[u][l] = live && !(rel >= 0 && rel < BNL) ? y[xb[u] + l] : T(0);
+                    }
+#pragma unroll
+                for (int u = 0; u < kBatch; u++) {
+                    if (j0 + u >= b1) break;
+#pragma unroll
+                    for (int l = 0; l < BNW; l++) {
+                        const int rel = xb[u] + l - i;
+                        const T v = vv[u][l];
+                        if (rel >= 0 && rel < BNL) {
+                            const T s0 = __shfl_sync(mask, t, rel, G);
+                            const T t0 = t - v * s0;
+                            const T s1 = __shfl_sync(mask, t0, rel, G);  // y[col] after its own pair
+                            t = (lane >> 1) > (rel >> 1) ? t - v * s1 : t0;
+                        } else {
+                            t -= v * yy[u][l];
+                        }
                     }
                 }
             }
         } else {
-            for (int j = b1 - 1; j >= b0 + BREM; j--) {
-                const int xb = bcind[j] * BNW;
+            // blocks right of the diagonal square, from the last one down
+            for (int j0 = b1 - 1; j0 >= b0 + BREM; j0 -= kBatch) {
+                T vv[kBatch][BNW], yy[kBatch][BNW];
 #pragma unroll
-                for (int l = 0; l < BNW; l++) {
-                    const T v = lane < BNL ? bval[(size_t)j * BS + l * BNL + lane] : T(0);
-                    t -= v * y[xb + l];
+                for (int u = 0; u < kBatch; u++) {
+                    const int j = j0 - u;
+                    const bool live = j >= b0 + BREM;
+                    const int xb = live ? bcind[j] * BNW : 0;
+#pragma unroll
+                    for (int l = 0; l < BNW; l++) {
+                        vv[u][l] = live && lane < BNL ? bval[(size_t)j * BS + l * BNL + lane] : T(0);
+                        yy[u][l] = live ? y[xb + l] : T(0);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kBatch; u++) {
+                    if (j0 - u < b0 + BREM) break;
+#pragma unroll
+                    for (int l = 0; l < BNW; l++) t -= vv[u][l] * yy[u][l];
                 }
             }
 #pragma unroll
