@@ -537,7 +537,8 @@ int senk_mpnn_apply(senk_mpnn *net, senk_system *sys, const double *r, double *o
 int senk_system_set_learned(senk_system *sys, senk_mpnn *net, double stall);
 int senk_system_learned_fallback(senk_system *sys);
 /* The tensor-core products alone, for tests: C = A Bt^T (A n x K, Bt NO x K,
- * BF16; C FP32; K = 128 with NO = 64, or K = 64 with NO = 128) and
+ * BF16; C FP32; K = 128 with NO = 64, or K = 64 with NO = 128; A, Bt and C
+ * 16-byte aligned, else SENK_ERR_ARG) and
  * out[128][64] = X^T dZ (X n x 128, dZ n x 64, BF16). */
 int senk_dev_gemm_bf16(const void *A, const void *Bt, float *C, int n, int K, int NO, void *stream);
 int senk_dev_gemm_tn_bf16(const void *X, const void *dZ, float *out, int n, void *stream);

@@ -27,9 +27,9 @@ namespace {
 
 // Dynamic shared memory of the tensor-core GEMMs. Besides the two tiles it caps
 // the CTAs resident on an SM so that their TMEM accumulators fit in its 512
-// columns: 48 KB -> 4 CTAs x 64 columns; 56 KB -> 4 CTAs x 128 columns.
-constexpr int kSmemFwd = 128 * 128 * 2 + 64 * 128 * 2;  // 48 KB
-constexpr int kSmemDx = 56 * 1024;                      // tiles need 32 KB
+// columns: 48 KB -> 4 CTAs x 64 columns; 66 KB -> 3 CTAs x 128 columns.
+constexpr int kSmemFwd = tc_gemm_smem(128, 64);  // 48 KB of operand tiles
+constexpr int kSmemDx = tc_gemm_smem(64, 128);   // 66 KB: the 128 x 132 FP32 result tile
 constexpr int kSmemTn = 8 * 1024;                       // + 24 KB static: 7 CTAs x 64 columns
 
 constexpr int kHid = 64;
@@ -85,43 +85,76 @@ k_encode(const float *fd, const float *fs, const T *r, const float *rms, const f
     X[i * 128 + j] = __float2bfloat16_rn(h);
 }
 
-// m = W h: warp per row, lane l holds features 2l, 2l+1; h = X[:, :64] (bf16),
-// m -> X[:, 64:128] (bf16), FP32 accumulation.
+// m = W h, 8 lanes per row (4 rows per warp), lane k of a row holding
+// features 8k..8k+7 (one 16-byte load of bf16 per entry); h = X[:, :64]
+// (bf16), m -> X[:, 64:128] (bf16), FP32 accumulation in the entries' order.
 __global__ void __launch_bounds__(kThreads)
-k_aggregate(const int *rptr, const int *cind, const float *w, bf16 *X, long long n)
+k_aggregate(const int *__restrict__ rptr, const int *__restrict__ cind, const float *__restrict__ w, bf16 *X,
+            long long n)
 {
-    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const int sub = threadIdx.x & 7;
     if (row >= n) return;
-    float a0 = 0.f, a1 = 0.f;
-    for (int p = rptr[row]; p < rptr[row + 1]; p++) {
-        const int c = cind[p];
+    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int p1 = rptr[row + 1];
+#pragma unroll 4
+    for (int p = rptr[row]; p < p1; p++) {
         const float wv = w[p];
-        const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(X + (long long)c * 128 + 2 * lane);
-        a0 += wv * __bfloat162float(h.x);
-        a1 += wv * __bfloat162float(h.y);
+        const uint4 u = *reinterpret_cast<const uint4 *>(X + (long long)cind[p] * 128 + 8 * sub);
+        const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            a[2 * k] += wv * __bfloat162float(h[k].x);
+            a[2 * k + 1] += wv * __bfloat162float(h[k].y);
+        }
     }
-    *reinterpret_cast<__nv_bfloat162 *>(X + row * 128 + 64 + 2 * lane) = __floats2bfloat162_rn(a0, a1);
+    uint4 o;
+    uint32_t *ow = reinterpret_cast<uint32_t *>(&o);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const __nv_bfloat162 v = __floats2bfloat162_rn(a[2 * k], a[2 * k + 1]);
+        ow[k] = *reinterpret_cast<const uint32_t *>(&v);
+    }
+    *reinterpret_cast<uint4 *>(X + row * 128 + 64 + 8 * sub) = o;
 }
 
-// dH += W^T dM (fp32), warp per row of W^T, lane holds two features
+// dH += W^T dM (fp32), 8 lanes per row of W^T (4 rows per warp), lane k of a
+// row holding features 8k..8k+7 (two 16-byte loads per entry).
 __global__ void __launch_bounds__(kThreads)
-k_aggregate_back(const int *rptr, const int *cind, const float *w, const float *dM, float *dH, long long n)
+k_aggregate_back(const int *__restrict__ rptr, const int *__restrict__ cind, const float *__restrict__ w,
+                 const float *__restrict__ dM, float *__restrict__ dH, long long n)
 {
-    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const int sub = threadIdx.x & 7;
     if (row >= n) return;
-    float a0 = 0.f, a1 = 0.f;
-    for (int p = rptr[row]; p < rptr[row + 1]; p++) {
-        const float2 d = *reinterpret_cast<const float2 *>(dM + (long long)cind[p] * 64 + 2 * lane);
-        a0 += w[p] * d.x;
-        a1 += w[p] * d.y;
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+    const int p1 = rptr[row + 1];
+#pragma unroll 4
+    for (int p = rptr[row]; p < p1; p++) {
+        const float wv = w[p];
+        const float4 *d = reinterpret_cast<const float4 *>(dM + (long long)cind[p] * 64 + 8 * sub);
+        const float4 d0 = d[0], d1 = d[1];
+        a0.x += wv * d0.x;
+        a0.y += wv * d0.y;
+        a0.z += wv * d0.z;
+        a0.w += wv * d0.w;
+        a1.x += wv * d1.x;
+        a1.y += wv * d1.y;
+        a1.z += wv * d1.z;
+        a1.w += wv * d1.w;
     }
-    float2 *o = reinterpret_cast<float2 *>(dH + row * 64 + 2 * lane);
-    float2 v = *o;
-    v.x += a0;
-    v.y += a1;
-    *o = v;
+    float4 *o = reinterpret_cast<float4 *>(dH + row * 64 + 8 * sub);
+    float4 v0 = o[0], v1 = o[1];
+    v0.x += a0.x;
+    v0.y += a0.y;
+    v0.z += a0.z;
+    v0.w += a0.w;
+    v1.x += a1.x;
+    v1.y += a1.y;
+    v1.z += a1.z;
+    v1.w += a1.w;
+    o[0] = v0;
+    o[1] = v1;
 }
 
 // Inference epilogue: out_i = ilu_i + (rms / d) * (h_i . w_out + b_out); warp per node.
@@ -160,21 +193,38 @@ k_target(const T *e, const T *ilu, const float *rms, float d, float *t, long lon
 }
 
 // dZ = bf16(dH (.) [z > 0]); grad beta += column sums of the FP32 product.
-// Block of 256 threads = 4 nodes x 64 features, grid-stride over nodes.
+// Block of 256 threads = 16 nodes x 16 groups of 4 features (16-byte loads of
+// dH, 8-byte loads of z), grid-stride over nodes.
 __global__ void __launch_bounds__(kThreads)
 k_relu_back(const float *dH, const bf16 *Z, bf16 *dZ, float *gbeta, long long n)
 {
-    const int j = threadIdx.x & 63, sub = threadIdx.x >> 6;
-    float s = 0.f;
-    for (long long i = (long long)blockIdx.x * 4 + sub; i < n; i += (long long)gridDim.x * 4) {
-        const float g = __bfloat162float(Z[i * 64 + j]) > 0.f ? dH[i * 64 + j] : 0.f;
-        dZ[i * 64 + j] = __float2bfloat16_rn(g);
-        s += g;
+    const int j = (threadIdx.x & 15) * 4, sub = threadIdx.x >> 4;
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (long long i = (long long)blockIdx.x * 16 + sub; i < n; i += (long long)gridDim.x * 16) {
+        const uint2 zz = __ldg(reinterpret_cast<const uint2 *>(Z + i * 64 + j));
+        const float4 d = __ldg(reinterpret_cast<const float4 *>(dH + i * 64 + j));
+        const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162 *>(&zz.x);
+        const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162 *>(&zz.y);
+        const float4 g = make_float4(__bfloat162float(z01.x) > 0.f ? d.x : 0.f, __bfloat162float(z01.y) > 0.f ? d.y : 0.f,
+                                     __bfloat162float(z23.x) > 0.f ? d.z : 0.f, __bfloat162float(z23.y) > 0.f ? d.w : 0.f);
+        st_bf16x4(dZ + i * 64 + j, g.x, g.y, g.z, g.w);
+        s.x += g.x;
+        s.y += g.y;
+        s.z += g.z;
+        s.w += g.w;
     }
-    __shared__ float sh[4][64];
-    sh[sub][j] = s;
+    __shared__ float sh[16][64];
+    sh[sub][j] = s.x;
+    sh[sub][j + 1] = s.y;
+    sh[sub][j + 2] = s.z;
+    sh[sub][j + 3] = s.w;
     __syncthreads();
-    if (threadIdx.x < 64) atomicAdd(gbeta + j, sh[0][j] + sh[1][j] + sh[2][j] + sh[3][j]);
+    if (threadIdx.x < 64) {
+        float t = 0.f;
+#pragma unroll
+        for (int k = 0; k < 16; k++) t += sh[k][threadIdx.x];
+        atomicAdd(gbeta + threadIdx.x, t);
+    }
 }
 
 // Encoder backward: dz = dH0 (.) [z0 > 0] (z0 recomputed); grad W_in += f dz, grad b_in += dz.
@@ -557,7 +607,7 @@ struct Mpnn {
         k_encode<T><<<ceil_div(n * kHid, kThreads), kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, H[0].p, X[0].p, n);
         const int tiles = ceil_div(n, 128);
         for (int l = 0; l < kLayers; l++) {
-            k_aggregate<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(wr.p, wc.p, wv.p, X[l].p, n);
+            k_aggregate<<<ceil_div(n * 8, kThreads), kThreads, 0, s>>>(wr.p, wc.p, wv.p, X[l].p, n);
             TcArgs a;
             a.bias = P.p + kOffLayer + l * kLayerSize + 2 * kHid * kHid;
             a.hin = H[l].p;
@@ -637,7 +687,7 @@ struct Mpnn {
             a.dm = dM.p;
             k_tc_gemm<64, 128, kTcDx><<<tiles, 128, kSmemDx, s>>>(
                 dZ.p, 64, Wb.p + (size_t)l * 128 * 64, (int)n, a, status.p);
-            k_aggregate_back<<<ceil_div(n * 32, kThreads), kThreads, 0, s>>>(tr.p, tcol.p, tv.p, dM.p, dh2, n);
+            k_aggregate_back<<<ceil_div(n * 8, kThreads), kThreads, 0, s>>>(tr.p, tcol.p, tv.p, dM.p, dh2, n);
             std::swap(dh, dh2);
         }
         k_encode_back<T><<<sm_count() * 8, kThreads, 0, s>>>(fd.p, fs.p, r, rms.p, P.p, dh, G.p, n);
@@ -861,7 +911,8 @@ int senk_dev_gemm_bf16(const void *A, const void *Bt, float *C, int n, int K, in
 {
     return guarded("senk_dev_gemm_bf16", [&] {
         SENK_REQUIRE(A && Bt && C && n > 0, "null argument");
-        SENK_REQUIRE(((uintptr_t)A & 15) == 0 && ((uintptr_t)Bt & 15) == 0, "operands must be 16-byte aligned");
+        SENK_REQUIRE(((uintptr_t)A & 15) == 0 && ((uintptr_t)Bt & 15) == 0 && ((uintptr_t)C & 15) == 0,
+                     "operands and result must be 16-byte aligned");
         set_smem_limits();
         static DevBuf<int> st;
         if (!st.p) {

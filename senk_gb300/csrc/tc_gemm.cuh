@@ -27,13 +27,111 @@ struct TcArgs {
     float *dm = nullptr;              // N x 64 fp32 (kTcDx, columns 64..127 of the product)
 };
 
+// Row stride (floats) of the 128 x NO FP32 result tile that the epilogue
+// stages in shared memory: rows stay 16-byte aligned, and the eight lanes of a
+// quarter warp that move one float4 each (a row per lane when written from
+// TMEM, consecutive columns of one row when read) fall in distinct banks.
+template <int NO>
+constexpr int kTcTileStride = NO + 4;
+
+// Dynamic shared memory of k_tc_gemm<K, NO>: the two operand tiles, or the
+// 128 x NO FP32 result tile of the epilogue, which reuses them once the MMAs
+// have completed.
+__host__ __device__ constexpr int tc_gemm_smem(int K, int NO)
+{
+    return (128 * K * 2 + NO * K * 2) > 128 * (NO + 4) * 4 ? (128 * K * 2 + NO * K * 2) : 128 * (NO + 4) * 4;
+}
+
+__device__ __forceinline__ void st_bf16x4(__nv_bfloat16 *p, float a, float b, float c, float d)
+{
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(a, b), hi = __floats2bfloat162_rn(c, d);
+    uint2 u;
+    u.x = *reinterpret_cast<const uint32_t *>(&lo);
+    u.y = *reinterpret_cast<const uint32_t *>(&hi);
+    *reinterpret_cast<uint2 *>(p) = u;
+}
+
+// Epilogue of k_tc_gemm over the result tile (rows [0, rows) of it valid). Each
+// thread owns one group of four consecutive columns and walks rows 128 / G
+// apart (G = the row's groups), so every global access is a 16-byte (FP32) or
+// 8-byte (BF16) vector and a warp's accesses cover whole rows. The global
+// loads of a batch of rows are all issued before the first store.
+template <int NO, int EPI>
+__device__ __forceinline__ void tc_epilogue(const float *tile, long long row0, int rows, const TcArgs &args)
+{
+    constexpr int S = kTcTileStride<NO>;
+    const int tid = threadIdx.x;
+    if constexpr (EPI == kTcPlain) {
+        constexpr int G = NO / 4, RP = 128 / G;  // groups per row, rows per pass
+        const int j = (tid % G) * 4;
+#pragma unroll 4
+        for (int rr = tid / G; rr < rows; rr += RP)
+            *reinterpret_cast<float4 *>(args.c + (row0 + rr) * NO + j) =
+                *reinterpret_cast<const float4 *>(tile + rr * S + j);
+    } else {
+        // both fused epilogues: 64 columns of h per row (kTcDx: then the 64 of dm)
+        constexpr int RP = 8, B = 8;  // rows per pass, passes per batch of loads
+        const int j = (tid & 15) * 4, rb = tid >> 4;
+        float4 bias = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (EPI == kTcLayerFwd) bias = make_float4(args.bias[j], args.bias[j + 1], args.bias[j + 2], args.bias[j + 3]);
+#pragma unroll 1
+        for (int p0 = 0; p0 < 128 / RP; p0 += B) {
+            float4 h[B];
+#pragma unroll
+            for (int u = 0; u < B; u++) {
+                const int rr = rb + RP * (p0 + u);
+                h[u] = rr < rows ? __ldg(reinterpret_cast<const float4 *>(args.hin + (row0 + rr) * 64 + j))
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < B; u++) {
+                const int rr = rb + RP * (p0 + u);
+                if (rr >= rows) break;
+                const long long row = row0 + rr;
+                const float4 a = *reinterpret_cast<const float4 *>(tile + rr * S + j);
+                if constexpr (EPI == kTcLayerFwd) {
+                    const float4 z = make_float4(a.x + bias.x, a.y + bias.y, a.z + bias.z, a.w + bias.w);
+                    if (args.zout) st_bf16x4(args.zout + row * 64 + j, z.x, z.y, z.z, z.w);
+                    const float4 o = make_float4(h[u].x + fmaxf(z.x, 0.f), h[u].y + fmaxf(z.y, 0.f),
+                                                 h[u].z + fmaxf(z.z, 0.f), h[u].w + fmaxf(z.w, 0.f));
+                    *reinterpret_cast<float4 *>(args.hout + row * 64 + j) = o;
+                    if (args.xout) st_bf16x4(args.xout + row * args.xld + j, o.x, o.y, o.z, o.w);
+                } else {
+                    *reinterpret_cast<float4 *>(args.hout + row * 64 + j) =
+                        make_float4(h[u].x + a.x, h[u].y + a.y, h[u].z + a.z, h[u].w + a.w);
+                    *reinterpret_cast<float4 *>(args.dm + row * 64 + j) =
+                        *reinterpret_cast<const float4 *>(tile + rr * S + 64 + j);
+                }
+            }
+        }
+    }
+}
+
+// 16-byte copy global -> shared that completes asynchronously (cp.async);
+// with pred false nothing is read and the 16 bytes are zeroed.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool pred)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src),
+                 "r"(pred ? 16 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // Y = epilogue(A * Bt^T) for one tile of 128 rows: A is n x K (bf16, row
 // stride lda, 16-byte aligned rows), Bt is NO x K (bf16, row stride K). One CTA
-// of 128 threads: all threads stage both tiles into shared memory in the
-// K-major core-matrix layout, thread 0 issues K/16 MMAs into a 128 x NO FP32
-// TMEM accumulator and commits them to an mbarrier, and warp w reads TMEM lanes
-// [32w, 32w+32) (rows) for the epilogue. A wait that runs out sets *status; the
-// CTA then waits once more (bounded), frees its TMEM and leaves.
+// of 128 threads: all threads issue their 16-byte chunks of both tiles as
+// asynchronous copies into the K-major core-matrix layout (all in flight at
+// once; rows past n are zero-filled), thread 0 issues K/16 MMAs into a
+// 128 x NO FP32 TMEM accumulator and commits them to an mbarrier, warp w reads
+// TMEM lanes [32w, 32w+32) (rows) into a shared-memory tile, and the epilogue
+// (tc_epilogue) then walks the tile with 16-byte vectors along the rows, so
+// every global load and store of a warp covers whole rows (all pointers of
+// TcArgs 16-byte aligned; xld a multiple of 4). A wait that runs out sets *status;
+// the CTA then waits once more (bounded), frees its TMEM and leaves.
 template <int K, int NO, int EPI>
 __global__ void __launch_bounds__(128)
 k_tc_gemm(const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__restrict__ Bt, int n, TcArgs args,
@@ -56,17 +154,18 @@ k_tc_gemm(const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__r
     if (tid == 0) mbar_init(&bar, 1);
     // stage A (128 x K) and Bt (NO x K): 16-byte chunks of 8 elements
     constexpr int CPR = K / 8;  // chunks per row
+#pragma unroll 4
     for (int c = tid; c < 128 * CPR; c += 128) {
         const int r = c / CPR, kc = c % CPR;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (row0 + r < n) v = *reinterpret_cast<const uint4 *>(A + (row0 + r) * lda + kc * 8);
-        *reinterpret_cast<uint4 *>(sa + tc::kmajor_offset(r, kc * 8, K)) = v;
+        const bool in = row0 + r < n;
+        cp_async16(sa + tc::kmajor_offset(r, kc * 8, K), in ? A + (row0 + r) * lda + kc * 8 : A, in);
     }
+#pragma unroll 4
     for (int c = tid; c < NO * CPR; c += 128) {
         const int r = c / CPR, kc = c % CPR;
-        const uint4 v = *reinterpret_cast<const uint4 *>(Bt + (long long)r * K + kc * 8);
-        *reinterpret_cast<uint4 *>(sb + tc::kmajor_offset(r, kc * 8, K)) = v;
+        cp_async16(sb + tc::kmajor_offset(r, kc * 8, K), Bt + (long long)r * K + kc * 8, true);
     }
+    cp_async_wait_all();
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -91,35 +190,20 @@ k_tc_gemm(const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__r
     }
     tc::fence_after_sync();
     if (ok) {
-        const long long row = row0 + warp * 32 + lane;
-        const bool live = row < n;
+        // the MMAs have read the operand tiles: their space holds the result tile
+        float *tile = reinterpret_cast<float *>(tc_smem);
+        const int r = warp * 32 + lane;
 #pragma unroll
         for (int c0 = 0; c0 < NO; c0 += 16) {
             float v[16];
             tc::tmem_ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (!live) continue;
-            if (EPI == kTcPlain) {
 #pragma unroll
-                for (int q = 0; q < 16; q++) args.c[row * NO + c0 + q] = v[q];
-            } else if (EPI == kTcLayerFwd) {
-#pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    const int j = c0 + q;
-                    const float z = v[q] + args.bias[j];
-                    if (args.zout) args.zout[row * 64 + j] = __float2bfloat16_rn(z);
-                    const float h = args.hin[row * 64 + j] + fmaxf(z, 0.f);
-                    args.hout[row * 64 + j] = h;
-                    if (args.xout) args.xout[row * args.xld + j] = __float2bfloat16_rn(h);
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    const int j = c0 + q;
-                    if (j < 64) args.hout[row * 64 + j] = args.hin[row * 64 + j] + v[q];
-                    else args.dm[row * 64 + (j - 64)] = v[q];
-                }
-            }
+            for (int q = 0; q < 16; q += 4)
+                *reinterpret_cast<float4 *>(tile + r * kTcTileStride<NO> + c0 + q) =
+                    make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
         }
+        __syncthreads();
+        tc_epilogue<NO, EPI>(tile, row0, (int)min((long long)128, (long long)n - row0), args);
     }
     tc::fence_before_sync();
     __syncthreads();
