@@ -94,6 +94,12 @@ typedef struct {
                                  barrier separates the colours, each group's block
                                  is staged while the group before it is solved);
                                  wider colours keep one launch each */
+#define SENK_SWEEP_WIDE 5     /* as SENK_SWEEP_COMPACT, every colour with two rows
+                                 per thread (CTAs of bsize/2 warps) where the ABMC
+                                 block size is at least 4 (smaller blocks: one row
+                                 per thread). COMPACT and AUTO take that kernel
+                                 only for colours with more groups than one wave
+                                 of one-row-per-thread CTAs holds */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0

@@ -181,6 +181,8 @@ struct SweepFactor {
         // a cooperative launch (k_sweep_cp) of colours [cbeg, cend) on `grid` CTAs
         // instead of one colour (k_sweep_cc)
         int coop = 0, cbeg = 0, cend = 0, grid = 0;
+        // 1: k_sweep_cc2 (two rows per thread) instead of k_sweep_cc
+        int wide = 0;
     };
     std::vector<Launch> launches;
     DevBuf<WfGroup> wgroups;
@@ -195,6 +197,8 @@ struct SweepFactor {
     // buffers; ctrl holds its barrier words)
     bool persistent = false;
     size_t cp_buf = 0;
+    // compact, per colour: every colour takes k_sweep_cc2 (SENK_SWEEP_WIDE)
+    bool force_wide = false;
 };
 
 // A split ILU factorisation with its sweep schedule.

@@ -1198,20 +1198,14 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int g0, int ng, const int2 *__res
     }
 }
 
-// One group of the compact chain layout, staged in shared memory (cw, vw: its
-// block; cnt: its per-chain row counts), for the thread of row l of chain q
-// (t: x of that row on entry): subtracts the row's external entries, then runs
-// the in-chain recurrence; the solved rows are in tsh on return (all threads
-// past a CTA barrier). NC reads y through the non-coherent path, for kernels in
-// which y's earlier rows were written by earlier kernels.
-template <typename VT, typename XT, int BS, bool UPPER, bool NC>
-__device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
-                                         XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, XT t,
-                                         const XT *y, int l, int q)
+// Row l's place in the external entries of its chain's lane stream (rows come
+// in solve order): eo = entries of the rows solved before it, ne = its own.
+// cq: the chain's 2*BS row counts (external, then in-chain).
+template <int BS, bool UPPER>
+__device__ __forceinline__ void cc_row_counts(const unsigned char *cq, int l, int &eo, int &ne)
 {
-    // row l's external entries; in lane q's stream rows come in solve order
-    const unsigned char *cq = cnt + q * 2 * BS;
-    int eo = 0, ne = 0;
+    eo = 0;
+    ne = 0;
     if constexpr (BS >= 8) {
         // the chain's counts as 16-byte words (2 BS bytes per chain, 16-byte aligned)
         const uint4 *c4 = reinterpret_cast<const uint4 *>(cq);
@@ -1234,54 +1228,174 @@ __device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const 
             if (UPPER ? r > l : r < l) eo += cq[r];
         ne = cq[l];
     }
-#pragma unroll 4
-    for (int k = 0; k < ne; k++) {
-        const int at = (eo + k) * 32 + q;
-        t -= (XT)vw[at] * (NC ? __ldg(y + (cw[at] & kColMask)) : y[cw[at] & kColMask]);
-    }
-    tsh[q][l] = t;
-    __syncthreads();
-    // In-chain recurrence, BS lanes per chain (lane = row), 32 / BS chains
-    // per warp, all warps busy: the rows are finished in solve order; the
-    // lane of the row finished at step s (U: after its inverted diagonal)
-    // broadcasts it by a shuffle within the chain's lanes, and every lane
-    // whose next in-chain entry is that column subtracts it. A lane's
-    // entries come in the same order as the steps (the reference's column
-    // order), two of them held in registers and refilled from the block.
-    if (BS > 1 || UPPER) {
-        constexpr int CPW = 32 / BS;  // chains per warp
-        const int lane = threadIdx.x & 31;
-        const int qc = l * CPW + lane / BS, rr = lane % BS;
-        const int *iw = cw + d.emax * 32 + ibase[qc];
-        const VT *iv = vw + d.emax * 32 + ibase[qc];
+}
+
+// In-chain recurrence of one chain qc in the BS lanes [BS*k, BS*k+BS) of a warp
+// (lane = row rr): the rows are finished in solve order; the lane of the row
+// finished at step s (U: after its inverted diagonal) broadcasts it by a
+// shuffle within the chain's lanes, and every lane whose next in-chain entry is
+// that column subtracts it. A lane's entries come in the same order as the
+// steps (the reference's column order), two of them held in registers and
+// refilled from the block. Every lane of the warp calls step(s) for every s.
+template <typename VT, typename XT, int BS, bool UPPER>
+struct ChainRec {
+    const int *iw;
+    const VT *iv;
+    int left, at, c0, c1, rr;
+    XT v0, v1, tt, di;
+
+    __device__ __forceinline__ void init(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
+                                         const XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, int qc,
+                                         int row)
+    {
+        rr = row;
+        iw = cw + d.emax * 32 + ibase[qc];
+        iv = vw + d.emax * 32 + ibase[qc];
         const unsigned char *cc = cnt + qc * 2 * BS;
         int io = 0;
 #pragma unroll
         for (int r = 0; r < BS; r++)
             if (UPPER ? r > rr : r < rr) io += cc[BS + r];
-        int left = cc[BS + rr];
-        XT tt = tsh[qc][rr];
-        const XT di = UPPER ? dsh[qc][rr] : XT(1);
-        int c0 = -1, c1 = -1;
-        XT v0 = XT(0), v1 = XT(0);
-        int at = io;
-        if (left > 0) { c0 = iw[at] & 255; v0 = (XT)iv[at]; at++; }
-        if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
-#pragma unroll
-        for (int s = 0; s < BS; s++) {
-            const int c = UPPER ? BS - 1 - s : s;
-            if (UPPER && rr == c) tt *= di;
-            const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
-            if (c0 == c) {
-                tt -= v0 * yc;
-                left--;
-                c0 = c1;
-                v0 = v1;
-                c1 = -1;
-                if (left > 1) { c1 = iw[at] & 255; v1 = (XT)iv[at]; at++; }
+        left = cc[BS + rr];
+        tt = tsh[qc][rr];
+        di = UPPER ? dsh[qc][rr] : XT(1);
+        c0 = c1 = -1;
+        v0 = v1 = XT(0);
+        at = io;
+        if (left > 0) {
+            c0 = iw[at] & 255;
+            v0 = (XT)iv[at];
+            at++;
+        }
+        if (left > 1) {
+            c1 = iw[at] & 255;
+            v1 = (XT)iv[at];
+            at++;
+        }
+    }
+
+    __device__ __forceinline__ void step(int s)
+    {
+        const int c = UPPER ? BS - 1 - s : s;
+        if (UPPER && rr == c) tt *= di;
+        const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
+        if (c0 == c) {
+            tt -= v0 * yc;
+            left--;
+            c0 = c1;
+            v0 = v1;
+            c1 = -1;
+            if (left > 1) {
+                c1 = iw[at] & 255;
+                v1 = (XT)iv[at];
+                at++;
             }
         }
-        tsh[qc][rr] = tt;
+    }
+};
+
+// One group of the compact chain layout, staged in shared memory (cw, vw: its
+// block; cnt: its per-chain row counts), for the thread of row l of chain q
+// (t: x of that row on entry): subtracts the row's external entries, then runs
+// the in-chain recurrence; the solved rows are in tsh on return (all threads
+// past a CTA barrier). NC reads y through the non-coherent path, for kernels in
+// which y's earlier rows were written by earlier kernels.
+template <typename VT, typename XT, int BS, bool UPPER, bool NC>
+__device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
+                                         XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, XT t,
+                                         const XT *y, int l, int q)
+{
+    int eo, ne;
+    cc_row_counts<BS, UPPER>(cnt + q * 2 * BS, l, eo, ne);
+    // up to 8 entries at a time, all their gathers issued before the first
+    // subtraction (one memory latency per batch); the subtractions keep the
+    // entries' order
+    for (int k0 = 0; k0 < ne; k0 += 8) {
+        VT vv[8];
+        XT yy[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const bool in = k0 + u < ne;
+            const int at = (eo + k0 + u) * 32 + q;
+            const int c = in ? (cw[at] & kColMask) : 0;
+            vv[u] = in ? vw[at] : VT(0);
+            yy[u] = in ? (NC ? __ldg(y + c) : y[c]) : XT(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (k0 + u < ne) t -= (XT)vv[u] * yy[u];
+    }
+    tsh[q][l] = t;
+    __syncthreads();
+    // In-chain recurrence, BS lanes per chain (lane = row), 32 / BS chains
+    // per warp, all warps busy.
+    if (BS > 1 || UPPER) {
+        constexpr int CPW = 32 / BS;  // chains per warp
+        const int lane = threadIdx.x & 31;
+        const int qc = l * CPW + lane / BS;
+        ChainRec<VT, XT, BS, UPPER> a;
+        a.init(d, cw, vw, cnt, tsh, dsh, ibase, qc, lane % BS);
+#pragma unroll
+        for (int s = 0; s < BS; s++) a.step(s);
+        tsh[qc][a.rr] = a.tt;
+    }
+    __syncthreads();
+}
+
+// cc_solve with two rows per thread, for a CTA of BS/2 warps (BS >= 4): the
+// thread of warp w, lane q takes rows w and w + BS/2 of chain q (t0, t1: x of
+// those rows on entry). The external entries of both rows are gathered
+// together, up to 4 of each at a time; the in-chain recurrence runs the
+// group's 32 chains as two interleaved halves of 16 (2 * 32 / BS chains per
+// warp and half). Same subtractions, in the same order, as cc_solve.
+template <typename VT, typename XT, int BS, bool UPPER>
+__device__ __forceinline__ void cc_solve2(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
+                                          XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, XT t0, XT t1,
+                                          const XT *y, int w, int q)
+{
+    static_assert(BS >= 4, "two rows per thread need at least two warps");
+    constexpr int W = BS / 2;
+    const int l0 = w, l1 = w + W;
+    int eo0, ne0, eo1, ne1;
+    cc_row_counts<BS, UPPER>(cnt + q * 2 * BS, l0, eo0, ne0);
+    cc_row_counts<BS, UPPER>(cnt + q * 2 * BS, l1, eo1, ne1);
+    const int nmax = max(ne0, ne1);
+    for (int k0 = 0; k0 < nmax; k0 += 4) {
+        VT va[4], vb[4];
+        XT ya[4], yb[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool ia = k0 + u < ne0, ib = k0 + u < ne1;
+            const int aa = (eo0 + k0 + u) * 32 + q, ab = (eo1 + k0 + u) * 32 + q;
+            const int ca = ia ? (cw[aa] & kColMask) : 0, cb = ib ? (cw[ab] & kColMask) : 0;
+            va[u] = ia ? vw[aa] : VT(0);
+            vb[u] = ib ? vw[ab] : VT(0);
+            ya[u] = ia ? __ldg(y + ca) : XT(0);
+            yb[u] = ib ? __ldg(y + cb) : XT(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (k0 + u < ne0) t0 -= (XT)va[u] * ya[u];
+            if (k0 + u < ne1) t1 -= (XT)vb[u] * yb[u];
+        }
+    }
+    tsh[q][l0] = t0;
+    tsh[q][l1] = t1;
+    __syncthreads();
+    {
+        constexpr int CPW = 32 / BS;  // chains per warp in each half
+        const int lane = threadIdx.x & 31;
+        const int qa = w * CPW + lane / BS, qb = qa + 16;
+        ChainRec<VT, XT, BS, UPPER> a, b;
+        a.init(d, cw, vw, cnt, tsh, dsh, ibase, qa, lane % BS);
+        b.init(d, cw, vw, cnt, tsh, dsh, ibase, qb, lane % BS);
+#pragma unroll
+        for (int s = 0; s < BS; s++) {
+            a.step(s);
+            b.step(s);
+        }
+        tsh[qa][a.rr] = a.tt;
+        tsh[qb][b.rr] = b.tt;
     }
     __syncthreads();
 }
@@ -1362,6 +1476,92 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
     if (!early_x && live) t = x[row];
     cc_solve<VT, XT, BS, UPPER, true>(d, cw, vw, cnt, tsh, dsh, ibase, t, y, l, q);
     if (live) y[row] = tsh[q][l];
+}
+
+// Resident CTAs per SM that k_sweep_cc2 is compiled for: 1,280 threads, i.e.
+// at most 51 registers a thread (BS = 32: 1,024 threads, 64 registers, still
+// twice the groups of k_sweep_cc's one 1,024-thread CTA).
+constexpr int cc2_min_blocks(int bs) { return bs == 32 ? 2 : 1280 / (bs * 16); }
+
+// k_sweep_cc with two rows per thread: one CTA of BS/2 warps per group, warp w
+// taking rows w and w + BS/2 of every chain (cc_solve2). Half the threads and,
+// at up to 48 registers, five CTAs per SM instead of four (BS = 16), so a
+// colour with more groups than k_sweep_cc keeps resident runs in one wave
+// (the 128^3 system's widest colours have 630-689 groups against 608 resident
+// CTAs of k_sweep_cc on 152 SMs). Same prologue, waits and error handling.
+template <typename VT, typename XT, int BS, bool UPPER>
+__global__ void __launch_bounds__(BS * 16, cc2_min_blocks(BS))
+k_sweep_cc2(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
+            const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
+            const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x)
+{
+    static_assert(BS >= 4, "two rows per thread need at least two warps");
+    constexpr int W = BS / 2;
+    extern __shared__ __align__(128) unsigned char ccs[];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ XT tsh[32][BS + 1];
+    __shared__ XT dsh[UPPER ? 32 : 1][BS + 1];
+    __shared__ int ibase[32];
+    const int g = g0 + blockIdx.x;
+    const int w = threadIdx.x >> 5, q = threadIdx.x & 31;
+    const WfGroup d = groups[g];
+    const int slots = d.emax + d.imax;
+    const unsigned cbytes = (unsigned)slots * 32u * 4u, vbytes = (unsigned)slots * 32u * (unsigned)sizeof(VT);
+    constexpr unsigned nbytes = 32u * 2u * BS;
+    int *cw = reinterpret_cast<int *>(ccs);
+    VT *vw = reinterpret_cast<VT *>(ccs + cbytes);
+    unsigned char *cnt = ccs + cbytes + vbytes;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, cbytes + vbytes + nbytes);
+        if (slots > 0) {
+            bulk_g2s(cw, col + d.off, cbytes, &bar);
+            bulk_g2s(vw, val + d.off, vbytes, &bar);
+        }
+        bulk_g2s(cnt, counts + (size_t)g * nbytes, nbytes, &bar);
+    }
+    __syncthreads();
+    const bool live = q < d.nchains;
+    const int2 ch = live ? __ldg(chains + (size_t)g * 32 + q) : make_int2(0, 0);
+    const int row0 = ch.x + w, row1 = ch.x + w + W;
+    if (UPPER) {
+        dsh[q][w] = live ? (XT)__ldg(dinv + row0) : XT(0);
+        dsh[q][w + W] = live ? (XT)__ldg(dinv + row1) : XT(0);
+    }
+    if (w == 0) {  // where each chain's in-chain entries start in the block
+        const int I = (int)((unsigned)ch.y >> 16);
+        int v = I;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (q >= o) v += u;
+        }
+        ibase[q] = v - I;
+    }
+    XT t0 = XT(0), t1 = XT(0);
+    if (early_x && live) {
+        t0 = x[row0];
+        t1 = x[row1];
+    }
+    if (!early_x) pdl_launch_dependents();
+    pdl_wait();  // the previous colour (or the producer of x) has finished
+    if (early_x) pdl_launch_dependents();
+    const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(status, 2);
+        if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
+        return;
+    }
+    if (gated(gate)) return;
+    if (!early_x && live) {
+        t0 = x[row0];
+        t1 = x[row1];
+    }
+    cc_solve2<VT, XT, BS, UPPER>(d, cw, vw, cnt, tsh, dsh, ibase, t0, t1, y, w, q);
+    if (live) {
+        y[row0] = tsh[q][w];
+        y[row1] = tsh[q][w + W];
+    }
 }
 
 // Colours [cbeg, cend) of one sweep in one cooperative launch, on the

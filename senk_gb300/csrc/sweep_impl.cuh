@@ -180,6 +180,7 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.dataflow = false;
     F.compact = false;
     F.persistent = false;
+    F.force_wide = false;
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
 }
@@ -219,6 +220,7 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.compact = true;
     F.dataflow = dataflow;
     F.persistent = false;
+    F.force_wide = false;
     F.ngroups = ng;
     F.slots_max = lay.slots_max;
     F.elems = (long long)lay.col.size();
@@ -421,6 +423,16 @@ void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaSt
         at[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
+        if constexpr (BS >= 4) {
+            if (L.wide) {
+                cfg.blockDim = dim3(BS * 16);
+                SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cc2<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p,
+                                             L.g0, (const int2 *)F.wchains.p, (const unsigned char *)F.wcounts.p,
+                                             (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, x, y,
+                                             gate, status, L.early_x));
+                continue;
+            }
+        }
         SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_cc<VT, XT, BS, UPPER>, (const WfGroup *)F.wgroups.p, L.g0,
                                      (const int2 *)F.wchains.p, (const unsigned char *)F.wcounts.p,
                                      (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate,
@@ -428,13 +440,34 @@ void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaSt
     }
 }
 
+// Dynamic shared memory limits of the per-colour kernels, and which colours
+// take the two-rows-per-thread kernel: those with more groups than one wave of
+// k_sweep_cc holds at once, when k_sweep_cc2 holds more (or all colours with
+// force_wide).
 template <typename VT, int BS, bool UPPER>
 void shape_cc(SweepFactor<VT> &F)
 {
     size_t most = 0;
     for (const auto &L : F.launches) most = std::max(most, L.smem);
-    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)std::max<size_t>(most, 48 * 1024)));
+    const int lim = (int)std::max<size_t>(most, 48 * 1024);
+    SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    if constexpr (BS >= 4) {
+        SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc2<VT, VT, BS, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       lim));
+        for (auto &L : F.launches) {
+            if (L.coop) continue;
+            if (F.force_wide) {
+                L.wide = 1;
+                continue;
+            }
+            int one = 0, two = 0;
+            SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&one, k_sweep_cc<VT, VT, BS, UPPER>, BS * 32,
+                                                                    L.smem));
+            SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&two, k_sweep_cc2<VT, VT, BS, UPPER>, BS * 16,
+                                                                    L.smem));
+            L.wide = (L.g1 - L.g0) > one * sm_count() && two > one ? 1 : 0;
+        }
+    }
 }
 
 // Shape of the cooperative launches: two staging buffers of the widest group's
@@ -662,7 +695,7 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
 {
     SENK_REQUIRE(sweep_mode == SENK_SWEEP_AUTO || sweep_mode == SENK_SWEEP_COLOURS ||
                      sweep_mode == SENK_SWEEP_DATAFLOW || sweep_mode == SENK_SWEEP_COMPACT ||
-                     sweep_mode == SENK_SWEEP_PERSISTENT,
+                     sweep_mode == SENK_SWEEP_PERSISTENT || sweep_mode == SENK_SWEEP_WIDE,
                  "unknown sweep mode");
     SENK_REQUIRE(N > 0, "N must be positive");
     SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
@@ -710,13 +743,15 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
     // per sweep. A factor whose widest group does not fit shared memory falls
     // back to row slots.
     const bool persistent = sweep_mode == SENK_SWEEP_PERSISTENT;
-    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW || persistent ||
+    const bool wide = sweep_mode == SENK_SWEEP_WIDE;
+    const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW || persistent || wide ||
                          (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == 4);
     const bool df = sweep_mode == SENK_SWEEP_DATAFLOW;
     if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s)))
         build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
     else {
         L.persistent = persistent;
+        L.force_wide = wide;
         shape_wf_bs<VT, false>(L);
     }
     // For U, "earlier" means a later colour: flip the colour numbers.
@@ -725,6 +760,7 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
     else {
         U.persistent = persistent;
+        U.force_wide = wide;
         shape_wf_bs<VT, true>(U);
     }
 }
