@@ -1198,29 +1198,29 @@ k_sweep_wf(const WfGroup *__restrict__ groups, int g0, int ng, const int2 *__res
     }
 }
 
-// Row l's place in the external entries of its chain's lane stream (rows come
-// in solve order): eo = entries of the rows solved before it, ne = its own.
-// cq: the chain's 2*BS row counts (external, then in-chain).
+// Row l's place in one of its chain's count arrays (BS bytes, one per row;
+// rows come in solve order, i.e. descending for U): eo = the sum over the rows
+// solved before l, ne = row l's own count. With BS >= 8 the counts are read as
+// 32-bit words and summed four bytes at a time (__dp4a) under a byte mask of
+// the rows that come first.
 template <int BS, bool UPPER>
 __device__ __forceinline__ void cc_row_counts(const unsigned char *cq, int l, int &eo, int &ne)
 {
     eo = 0;
     ne = 0;
     if constexpr (BS >= 8) {
-        // the chain's counts as 16-byte words (2 BS bytes per chain, 16-byte aligned)
-        const uint4 *c4 = reinterpret_cast<const uint4 *>(cq);
+        const uint32_t *cw = reinterpret_cast<const uint32_t *>(cq);
 #pragma unroll
-        for (int w = 0; w < (BS + 15) / 16; w++) {
-            const uint4 v = c4[w];
-            const unsigned words[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int b = 0; b < 16; b++) {
-                const int r = w * 16 + b;
-                if (r >= BS) break;
-                const int c = (int)((words[b >> 2] >> (8 * (b & 3))) & 255u);
-                if (r == l) ne = c;
-                if (UPPER ? r > l : r < l) eo += c;
-            }
+        for (int k = 0; k < BS / 4; k++) {
+            const uint32_t v = cw[k];
+            // rows 4k .. 4k+3 of this word solved before l: the lowest n (L),
+            // the highest n (U)
+            const int n = UPPER ? min(max(4 * k + 3 - l, 0), 4) : min(max(l - 4 * k, 0), 4);
+            uint32_t m;
+            if (UPPER) m = n == 0 ? 0u : n == 4 ? ~0u : ~((1u << (8 * (4 - n))) - 1u);
+            else m = n == 4 ? ~0u : (1u << (8 * n)) - 1u;
+            eo += (int)__dp4a(v & m, 0x01010101u, 0u);
+            if ((l >> 2) == k) ne = (int)((v >> (8 * (l & 3))) & 255u);
         }
     } else {
 #pragma unroll
@@ -1230,66 +1230,62 @@ __device__ __forceinline__ void cc_row_counts(const unsigned char *cq, int l, in
     }
 }
 
+__device__ __forceinline__ float ld_shared_volatile(const float *p)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(smem_addr(p)));
+    return v;
+}
+__device__ __forceinline__ double ld_shared_volatile(const double *p)
+{
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(smem_addr(p)));
+    return v;
+}
+
 // In-chain recurrence of one chain qc in the BS lanes [BS*k, BS*k+BS) of a warp
 // (lane = row rr): the rows are finished in solve order; the lane of the row
 // finished at step s (U: after its inverted diagonal) broadcasts it by a
-// shuffle within the chain's lanes, and every lane whose next in-chain entry is
-// that column subtracts it. A lane's entries come in the same order as the
-// steps (the reference's column order), two of them held in registers and
-// refilled from the block. Every lane of the warp calls step(s) for every s.
+// shuffle within the chain's lanes, and every lane that has an in-chain entry
+// in that column subtracts it. A lane's entries come in the same order as the
+// steps (the reference's column order): `mask` holds their columns and `at`
+// the next one's place in the block. Every lane of the warp calls step(s) for
+// every s.
 template <typename VT, typename XT, int BS, bool UPPER>
 struct ChainRec {
-    const int *iw;
     const VT *iv;
-    int left, at, c0, c1, rr;
-    XT v0, v1, tt, di;
+    int at, rr;
+    uint32_t mask;
+    XT tt, di;
 
     __device__ __forceinline__ void init(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
                                          const XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, int qc,
                                          int row)
     {
         rr = row;
-        iw = cw + d.emax * 32 + ibase[qc];
+        const int *iw = cw + d.emax * 32 + ibase[qc];
         iv = vw + d.emax * 32 + ibase[qc];
-        const unsigned char *cc = cnt + qc * 2 * BS;
-        int io = 0;
-#pragma unroll
-        for (int r = 0; r < BS; r++)
-            if (UPPER ? r > rr : r < rr) io += cc[BS + r];
-        left = cc[BS + rr];
+        int left;
+        cc_row_counts<BS, UPPER>(cnt + qc * 2 * BS + BS, rr, at, left);
+        mask = 0;
+        for (int k = 0; k < left; k++) mask |= 1u << (iw[at + k] & 255);
         tt = tsh[qc][rr];
         di = UPPER ? dsh[qc][rr] : XT(1);
-        c0 = c1 = -1;
-        v0 = v1 = XT(0);
-        at = io;
-        if (left > 0) {
-            c0 = iw[at] & 255;
-            v0 = (XT)iv[at];
-            at++;
-        }
-        if (left > 1) {
-            c1 = iw[at] & 255;
-            v1 = (XT)iv[at];
-            at++;
-        }
     }
 
     __device__ __forceinline__ void step(int s)
     {
         const int c = UPPER ? BS - 1 - s : s;
         if (UPPER && rr == c) tt *= di;
+        const bool hit = (mask >> c) & 1u;
+        // the entry's value is loaded here, beside the shuffle, rather than
+        // hoisted across the steps (which would hold up to BS values in
+        // registers)
+        const XT v = hit ? (XT)ld_shared_volatile(iv + at) : XT(0);
         const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
-        if (c0 == c) {
-            tt -= v0 * yc;
-            left--;
-            c0 = c1;
-            v0 = v1;
-            c1 = -1;
-            if (left > 1) {
-                c1 = iw[at] & 255;
-                v1 = (XT)iv[at];
-                at++;
-            }
+        if (hit) {
+            tt -= v * yc;
+            at++;
         }
     }
 };
@@ -1307,14 +1303,16 @@ __device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const 
 {
     int eo, ne;
     cc_row_counts<BS, UPPER>(cnt + q * 2 * BS, l, eo, ne);
-    // up to 8 entries at a time, all their gathers issued before the first
-    // subtraction (one memory latency per batch); the subtractions keep the
-    // entries' order
-    for (int k0 = 0; k0 < ne; k0 += 8) {
-        VT vv[8];
-        XT yy[8];
+    // up to 6 entries at a time (a 7-point stencil row's external entries in
+    // one batch; 6 keeps the kernel within 32 registers), all their gathers
+    // issued before the first subtraction (one memory latency per batch); the
+    // subtractions keep the entries' order
+    constexpr int B = 6;
+    for (int k0 = 0; k0 < ne; k0 += B) {
+        VT vv[B];
+        XT yy[B];
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
+        for (int u = 0; u < B; u++) {
             const bool in = k0 + u < ne;
             const int at = (eo + k0 + u) * 32 + q;
             const int c = in ? (cw[at] & kColMask) : 0;
@@ -1322,7 +1320,7 @@ __device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const 
             yy[u] = in ? (NC ? __ldg(y + c) : y[c]) : XT(0);
         }
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < B; u++)
             if (k0 + u < ne) t -= (XT)vv[u] * yy[u];
     }
     tsh[q][l] = t;
@@ -1400,6 +1398,10 @@ __device__ __forceinline__ void cc_solve2(const WfGroup &d, const int *cw, const
     __syncthreads();
 }
 
+// Resident CTAs per SM that k_sweep_cc is compiled for: 2,048 threads (the
+// SM's limit), i.e. at most 32 registers a thread.
+constexpr int cc_min_blocks(int bs) { return 2048 / (bs * 32) < 32 ? 2048 / (bs * 32) : 32; }
+
 // One colour per launch on the compact chain layout, one CTA of BS warps per
 // group: warp l takes row l of every chain (lane q = chain q) and subtracts
 // that row's external entries, read from the staged block at lane q's offset
@@ -1415,7 +1417,7 @@ __device__ __forceinline__ void cc_solve2(const WfGroup &d, const int *cw, const
 // only where the kernels still running cannot be writing these rows (not for
 // the first colour of a sweep). A TMA wait that runs out sets *status = 2.
 template <typename VT, typename XT, int BS, bool UPPER>
-__global__ void __launch_bounds__(BS * 32)
+__global__ void __launch_bounds__(BS * 32, cc_min_blocks(BS))
 k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
            const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
            const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x)
