@@ -1412,10 +1412,13 @@ constexpr int cc_min_blocks(int bs) { return 2048 / (bs * 32) < 32 ? 2048 / (bs 
 //
 // The group's block, its row counts (TMA) and U's inverted diagonal are read
 // before the kernel waits for the previous kernel (programmatic dependent
-// launch). With early_x, x is read before the wait too and the next kernel may
-// start its prologue only once this one has passed its wait; the host sets it
-// only where the kernels still running cannot be writing these rows (not for
-// the first colour of a sweep). A TMA wait that runs out sets *status = 2.
+// launch). With early_x, x and the gate are read before the wait too and the
+// next kernel may start its prologue only once this one has passed its wait;
+// the host sets it only where the kernels still running cannot be writing
+// these rows (not for the first colour of a sweep; only the sweeps use
+// programmatic launches, so the kernel before a sweep, and every writer of the
+// gate, has completed before its second colour starts). A TMA wait that runs
+// out sets *status = 2.
 template <typename VT, typename XT, int BS, bool UPPER>
 __global__ void __launch_bounds__(BS * 32, cc_min_blocks(BS))
 k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
@@ -1463,19 +1466,29 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         }
         ibase[q] = v - I;
     }
+    // x and the gate: before the wait where early_x allows it (the gate's
+    // writer precedes the sweep), else right after it, so that their loads
+    // overlap the staging wait
     XT t = XT(0);
-    if (early_x && live) t = x[row];
+    bool skip = false;
+    if (early_x) {
+        if (live) t = x[row];
+        skip = gated(gate);
+    }
     if (!early_x) pdl_launch_dependents();
     pdl_wait();  // the previous colour (or the producer of x) has finished
     if (early_x) pdl_launch_dependents();
+    else {
+        skip = gated(gate);
+        if (live) t = x[row];
+    }
     const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
     if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) atomicExch(status, 2);
         if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
         return;
     }
-    if (gated(gate)) return;
-    if (!early_x && live) t = x[row];
+    if (skip) return;
     cc_solve<VT, XT, BS, UPPER, true>(d, cw, vw, cnt, tsh, dsh, ibase, t, y, l, q);
     if (live) y[row] = tsh[q][l];
 }
@@ -1541,24 +1554,31 @@ k_sweep_cc2(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__
         ibase[q] = v - I;
     }
     XT t0 = XT(0), t1 = XT(0);
-    if (early_x && live) {
-        t0 = x[row0];
-        t1 = x[row1];
+    bool skip = false;
+    if (early_x) {
+        if (live) {
+            t0 = x[row0];
+            t1 = x[row1];
+        }
+        skip = gated(gate);
     }
     if (!early_x) pdl_launch_dependents();
     pdl_wait();  // the previous colour (or the producer of x) has finished
     if (early_x) pdl_launch_dependents();
+    else {
+        skip = gated(gate);
+        if (live) {
+            t0 = x[row0];
+            t1 = x[row1];
+        }
+    }
     const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
     if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) atomicExch(status, 2);
         if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
         return;
     }
-    if (gated(gate)) return;
-    if (!early_x && live) {
-        t0 = x[row0];
-        t1 = x[row1];
-    }
+    if (skip) return;
     cc_solve2<VT, XT, BS, UPPER>(d, cw, vw, cnt, tsh, dsh, ibase, t0, t1, y, w, q);
     if (live) {
         y[row0] = tsh[q][w];
