@@ -1209,19 +1209,20 @@ __device__ __forceinline__ void cc_row_counts(const unsigned char *cq, int l, in
     eo = 0;
     ne = 0;
     if constexpr (BS >= 8) {
+        // the words before (L) or after (U) row l's word count whole; row l's
+        // own word counts its bytes below (L) or above (U) row l's
         const uint32_t *cw = reinterpret_cast<const uint32_t *>(cq);
+        const int k = l >> 2, b = 8 * (l & 3);
+        uint32_t mine = 0;
 #pragma unroll
-        for (int k = 0; k < BS / 4; k++) {
-            const uint32_t v = cw[k];
-            // rows 4k .. 4k+3 of this word solved before l: the lowest n (L),
-            // the highest n (U)
-            const int n = UPPER ? min(max(4 * k + 3 - l, 0), 4) : min(max(l - 4 * k, 0), 4);
-            uint32_t m;
-            if (UPPER) m = n == 0 ? 0u : n == 4 ? ~0u : ~((1u << (8 * (4 - n))) - 1u);
-            else m = n == 4 ? ~0u : (1u << (8 * n)) - 1u;
-            eo += (int)__dp4a(v & m, 0x01010101u, 0u);
-            if ((l >> 2) == k) ne = (int)((v >> (8 * (l & 3))) & 255u);
+        for (int j = 0; j < BS / 4; j++) {
+            const uint32_t v = cw[j];
+            if (UPPER ? j > k : j < k) eo += (int)__dp4a(v, 0x01010101u, 0u);
+            if (j == k) mine = v;
         }
+        const uint32_t m = UPPER ? (b == 24 ? 0u : ~0u << (b + 8)) : (1u << b) - 1u;
+        eo += (int)__dp4a(mine & m, 0x01010101u, 0u);
+        ne = (int)((mine >> b) & 255u);
     } else {
 #pragma unroll
         for (int r = 0; r < BS; r++)
@@ -1306,13 +1307,16 @@ __device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const 
     // up to 6 entries at a time (a 7-point stencil row's external entries in
     // one batch; 6 keeps the kernel within 32 registers), all their gathers
     // issued before the first subtraction (one memory latency per batch); the
-    // subtractions keep the entries' order
-    constexpr int B = 6;
-    for (int k0 = 0; k0 < ne; k0 += B) {
+    // second half of a batch only where a lane of the warp needs it. The
+    // subtractions keep the entries' order.
+    constexpr int B = 6, H = 3;
+    for (int k0 = 0; __any_sync(0xffffffffu, k0 < ne); k0 += B) {  // warp-uniform
         VT vv[B];
         XT yy[B];
+        const bool more = __any_sync(0xffffffffu, k0 + H < ne);
 #pragma unroll
         for (int u = 0; u < B; u++) {
+            if (u >= H && !more) break;
             const bool in = k0 + u < ne;
             const int at = (eo + k0 + u) * 32 + q;
             const int c = in ? (cw[at] & kColMask) : 0;
@@ -1320,8 +1324,10 @@ __device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const 
             yy[u] = in ? (NC ? __ldg(y + c) : y[c]) : XT(0);
         }
 #pragma unroll
-        for (int u = 0; u < B; u++)
+        for (int u = 0; u < B; u++) {
+            if (u >= H && !more) break;
             if (k0 + u < ne) t -= (XT)vv[u] * yy[u];
+        }
     }
     tsh[q][l] = t;
     __syncthreads();
