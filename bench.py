@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--eps", type=float, default=1e-8)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2", "mgs"])
     ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
-    ap.add_argument("--sweep", default="auto", choices=["auto", "colours", "dataflow", "compact", "persistent", "wide"],
+    ap.add_argument("--sweep", default="auto",
+                    choices=["auto", "colours", "dataflow", "compact", "persistent", "wide", "rows", "rows_wide"],
                     help="schedule of the ABMC triangular sweeps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -458,7 +459,8 @@ def run_gpu(args, rank, world):
     orth = {"cgs2": L.ORTH_CGS2, "cgs": L.ORTH_CGS, "mgs": L.ORTH_MGS}[args.orth]
     spmv = {"auto": L.SPMV_AUTO, "csr": L.SPMV_CSR, "sell": L.SPMV_SELL}[args.spmv]
     sweep = {"auto": L.SWEEP_AUTO, "colours": L.SWEEP_COLOURS, "dataflow": L.SWEEP_DATAFLOW,
-             "compact": L.SWEEP_COMPACT, "persistent": L.SWEEP_PERSISTENT, "wide": L.SWEEP_WIDE}[args.sweep]
+             "compact": L.SWEEP_COMPACT, "persistent": L.SWEEP_PERSISTENT, "wide": L.SWEEP_WIDE, "rows": L.SWEEP_ROWS,
+             "rows_wide": L.SWEEP_ROWS_WIDE}[args.sweep]
     outer = 10000 // args.m
     ir_outer = 20
     sysm = SV.System(Ar, Lf, Uf, L.PC_ILU_ABMC, sc, nc, 16, m_max=args.m, mixed=True, orth=orth, spmv=spmv,

@@ -77,7 +77,7 @@ typedef struct {
 #define SENK_SWEEP_AUTO 0     /* the fastest as measured: natural-order or AMC
                                  systems whose vector fits in shared memory (up to
                                  192 KB) sweep both factors in one CTA; otherwise
-                                 FP32 factors take SENK_SWEEP_COMPACT and FP64
+                                 FP32 factors take SENK_SWEEP_ROWS and FP64
                                  factors SENK_SWEEP_COLOURS */
 #define SENK_SWEEP_COLOURS 1  /* row-slot layout, one launch per colour (level set),
                                  one CTA per group */
@@ -100,6 +100,15 @@ typedef struct {
                                  per thread). COMPACT and AUTO take that kernel
                                  only for colours with more groups than one wave
                                  of one-row-per-thread CTAs holds */
+#define SENK_SWEEP_ROWS 6     /* compact chain layout with each group's external
+                                 entries chain after chain; one launch per colour,
+                                 the lanes of a chain holding its rows in every
+                                 phase (coalesced x and y, neighbouring gathers,
+                                 no CTA barrier after staging); colours with more
+                                 groups than one wave holds take two chains per
+                                 lane */
+#define SENK_SWEEP_ROWS_WIDE 7 /* as SENK_SWEEP_ROWS, two chains per lane in
+                                 every colour (ABMC block size >= 2) */
 
 /* Preconditioners and the schedules of their triangular sweeps. */
 #define SENK_PC_NONE 0

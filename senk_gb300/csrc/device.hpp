@@ -197,8 +197,12 @@ struct SweepFactor {
     // buffers; ctrl holds its barrier words)
     bool persistent = false;
     size_t cp_buf = 0;
-    // compact, per colour: every colour takes k_sweep_cc2 (SENK_SWEEP_WIDE)
+    // compact, per colour: every colour takes k_sweep_cc2 (SENK_SWEEP_WIDE), or
+    // with rowlane every colour k_sweep_rl with two chains per lane
     bool force_wide = false;
+    // compact, per colour, external entries chain-major: k_sweep_rl (lanes =
+    // rows of a chain) instead of k_sweep_cc
+    bool rowlane = false;
 };
 
 // A split ILU factorisation with its sweep schedule.

@@ -1259,19 +1259,28 @@ struct ChainRec {
     uint32_t mask;
     XT tt, di;
 
+    // iw, iv0: the chain's in-chain entries in the block; cc: its 2*BS row
+    // counts; t: the row's value after its external entries; d_inv: U's
+    // inverted diagonal of the row
+    __device__ __forceinline__ void init_at(const int *iw, const VT *iv0, const unsigned char *cc, int row, XT t,
+                                            XT d_inv)
+    {
+        rr = row;
+        iv = iv0;
+        int left;
+        cc_row_counts<BS, UPPER>(cc + BS, rr, at, left);
+        mask = 0;
+        for (int k = 0; k < left; k++) mask |= 1u << (iw[at + k] & 255);
+        tt = t;
+        di = d_inv;
+    }
+
     __device__ __forceinline__ void init(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
                                          const XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, int qc,
                                          int row)
     {
-        rr = row;
-        const int *iw = cw + d.emax * 32 + ibase[qc];
-        iv = vw + d.emax * 32 + ibase[qc];
-        int left;
-        cc_row_counts<BS, UPPER>(cnt + qc * 2 * BS + BS, rr, at, left);
-        mask = 0;
-        for (int k = 0; k < left; k++) mask |= 1u << (iw[at + k] & 255);
-        tt = tsh[qc][rr];
-        di = UPPER ? dsh[qc][rr] : XT(1);
+        init_at(cw + d.emax * 32 + ibase[qc], vw + d.emax * 32 + ibase[qc], cnt + qc * 2 * BS, row, tsh[qc][row],
+                UPPER ? dsh[qc][row] : XT(1));
     }
 
     __device__ __forceinline__ void step(int s)
@@ -1590,6 +1599,147 @@ k_sweep_cc2(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__
         y[row0] = tsh[q][w];
         y[row1] = tsh[q][w + W];
     }
+}
+
+// Resident CTAs per SM that k_sweep_rl is compiled for: one chain per lane as
+// k_sweep_cc (2,048 threads), two as k_sweep_cc2 (1,280 threads).
+constexpr int rl_min_blocks(int bs, int r) { return r == 1 ? cc_min_blocks(bs) : cc2_min_blocks(bs); }
+
+// One colour per launch on the compact chain layout with the external part
+// chain-major (make_wf_layout with chain_major), one CTA per group of 32
+// chains. Every thread holds row rr = lane % BS of R chains (chain
+// w * 32/BS + lane / BS, plus 32/R * r for the r-th), so the lanes of a chain
+// are its rows throughout: a chain's x loads and y stores are consecutive
+// words, and its rows' gathers of earlier colours fall in a few neighbouring
+// chains. Each row subtracts its external entries (the chain's stream at
+// qc * emax in the staged block, the rows of one chain in different banks),
+// then the chain's in-chain recurrence runs in the same lanes (ChainRec) with
+// the row's value already in a register, and each lane stores its row; after
+// the staging wait no CTA barrier is needed. R = 2 (BS >= 2) halves the
+// threads of a group, for colours with more groups than one wave of R = 1
+// holds. Prologue, programmatic launch, early_x, gate and error handling as in
+// k_sweep_cc.
+template <typename VT, typename XT, int BS, bool UPPER, int R>
+__global__ void __launch_bounds__(BS * 32 / R, rl_min_blocks(BS, R))
+k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
+           const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
+           const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x)
+{
+    static_assert(R == 1 || (R == 2 && BS >= 2), "two chains per lane need chains of at least two rows");
+    constexpr int CPW = 32 / BS;  // chains per warp, per r
+    extern __shared__ __align__(128) unsigned char ccs[];
+    __shared__ __align__(8) unsigned long long bar;
+    const int g = g0 + blockIdx.x;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane % BS;
+    const WfGroup d = groups[g];
+    const int slots = d.emax + d.imax;
+    const unsigned cbytes = (unsigned)slots * 32u * 4u, vbytes = (unsigned)slots * 32u * (unsigned)sizeof(VT);
+    constexpr unsigned nbytes = 32u * 2u * BS;
+    const int *cw = reinterpret_cast<const int *>(ccs);
+    const VT *vw = reinterpret_cast<const VT *>(ccs + cbytes);
+    const unsigned char *cnt = ccs + cbytes + vbytes;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_expect_tx(&bar, cbytes + vbytes + nbytes);
+        if (slots > 0) {
+            bulk_g2s(ccs, col + d.off, cbytes, &bar);
+            bulk_g2s(ccs + cbytes, val + d.off, vbytes, &bar);
+        }
+        bulk_g2s(ccs + cbytes + vbytes, counts + (size_t)g * nbytes, nbytes, &bar);
+    }
+    __syncthreads();
+    // every warp reads the group's 32 chain descriptors (lane j: chain j) and
+    // the prefix of their in-chain counts (where each chain's in-chain entries
+    // start in the block)
+    const int2 cj = __ldg(chains + (size_t)g * 32 + lane);
+    const int nin = (int)((unsigned)cj.y >> 16);
+    int incl = nin;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    int qc[R], row[R], ib[R];
+    bool live[R];
+    XT t[R], di[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        qc[r] = w * CPW + lane / BS + (32 / R) * r;
+        row[r] = __shfl_sync(0xffffffffu, cj.x, qc[r]) + rr;
+        ib[r] = __shfl_sync(0xffffffffu, incl - nin, qc[r]);
+        live[r] = qc[r] < d.nchains;
+        di[r] = UPPER && live[r] ? (XT)__ldg(dinv + row[r]) : XT(1);
+        t[r] = XT(0);
+    }
+    bool skip = false;
+    if (early_x) {
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (live[r]) t[r] = x[row[r]];
+        skip = gated(gate);
+    }
+    if (!early_x) pdl_launch_dependents();
+    pdl_wait();  // the previous colour (or the producer of x) has finished
+    if (early_x) pdl_launch_dependents();
+    else {
+        skip = gated(gate);
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (live[r]) t[r] = x[row[r]];
+    }
+    const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(status, 2);
+        if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
+        return;
+    }
+    if (skip) return;
+    // external entries, B at a time per chain with all gathers of a batch
+    // issued before its first subtraction (R = 1: the second half of a batch
+    // only where a lane of the warp needs it); each row's subtractions keep
+    // its entries' order
+    int eo[R], ne[R], nmax = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        cc_row_counts<BS, UPPER>(cnt + qc[r] * 2 * BS, rr, eo[r], ne[r]);
+        nmax = max(nmax, ne[r]);
+    }
+    constexpr int B = R == 1 ? 6 : 3, H = R == 1 ? 3 : B;
+    for (int k0 = 0; __any_sync(0xffffffffu, k0 < nmax); k0 += B) {  // warp-uniform
+        VT vv[R][B];
+        XT yy[R][B];
+        const bool more = H == B || __any_sync(0xffffffffu, k0 + H < nmax);
+#pragma unroll
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int u = 0; u < B; u++) {
+                if (u >= H && !more) break;
+                const bool in = k0 + u < ne[r];
+                const int at = qc[r] * d.emax + eo[r] + k0 + u;
+                const int c = in ? (cw[at] & kColMask) : 0;
+                vv[r][u] = in ? vw[at] : VT(0);
+                yy[r][u] = in ? __ldg(y + c) : XT(0);
+            }
+#pragma unroll
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int u = 0; u < B; u++) {
+                if (u >= H && !more) break;
+                if (k0 + u < ne[r]) t[r] -= (XT)vv[r][u] * yy[r][u];
+            }
+    }
+    // in-chain recurrence in the chain's own lanes
+    ChainRec<VT, XT, BS, UPPER> a[R];
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        a[r].init_at(cw + d.emax * 32 + ib[r], vw + d.emax * 32 + ib[r], cnt + qc[r] * 2 * BS, rr, t[r], di[r]);
+#pragma unroll
+    for (int s = 0; s < BS; s++)
+#pragma unroll
+        for (int r = 0; r < R; r++) a[r].step(s);
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (live[r]) y[row[r]] = a[r].tt;
 }
 
 // Colours [cbeg, cend) of one sweep in one cooperative launch, on the

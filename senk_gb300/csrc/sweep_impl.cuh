@@ -181,6 +181,7 @@ void build_factor(SweepFactor<VT> &F, bool upper, int N, const VT *val, const in
     F.compact = false;
     F.persistent = false;
     F.force_wide = false;
+    F.rowlane = false;
     // Host vectors are released on return: finish the copies first.
     SENK_CUDA(cudaStreamSynchronize(s));
 }
@@ -204,13 +205,13 @@ constexpr size_t kSmallSmem = 220 * 1024;
 template <typename VT>
 bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const int *cind, const int *rptr,
                      const std::vector<Group> &colours, int bs, const std::vector<int> &colour_of, bool dataflow,
-                     cudaStream_t s, const std::vector<int> *rowmap = nullptr)
+                     cudaStream_t s, const std::vector<int> *rowmap = nullptr, bool chain_major = false)
 {
     std::vector<WfColour> cr;
     for (const Group &g : colours) cr.push_back({g.p0, g.p1});
     WfLayout<VT> lay;
     if (!make_wf_layout(lay, upper, N, val, cind, rptr, cr, bs, colour_of.data(),
-                        dataflow ? kMaxWfSmem : kMaxStagedBytes, rowmap ? rowmap->data() : nullptr))
+                        dataflow ? kMaxWfSmem : kMaxStagedBytes, rowmap ? rowmap->data() : nullptr, chain_major))
         return false;
     const int ng = (int)lay.groups.size();
     F.launches.clear();
@@ -221,6 +222,7 @@ bool build_factor_wf(SweepFactor<VT> &F, bool upper, int N, const VT *val, const
     F.dataflow = dataflow;
     F.persistent = false;
     F.force_wide = false;
+    F.rowlane = chain_major;
     F.ngroups = ng;
     F.slots_max = lay.slots_max;
     F.elems = (long long)lay.col.size();
@@ -423,6 +425,24 @@ void launch_cc(const SweepFactor<VT> &F, int *status, const XT *x, XT *y, cudaSt
         at[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
+        if (F.rowlane) {
+            if constexpr (BS >= 2) {
+                if (L.wide) {
+                    cfg.blockDim = dim3(BS * 16);
+                    SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_rl<VT, XT, BS, UPPER, 2>, (const WfGroup *)F.wgroups.p,
+                                                 L.g0, (const int2 *)F.wchains.p,
+                                                 (const unsigned char *)F.wcounts.p, (const VT *)F.val.p,
+                                                 (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate, status,
+                                                 L.early_x));
+                    continue;
+                }
+            }
+            SENK_CUDA(cudaLaunchKernelEx(&cfg, k_sweep_rl<VT, XT, BS, UPPER, 1>, (const WfGroup *)F.wgroups.p, L.g0,
+                                         (const int2 *)F.wchains.p, (const unsigned char *)F.wcounts.p,
+                                         (const VT *)F.val.p, (const int *)F.col.p, (const VT *)F.dinv.p, x, y, gate,
+                                         status, L.early_x));
+            continue;
+        }
         if constexpr (BS >= 4) {
             if (L.wide) {
                 cfg.blockDim = dim3(BS * 16);
@@ -450,6 +470,28 @@ void shape_cc(SweepFactor<VT> &F)
     size_t most = 0;
     for (const auto &L : F.launches) most = std::max(most, L.smem);
     const int lim = (int)std::max<size_t>(most, 48 * 1024);
+    if (F.rowlane) {
+        SENK_CUDA(cudaFuncSetAttribute(k_sweep_rl<VT, VT, BS, UPPER, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       lim));
+        if constexpr (BS >= 2) {
+            SENK_CUDA(cudaFuncSetAttribute(k_sweep_rl<VT, VT, BS, UPPER, 2>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+            for (auto &L : F.launches) {
+                if (L.coop) continue;
+                if (F.force_wide) {
+                    L.wide = 1;
+                    continue;
+                }
+                int one = 0, two = 0;
+                SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&one, k_sweep_rl<VT, VT, BS, UPPER, 1>,
+                                                                        BS * 32, L.smem));
+                SENK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&two, k_sweep_rl<VT, VT, BS, UPPER, 2>,
+                                                                        BS * 16, L.smem));
+                L.wide = (L.g1 - L.g0) > one * sm_count() && two > one ? 1 : 0;
+            }
+        }
+        return;
+    }
     SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc<VT, VT, BS, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
     if constexpr (BS >= 4) {
         SENK_CUDA(cudaFuncSetAttribute(k_sweep_cc2<VT, VT, BS, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -695,7 +737,8 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
 {
     SENK_REQUIRE(sweep_mode == SENK_SWEEP_AUTO || sweep_mode == SENK_SWEEP_COLOURS ||
                      sweep_mode == SENK_SWEEP_DATAFLOW || sweep_mode == SENK_SWEEP_COMPACT ||
-                     sweep_mode == SENK_SWEEP_PERSISTENT || sweep_mode == SENK_SWEEP_WIDE,
+                     sweep_mode == SENK_SWEEP_PERSISTENT || sweep_mode == SENK_SWEEP_WIDE ||
+                     sweep_mode == SENK_SWEEP_ROWS || sweep_mode == SENK_SWEEP_ROWS_WIDE,
                  "unknown sweep mode");
     SENK_REQUIRE(N > 0, "N must be positive");
     SENK_REQUIRE(lval && lcind && lrptr && uval && ucind && urptr, "null factor array");
@@ -735,19 +778,22 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
         for (int p = cptr[k] * bs; p < cptr[k + 1] * bs; p++) colour_of[p] = k;
     }
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
-    // AUTO, as measured on the 128^3 system: FP32 factors on compact chains,
-    // one launch per colour (application 0.176 ms against 0.194 ms on row
-    // slots, and 1.34x instead of 2.1x the algorithmic DRAM bytes), FP64
-    // factors on row slots (0.301 ms against 0.344 ms). COLOURS: row slots;
-    // COMPACT: compact chains per colour; DATAFLOW: compact chains, one launch
-    // per sweep. A factor whose widest group does not fit shared memory falls
-    // back to row slots.
+    // AUTO, as measured on the 128^3 system: FP32 factors on compact chains
+    // with the lanes of a chain holding its rows, one launch per colour
+    // (application 0.107 ms, against 0.139 ms with a lane per chain and 0.193
+    // ms on row slots), FP64 factors on row slots (0.301 ms against 0.354 ms
+    // row-per-lane and 0.405 ms lane-per-chain). COLOURS: row slots; COMPACT:
+    // compact chains per colour, a lane per chain; ROWS: a chain's rows in its
+    // lanes; DATAFLOW: compact chains, one launch per sweep. A factor whose
+    // widest group does not fit shared memory falls back to row slots.
     const bool persistent = sweep_mode == SENK_SWEEP_PERSISTENT;
-    const bool wide = sweep_mode == SENK_SWEEP_WIDE;
+    const bool rows = sweep_mode == SENK_SWEEP_ROWS || sweep_mode == SENK_SWEEP_ROWS_WIDE ||
+                      (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == 4);
+    const bool wide = sweep_mode == SENK_SWEEP_WIDE || sweep_mode == SENK_SWEEP_ROWS_WIDE;
     const bool compact = sweep_mode == SENK_SWEEP_COMPACT || sweep_mode == SENK_SWEEP_DATAFLOW || persistent || wide ||
-                         (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == 4);
+                         rows || (sweep_mode == SENK_SWEEP_AUTO && sizeof(VT) == 4);
     const bool df = sweep_mode == SENK_SWEEP_DATAFLOW;
-    if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s)))
+    if (!(compact && build_factor_wf(L, false, N, lval, lcind, lrptr, fwd, bs, colour_of, df, s, nullptr, rows)))
         build_factor(L, false, N, lval, lcind, lrptr, fwd, nullptr, bs, &colour_of, s);
     else {
         L.persistent = persistent;
@@ -756,7 +802,7 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
     }
     // For U, "earlier" means a later colour: flip the colour numbers.
     for (int p = 0; p < N; p++) colour_of[p] = cnum - 1 - colour_of[p];
-    if (!(compact && build_factor_wf(U, true, N, uval, ucind, urptr, bwd, bs, colour_of, df, s)))
+    if (!(compact && build_factor_wf(U, true, N, uval, ucind, urptr, bwd, bs, colour_of, df, s, nullptr, rows)))
         build_factor(U, true, N, uval, ucind, urptr, bwd, nullptr, bs, &colour_of, s);
     else {
         U.persistent = persistent;

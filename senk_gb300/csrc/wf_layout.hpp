@@ -19,6 +19,11 @@
 // also 2*bs bytes: the external then the in-chain entry count of each
 // chain-local row (rows in their natural order), for kernels that split a
 // chain's rows over warps.
+//
+// chain_major: the external part instead chain after chain, entry k of lane q
+// at off + q*emax + k, with emax rounded up to an odd number (the chains'
+// streams then start in different shared-memory banks), for kernels whose
+// lanes are the rows of one chain (k_sweep_rl).
 #pragma once
 
 #include <vector_functions.h>
@@ -80,7 +85,7 @@ struct WfLayout {
 template <typename VT>
 bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const int *cind, const int *rptr,
                     const std::vector<WfColour> &colours, int bs, const int *colour_of, size_t max_smem,
-                    const int *rowmap = nullptr)
+                    const int *rowmap = nullptr, bool chain_major = false)
 {
     if (N > kColMask) throw std::invalid_argument("N too large for the compact sweep layout (2^27 rows)");
     if (bs < 1 || bs > 32 || N % bs) throw std::invalid_argument("chain length must divide N and be at most 32");
@@ -164,6 +169,7 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
     int smax = 0;
     long long off = 0;
     for (WfGroup &d : gd) {
+        if (chain_major && d.emax > 0) d.emax |= 1;
         d.off = (int)off;
         off += (long long)(d.emax + d.imax) * 32;
         if (off >= INT_MAX) throw std::invalid_argument("factor too large for 32-bit slot offsets");
@@ -199,7 +205,8 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
                         out.val[at] = val[j];
                     } else {
                         cnt[l]++;
-                        const long long at = d.off + (long long)(ke++) * 32 + q;
+                        const long long at = chain_major ? d.off + (long long)q * d.emax + ke++
+                                                         : d.off + (long long)(ke++) * 32 + q;
                         out.col[at] = (int)(((unsigned)l << kColBits) | (unsigned)c);
                         out.val[at] = val[j];
                     }

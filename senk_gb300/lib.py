@@ -19,6 +19,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_BREAKDOWN, ERR_ZERO_PIVOT = range(6)
 ORTH_CGS, ORTH_CGS2, ORTH_MGS = 0, 1, 2
 SPMV_AUTO, SPMV_CSR, SPMV_SELL = 0, 1, 2
 SWEEP_AUTO, SWEEP_COLOURS, SWEEP_DATAFLOW, SWEEP_COMPACT, SWEEP_PERSISTENT, SWEEP_WIDE = 0, 1, 2, 3, 4, 5
+SWEEP_ROWS, SWEEP_ROWS_WIDE = 6, 7
 PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC, PC_ILUB, PC_ILUB_ABMC = 0, 1, 2, 3, 4, 5
 OP_SPMV, OP_PRECOND, OP_SWEEP_L, OP_SWEEP_U, OP_DOT, OP_MULTIDOT, OP_UPDATE, OP_INNER = 0, 1, 2, 3, 4, 5, 6, 16
 F64, F32 = 0, 1

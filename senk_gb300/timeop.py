@@ -37,13 +37,15 @@ def main(argv=None):
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--reps", type=int, default=50)
-    ap.add_argument("--sweep", default="auto", choices=["auto", "colours", "dataflow", "compact", "persistent", "wide"])
+    ap.add_argument("--sweep", default="auto",
+                    choices=["auto", "colours", "dataflow", "compact", "persistent", "wide", "rows", "rows_wide"])
     ap.add_argument("--problem", default="convdiff", choices=["convdiff", "vardiff", "block27", "poisson2d"])
     ap.add_argument("--order", default="abmc", choices=["abmc", "natural"], help="poisson2d only")
     args = ap.parse_args(argv)
     dt = np.float32 if args.dtype == "f32" else np.float64
     sweep = {"auto": L.SWEEP_AUTO, "colours": L.SWEEP_COLOURS, "dataflow": L.SWEEP_DATAFLOW,
-             "compact": L.SWEEP_COMPACT, "persistent": L.SWEEP_PERSISTENT, "wide": L.SWEEP_WIDE}[args.sweep]
+             "compact": L.SWEEP_COMPACT, "persistent": L.SWEEP_PERSISTENT, "wide": L.SWEEP_WIDE, "rows": L.SWEEP_ROWS,
+             "rows_wide": L.SWEEP_ROWS_WIDE}[args.sweep]
     if args.problem == "block27":
         A, G = P.block27(args.n, seed=0), P.block27_node_graph(args.n)
         nc, sc, LPn, _ = S.GetABMCPermutation(G.cind, G.rptr, G.n, 4, False, "connect")

@@ -168,7 +168,7 @@ SWEEPS = [("natural", 16), ("amc", 16), ("abmc", 16), ("abmc", 8), ("abmc", 32),
 
 
 @pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT,
-                                   L.SWEEP_PERSISTENT, L.SWEEP_WIDE])
+                                   L.SWEEP_PERSISTENT, L.SWEEP_WIDE, L.SWEEP_ROWS, L.SWEEP_ROWS_WIDE])
 @pytest.mark.parametrize("case", ["poisson128", "convdiff24", "vardiff16"])
 @pytest.mark.parametrize("sched,bsize", SWEEPS)
 def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
@@ -202,7 +202,7 @@ def test_ilu_sweeps_f64(torch, port, case, sched, bsize, sweep):
 
 
 @pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_DATAFLOW, L.SWEEP_COLOURS, L.SWEEP_COMPACT,
-                                   L.SWEEP_PERSISTENT, L.SWEEP_WIDE])
+                                   L.SWEEP_PERSISTENT, L.SWEEP_WIDE, L.SWEEP_ROWS, L.SWEEP_ROWS_WIDE])
 @pytest.mark.parametrize("sched,bsize", [("abmc", 16), ("natural", 16), ("amc", 16), ("abmc", 4)])
 def test_ilu_sweeps_f32(torch, port, sched, bsize, sweep):
     A = P.convdiff3d(24, 0.5)
@@ -235,9 +235,9 @@ def test_ilu_sweep_golden(torch, small):
 
 def test_ilu_sweep_at_benchmark_size(torch, port):
     """The 64^3 convection-diffusion system (16,384 chains, 11 colours) against
-    the oracle under the default, dataflow, compact, cooperative and
-    two-rows-per-thread schedules, FP64 and FP32, several applications in a
-    row."""
+    the oracle under the default, dataflow, compact, cooperative,
+    two-rows-per-thread and row-per-lane schedules, FP64 and FP32, several
+    applications in a row."""
     A = P.convdiff3d(64, 0.5)
     Ar, L_, U_, sc, nc, kind, bs = _factors(A, "abmc", 16)
     v = np.random.default_rng(9).uniform(-1, 1, A.n)
@@ -245,7 +245,9 @@ def test_ilu_sweep_at_benchmark_size(torch, port):
     for T, tol, sweep in ((np.float64, 1e-12, L.SWEEP_AUTO), (np.float32, 1e-5, L.SWEEP_AUTO),
                           (np.float64, 1e-12, L.SWEEP_DATAFLOW), (np.float32, 1e-5, L.SWEEP_COMPACT),
                           (np.float64, 1e-12, L.SWEEP_PERSISTENT), (np.float32, 1e-5, L.SWEEP_PERSISTENT),
-                          (np.float64, 1e-12, L.SWEEP_WIDE), (np.float32, 1e-5, L.SWEEP_WIDE)):
+                          (np.float64, 1e-12, L.SWEEP_WIDE), (np.float32, 1e-5, L.SWEEP_WIDE),
+                          (np.float64, 1e-12, L.SWEEP_ROWS), (np.float32, 1e-5, L.SWEEP_ROWS),
+                          (np.float32, 1e-5, L.SWEEP_ROWS_WIDE)):
         pl = Plan(L_, U_, kind, sc, nc, bs, T, sweep=sweep)
         L.check("plan", pl.code)
         xd = dev(torch, v.astype(T))

@@ -131,12 +131,13 @@ def test_nonconvergence_reports_outer_times_m(c1):
 
 
 @pytest.mark.parametrize("sweep", [L.SWEEP_AUTO, L.SWEEP_COLOURS, L.SWEEP_DATAFLOW, L.SWEEP_COMPACT,
-                                   L.SWEEP_WIDE])
+                                   L.SWEEP_WIDE, L.SWEEP_ROWS, L.SWEEP_ROWS_WIDE])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_c1_abmc_sweep_schedules(port, golden, c1, sweep, dtype):
     """Every schedule of the ABMC sweeps (compact chains per colour with one or
-    two rows per thread, row slots per colour, one dataflow launch per sweep)
-    in both precisions gives the reference's iteration count."""
+    two rows per thread, or with the lanes of a chain holding its rows; row
+    slots per colour; one dataflow launch per sweep) in both precisions gives
+    the reference's iteration count."""
     A, b, nb = c1
     nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
     Ar = S.Reordering(A, LP, RP)
