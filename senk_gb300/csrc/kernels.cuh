@@ -1231,19 +1231,6 @@ __device__ __forceinline__ void cc_row_counts(const unsigned char *cq, int l, in
     }
 }
 
-__device__ __forceinline__ float ld_shared_volatile(const float *p)
-{
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(smem_addr(p)));
-    return v;
-}
-__device__ __forceinline__ double ld_shared_volatile(const double *p)
-{
-    double v;
-    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(smem_addr(p)));
-    return v;
-}
-
 // In-chain recurrence of one chain qc in the BS lanes [BS*k, BS*k+BS) of a warp
 // (lane = row rr): the rows are finished in solve order; the lane of the row
 // finished at step s (U: after its inverted diagonal) broadcasts it by a
@@ -1283,20 +1270,19 @@ struct ChainRec {
                 UPPER ? dsh[qc][row] : XT(1));
     }
 
+    // Branch-free: the next entry's value is loaded whether or not this step
+    // uses it (at most one past the chain's in-chain entries, which is still
+    // inside the CTA's staged buffers), and the step selects.
     __device__ __forceinline__ void step(int s)
     {
         const int c = UPPER ? BS - 1 - s : s;
-        if (UPPER && rr == c) tt *= di;
+        if (UPPER) tt = rr == c ? tt * di : tt;
         const bool hit = (mask >> c) & 1u;
-        // the entry's value is loaded here, beside the shuffle, rather than
-        // hoisted across the steps (which would hold up to BS values in
-        // registers)
-        const XT v = hit ? (XT)ld_shared_volatile(iv + at) : XT(0);
+        const XT v = (XT)iv[at];
         const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
-        if (hit) {
-            tt -= v * yc;
-            at++;
-        }
+        const XT nt = tt - v * yc;
+        tt = hit ? nt : tt;
+        at += hit ? 1 : 0;
     }
 };
 
