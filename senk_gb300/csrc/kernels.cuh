@@ -885,12 +885,15 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
 {
     extern __shared__ __align__(128) unsigned char sms[];
     __shared__ __align__(8) unsigned long long full[kSmallMaxBufs], empty[kSmallMaxBufs];
-    __shared__ int4 lsh[kSmallMaxBufs];  // descriptor of the level staged in each buffer
     __shared__ int abort_flag;
     if (gated(gate)) return;
-    XT *ysh = reinterpret_cast<XT *>(sms);
-    unsigned char *bufs = sms + ((size_t)n * sizeof(XT) + 127) / 128 * 128;
     const int nl = (which & 1) ? Lf.ncolours : 0, nu = (which & 2) ? Uf.ncolours : 0, steps = nl + nu;
+    // shared memory: the vector, the descriptors of all levels in processing
+    // order (copied once, so the stager reads no global memory between levels),
+    // then the staging buffers (small_smem_bytes)
+    XT *ysh = reinterpret_cast<XT *>(sms);
+    int4 *lvs = reinterpret_cast<int4 *>(sms + ((size_t)n * sizeof(XT) + 127) / 128 * 128);
+    unsigned char *bufs = reinterpret_cast<unsigned char *>(lvs) + ((size_t)steps * 16 + 127) / 128 * 128;
     const int ncons = (int)blockDim.x - 32;  // consumer threads; the last warp stages
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; b++) {
@@ -900,6 +903,8 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
         abort_flag = 0;
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) ysh[i] = x[i];
+    for (int j = threadIdx.x; j < steps; j += blockDim.x)
+        lvs[j] = j < nl ? __ldg(Lf.levels + j) : __ldg(Uf.levels + (j - nl));
     __syncthreads();
     if ((int)threadIdx.x >= ncons) {
         if ((int)threadIdx.x != ncons) return;
@@ -923,11 +928,9 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
                     break;
                 }
             }
-            const int4 lv = j < nl ? __ldg(Lf.levels + j) : __ldg(Uf.levels + (j - nl));
-            lsh[b] = lv;
             unsigned char *buf = bufs + (size_t)b * buf_bytes;
-            if (j < nl) small_stage(Lf, false, lv, buf, &full[b]);
-            else small_stage(Uf, true, lv, buf, &full[b]);
+            if (j < nl) small_stage(Lf, false, lvs[j], buf, &full[b]);
+            else small_stage(Uf, true, lvs[j], buf, &full[b]);
             issued = j + 1;
         }
         // the last use of each buffer: complete (consumed or not) before the CTA leaves
@@ -935,44 +938,51 @@ k_ilu_small(SmallFactor<VT> Lf, SmallFactor<VT> Uf, int which, const XT *x, XT *
             mbar_wait_bounded(&full[j % nbuf], (unsigned)(j / nbuf) & 1u, kWaitLimit);
         return;
     }
+    // consumers: one barrier per level. A wait that runs out sets the abort
+    // flag (and *status = 2) before the level's barrier; after it every
+    // consumer sees the flag and all leave together.
     unsigned fpar = 0u;  // bit b: parity of buffer b's next fill
     for (int k = 0, b = 0; k < steps; k++, b = b + 1 == nbuf ? 0 : b + 1) {
         const bool upper = k >= nl;
-        bool ok = mbar_wait_bounded(&full[b], (fpar >> b) & 1u, kWaitLimit);
+        const bool ok = mbar_wait_bounded(&full[b], (fpar >> b) & 1u, kWaitLimit);
         fpar ^= 1u << b;
-        if (ok && *(volatile int *)&abort_flag) ok = false;
-        if (named_bar_or(1, ncons, !ok)) {
-            if (threadIdx.x == 0 && !*(volatile int *)&abort_flag) {
-                atomicExch(status, 2);
-                *(volatile int *)&abort_flag = 1;
-            }
-            return;
+        if (!ok) {
+            atomicExch(status, 2);
+            *(volatile int *)&abort_flag = 1;
         }
-        // written by the stager before the copies it counted on full[b]
-        const int4 lv = lsh[b];
-        const int G = lv.y, e0 = lv.z, ne = lv.w;
-        const unsigned char *sb = bufs + (size_t)b * buf_bytes;
-        const WfGroup *sd = reinterpret_cast<const WfGroup *>(sb);
-        const int2 *sc = reinterpret_cast<const int2 *>(sb + G * 16);
-        const int *scol = reinterpret_cast<const int *>(sb + G * 16 + G * 256);
-        const VT *sval = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * 4);
-        const VT *sdinv = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * (4 + sizeof(VT)));
-        for (int t = threadIdx.x; t < G * 32; t += ncons) {
-            const int gi = t >> 5, lane = t & 31;
-            const WfGroup d = sd[gi];
-            if (lane >= d.nchains) continue;
-            const int2 ch = sc[t];
-            const int row = ch.x, E = ch.y & 0xffff;
-            const int base = d.off - e0 + lane;
-            XT tt = ysh[row];
-            for (int e = 0; e < E; e++) tt -= (XT)sval[base + e * 32] * ysh[scol[base + e * 32] & kColMask];
-            if (upper) tt *= (XT)sdinv[t];
-            ysh[row] = tt;
+        if (ok && !*(volatile int *)&abort_flag) {
+            const int4 lv = lvs[k];
+            const int G = lv.y, e0 = lv.z, ne = lv.w;
+            const unsigned char *sb = bufs + (size_t)b * buf_bytes;
+            const WfGroup *sd = reinterpret_cast<const WfGroup *>(sb);
+            const int2 *sc = reinterpret_cast<const int2 *>(sb + G * 16);
+            const int *scol = reinterpret_cast<const int *>(sb + G * 16 + G * 256);
+            const VT *sval = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * 4);
+            const VT *sdinv = reinterpret_cast<const VT *>(sb + G * 16 + G * 256 + (size_t)ne * (4 + sizeof(VT)));
+            for (int t = threadIdx.x; t < G * 32; t += ncons) {
+                const int gi = t >> 5, lane = t & 31;
+                const WfGroup d = sd[gi];
+                if (lane >= d.nchains) continue;
+                const int2 ch = sc[t];
+                const int row = ch.x, E = ch.y & 0xffff;
+                const int base = d.off - e0 + lane;
+                XT tt = ysh[row];
+                for (int e = 0; e < E; e++) tt -= (XT)sval[base + e * 32] * ysh[scol[base + e * 32] & kColMask];
+                if (upper) tt *= (XT)sdinv[t];
+                ysh[row] = tt;
+            }
         }
         named_bar(1, ncons);  // the level's rows are final and buffer b is free
+        if (*(volatile int *)&abort_flag) return;
         if (threadIdx.x == 0) mbar_arrive(&empty[b]);
     }
     for (int i = threadIdx.x; i < n; i += ncons) y[i] = ysh[i];
+}
+
+// Dynamic shared memory of k_ilu_small: vector, level descriptors, buffers.
+inline size_t small_smem_bytes(size_t n, size_t xt_bytes, int steps, size_t buf_bytes, int nbuf)
+{
+    return (n * xt_bytes + 127) / 128 * 128 + ((size_t)steps * 16 + 127) / 128 * 128 + (size_t)nbuf * buf_bytes;
 }
 
 // ------------------------------------------------------ dataflow sweeps

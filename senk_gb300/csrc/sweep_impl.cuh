@@ -672,7 +672,9 @@ void IluPlan<VT>::sweep_small(int which, const VT *x, VT *y, cudaStream_t s, con
                                (const int *)F.col.p, (const VT *)F.cdinv.p, (const int4 *)F.levels.p,
                                (int)F.colour_groups.size() - 1};
     };
-    const size_t smem = ((size_t)n * sizeof(VT) + 127) / 128 * 128 + (size_t)small_nbuf * small_buf;
+    const int steps = ((which & 1) ? (int)L.colour_groups.size() - 1 : 0) +
+                      ((which & 2) ? (int)U.colour_groups.size() - 1 : 0);
+    const size_t smem = small_smem_bytes((size_t)n, sizeof(VT), steps, small_buf, small_nbuf);
     // small_threads consumers and one staging warp
     k_ilu_small<VT, VT><<<1, small_threads + 32, smem, s>>>(mk(L), mk(U), which, x, y, n, gate, status.p,
                                                             (int)small_buf, small_nbuf);
@@ -722,10 +724,12 @@ void IluPlan<VT>::build_small(int N, const VT *lval, const int *lcind, const int
             most = std::max(most, (F->colour_groups[c + 1] - F->colour_groups[c]) * 32);
     small_threads = std::min(992, (most + 31) / 32 * 32);
     small_buf = (std::max(L.level_bytes, U.level_bytes) + 127) / 128 * 128;
-    const size_t vec = ((size_t)N * sizeof(VT) + 127) / 128 * 128;
-    if (vec + 2 * small_buf > kSmallSmem) return;  // a level too large to stage next to the vector
-    small_nbuf = (int)std::min<size_t>(kSmallMaxBufs, (kSmallSmem - vec) / std::max<size_t>(small_buf, 128));
-    const size_t smem = vec + (size_t)small_nbuf * small_buf;
+    // the vector and the descriptors of both factors' levels (one application)
+    const int steps = (int)L.colour_groups.size() - 1 + (int)U.colour_groups.size() - 1;
+    const size_t fixed = small_smem_bytes((size_t)N, sizeof(VT), steps, 0, 0);
+    if (fixed + 2 * small_buf > kSmallSmem) return;  // a level too large to stage next to the vector
+    small_nbuf = (int)std::min<size_t>(kSmallMaxBufs, (kSmallSmem - fixed) / std::max<size_t>(small_buf, 128));
+    const size_t smem = small_smem_bytes((size_t)N, sizeof(VT), steps, small_buf, small_nbuf);
     SENK_CUDA(cudaFuncSetAttribute(k_ilu_small<VT, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     small = true;
 }
