@@ -1506,8 +1506,9 @@ k_sweep_cc(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 
 // Resident CTAs per SM that k_sweep_cc2 is compiled for: 1,280 threads, i.e.
 // at most 51 registers a thread (BS = 32: 1,024 threads, 64 registers, still
-// twice the groups of k_sweep_cc's one 1,024-thread CTA).
-constexpr int cc2_min_blocks(int bs) { return bs == 32 ? 2 : 1280 / (bs * 16); }
+// twice the groups of k_sweep_cc's one 1,024-thread CTA), at most the SM's 32
+// CTAs.
+constexpr int cc2_min_blocks(int bs) { return bs == 32 ? 2 : 1280 / (bs * 16) < 32 ? 1280 / (bs * 16) : 32; }
 
 // k_sweep_cc with two rows per thread: one CTA of BS/2 warps per group, warp w
 // taking rows w and w + BS/2 of every chain (cc_solve2). Half the threads and,
