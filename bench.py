@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--m", type=int, default=30)
     ap.add_argument("--eps", type=float, default=1e-8)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2", "mgs"])
-    ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell"])
+    ap.add_argument("--spmv", default="auto", choices=["auto", "csr", "sell", "sell_sigma"])
     ap.add_argument("--sweep", default="auto",
                     choices=["auto", "colours", "dataflow", "compact", "persistent", "wide", "rows", "rows_wide"],
                     help="schedule of the ABMC triangular sweeps")
@@ -457,7 +457,7 @@ def run_gpu(args, rank, world):
     Ar, Lf, Uf, nc, sc, b = setup_gpu(A, xt)
     nb = float(np.linalg.norm(b))
     orth = {"cgs2": L.ORTH_CGS2, "cgs": L.ORTH_CGS, "mgs": L.ORTH_MGS}[args.orth]
-    spmv = {"auto": L.SPMV_AUTO, "csr": L.SPMV_CSR, "sell": L.SPMV_SELL}[args.spmv]
+    spmv = {"auto": L.SPMV_AUTO, "csr": L.SPMV_CSR, "sell": L.SPMV_SELL, "sell_sigma": L.SPMV_SELL_SIGMA}[args.spmv]
     sweep = {"auto": L.SWEEP_AUTO, "colours": L.SWEEP_COLOURS, "dataflow": L.SWEEP_DATAFLOW,
              "compact": L.SWEEP_COMPACT, "persistent": L.SWEEP_PERSISTENT, "wide": L.SWEEP_WIDE, "rows": L.SWEEP_ROWS,
              "rows_wide": L.SWEEP_ROWS_WIDE}[args.sweep]

@@ -60,9 +60,13 @@ typedef struct {
 #define SENK_ORTH_CGS2 1 /* classical Gram-Schmidt + one re-orthogonalisation */
 #define SENK_ORTH_MGS 2  /* modified Gram-Schmidt, the reference's order */
 
-#define SENK_SPMV_AUTO 0  /* SELL-32 for the solver's inner SpMV */
+#define SENK_SPMV_AUTO 0  /* SELL-32-sigma(256) for the solver's SpMV */
 #define SENK_SPMV_CSR 1   /* CSR, lanes per row from the mean row length */
-#define SENK_SPMV_SELL 2  /* SELL-32 built on upload */
+#define SENK_SPMV_SELL 2  /* SELL-32 built on upload, rows in order */
+#define SENK_SPMV_SELL_SIGMA 3 /* SELL-32-sigma: within each window of 256 rows
+                                  the rows are taken longest first (stable) before
+                                  they are cut into slices of 32; y is written
+                                  through the position -> row map */
 
 typedef struct {
     int orth;         /* SENK_ORTH_* */
@@ -376,6 +380,11 @@ int senk_system_gcr(senk_system *sys, double nrm_b, int outer, int m, double eps
  * e.g. include/senk_gcr.hpp:119-120); x and y are device vectors of the
  * system's dtype. Synchronous; reports a sweep whose bounded wait ran out. */
 int senk_system_apply_pc(senk_system *sys, const void *x, void *y);
+/* y = A x with the system's own SpMV (the format opt.spmv chose: SELL-32-sigma,
+ * SELL-32 or CSR; senk::sparse::SpmvCsr, include/senk_sparse.hpp:25-35, and
+ * SpmvSell, :103-121, as its solvers apply it); x and y are device vectors of
+ * the system's dtype. Synchronous. */
+int senk_system_apply_a(senk_system *sys, const void *x, void *y);
 /* Mixed-precision GCR iterative refinement on a system created with
  * desc->mixed = 1 (new, like senk_system_gmres_ir): FP64 outer residual
  * r = b - A x and update x += ||r|| d, stopping on the FP64 true residual

@@ -108,6 +108,10 @@ struct ReduceScratch {
 // ----------------------------------------------------------------- SpMV op
 
 // A on the device. CSR always (for the residual); optionally a SELL-32 copy.
+// Sorting window of the solver's SELL-32-sigma copy of A (SENK_SPMV_AUTO and
+// SENK_SPMV_SELL_SIGMA): rows taken longest first within each 256 rows.
+constexpr int kSellSigma = 256;
+
 template <typename T>
 struct SpmvOp {
     int n = 0, nnz = 0;
@@ -117,16 +121,19 @@ struct SpmvOp {
     bool use_sell = false;
     DevBuf<T> sval;
     DevBuf<int> scol, soff;
+    DevBuf<int> sperm;           // SELL-32-sigma: slice position -> row
 
     // keep_csr = false (with a SELL format): only the SELL copy stays on the device
     void upload(const T *v, const int *c, const int *r, int N, int format, cudaStream_t s, bool keep_csr = true);
     template <typename S>
     void convert_from(const SpmvOp<S> &src, int format, cudaStream_t s, bool keep_csr);
     template <typename S>
-    void sell_from_device(const S *dv, const int *dc, const int *dr, const std::vector<int> &off, cudaStream_t s);
+    void sell_from_device(const S *dv, const int *dc, const int *dr, const std::vector<int> &off,
+                          const std::vector<int> &perm, cudaStream_t s);
     void drop_csr(cudaStream_t s);
     bool has_csr = false;
     std::vector<int> sell_off;  // host copy of the SELL slice offsets
+    std::vector<int> sell_perm; // host copy of the sigma permutation (empty: rows in order)
     long long h2d = 0;          // bytes copied from the host
     // y = A x (MODE 0) or y = b - A x (MODE 1)
     void apply(const T *x, T *y, cudaStream_t s, const int *gate) const;

@@ -137,18 +137,19 @@ k_spmv_sell32(const MT *__restrict__ val, const int *__restrict__ col, const int
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_residual_sell32(const T *__restrict__ val, const int *__restrict__ col, const int *__restrict__ off,
-                  const T *__restrict__ x, const T *__restrict__ b, T *__restrict__ r, int n, double *part,
-                  unsigned *ticket, double *norm_out, double *inv_out)
+                  const int *__restrict__ perm, const T *__restrict__ x, const T *__restrict__ b,
+                  T *__restrict__ r, int n, double *part, unsigned *ticket, double *norm_out, double *inv_out)
 {
     using A = typename Acc<T>::type;
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double nacc = 0;
-    if (p < n) {
+    if (p < n) {  // positions below n hold rows (sigma windows lie within the rows)
         const int s = (int)(p >> 5), lane = (int)(p & 31);
         const int o = __ldg(off + s), w = (__ldg(off + s + 1) - o) >> 5;
         const A sum = sell_row_sum<T, T, A>(val, col, x, o, w, lane);
-        const T v = (T)((A)b[p] - sum);
-        r[p] = v;
+        const long long row = perm ? (long long)__ldg(perm + p) : p;
+        const T v = (T)((A)b[row] - sum);
+        r[row] = v;
         nacc = (double)v * (double)v;
     }
     __shared__ double sh[32];

@@ -700,6 +700,21 @@ int senk_system_apply_pc(senk_system *sys, const void *x, void *y)
     });
 }
 
+int senk_system_apply_a(senk_system *sys, const void *x, void *y)
+{
+    return guarded("senk_system_apply_a", [&] {
+        SENK_REQUIRE(sys && x && y, "null argument");
+        if (sys->d) {
+            sys->d->A.apply((const double *)x, (double *)y, sys->d->stream, nullptr);
+            SENK_CUDA(cudaStreamSynchronize(sys->d->stream));
+        } else {
+            sys->f->A.apply((const float *)x, (float *)y, sys->f->stream, nullptr);
+            SENK_CUDA(cudaStreamSynchronize(sys->f->stream));
+        }
+        return (int)kOk;
+    });
+}
+
 int senk_system_gcr_ir(senk_system *sys, double nrm_b, int max_outer, int m, double epsilon, double inner_tol,
                        int inner_cycles, senk_result *res)
 {

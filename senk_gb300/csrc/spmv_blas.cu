@@ -50,20 +50,24 @@ void launch_spmv_csr_s(const float *v, const int *c, const int *r, const float *
     else spmv_csr_dispatch<float, float, 0>(v, c, r, x, b, y, n, lanes, s, gate);
 }
 
-// CSR -> SELL-32 on the device: one warp per slice of 32 rows, lane = row;
-// slot k of the slice's row is element off[slice] + 32 k + lane. Padding reads
-// a valid x entry (the row itself) times 0. Values are converted to TD.
+// CSR -> SELL-32 on the device: one warp per slice of 32 rows, lane = slice
+// position; slot k of position q's row is element off[slice] + 32 k + lane.
+// perm (optional, SELL-32-sigma) maps position -> row (-1 past the last row).
+// Padding reads a valid x entry (column 0) times 0. Values are converted to TD.
 template <typename TS, typename TD>
 __global__ void __launch_bounds__(kThreads)
 k_csr_to_sell(const TS *__restrict__ v, const int *__restrict__ c, const int *__restrict__ r,
-              const int *__restrict__ off, TD *__restrict__ sv, int *__restrict__ sc, int n)
+              const int *__restrict__ off, const int *__restrict__ perm, TD *__restrict__ sv, int *__restrict__ sc,
+              int n)
 {
     const long long slice = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     const long long q = slice * 32 + lane;
     if (slice * 32 >= n) return;
     const int o = off[slice], w = (off[slice + 1] - o) / 32;
-    const int b = q < n ? r[q] : 0, len = q < n ? r[q + 1] - b : 0;
+    const long long row = perm ? (long long)perm[q] : (q < n ? q : -1);
+    const bool live = row >= 0 && row < n;
+    const int b = live ? r[row] : 0, len = live ? r[row + 1] - b : 0;
     for (int k = 0; k < w; k++) {
         const long long at = o + (long long)k * 32 + lane;
         if (k < len) {
@@ -71,7 +75,7 @@ k_csr_to_sell(const TS *__restrict__ v, const int *__restrict__ c, const int *__
             sc[at] = c[b + k];
         } else {
             sv[at] = TD(0);
-            sc[at] = q < n ? (int)q : 0;
+            sc[at] = live ? (int)row : 0;
         }
     }
 }
@@ -83,37 +87,63 @@ __global__ void __launch_bounds__(kThreads) k_cast(const TS *__restrict__ a, TD 
         b[i] = (TD)a[i];
 }
 
-// Slice offsets of SELL-32 from a host row pointer: slice width = longest row.
-static std::vector<int> sell_offsets(const int *r, int N)
+// Slice offsets of SELL-32 from a host row pointer: slice width = longest row
+// of the slice. sigma > 1 (SELL-32-sigma): within each window of sigma rows
+// the rows are taken longest first (stable, so equal rows keep their order);
+// perm receives position -> row (-1 past the last row, size a multiple of 32).
+static std::vector<int> sell_offsets(const int *r, int N, int sigma = 0, std::vector<int> *perm = nullptr)
 {
     const int ns = (N + 31) / 32;
+    std::vector<int> pos;  // position -> row
+    if (sigma > 1) {
+        pos.assign((size_t)ns * 32, -1);
+        for (int w0 = 0; w0 < N; w0 += sigma) {
+            const int w1 = std::min(N, w0 + sigma);
+            for (int i = w0; i < w1; i++) pos[i] = i;
+            std::stable_sort(pos.begin() + w0, pos.begin() + w1,
+                             [&](int a, int b) { return r[a + 1] - r[a] > r[b + 1] - r[b]; });
+        }
+    }
     std::vector<int> off(ns + 1, 0);
     long long acc = 0;
     for (int i = 0; i < ns; i++) {
         int w = 0;
         const int e = std::min(N, i * 32 + 32);
-        for (int q = i * 32; q < e; q++) w = std::max(w, r[q + 1] - r[q]);
+        for (int q = i * 32; q < e; q++) {
+            const int row = pos.empty() ? q : pos[q];
+            w = std::max(w, r[row + 1] - r[row]);
+        }
         acc += 32LL * w;
         SENK_REQUIRE(acc < INT_MAX, "matrix too large for SELL-32 offsets");
         off[i + 1] = (int)acc;
     }
+    if (perm) *perm = std::move(pos);
     return off;
 }
 
 template <typename T>
 template <typename S>
-void SpmvOp<T>::sell_from_device(const S *dv, const int *dc, const int *dr, const std::vector<int> &off, cudaStream_t s)
+void SpmvOp<T>::sell_from_device(const S *dv, const int *dc, const int *dr, const std::vector<int> &off,
+                                 const std::vector<int> &perm, cudaStream_t s)
 {
     sell_off = off;
-    h2d += (long long)sizeof(int) * off.size();
+    sell_perm = perm;
+    h2d += (long long)sizeof(int) * (off.size() + perm.size());
     const int ns = (int)off.size() - 1;
     sval.alloc(std::max(off[ns], 1));
     scol.alloc(std::max(off[ns], 1));
     soff.alloc(off.size());
     soff.upload(off.data(), off.size(), s);
-    k_csr_to_sell<S, T><<<ceil_div((long long)ns * 32, kThreads), kThreads, 0, s>>>(dv, dc, dr, soff.p, sval.p, scol.p,
-                                                                                   n);
+    if (!perm.empty()) {
+        sperm.alloc(perm.size());
+        sperm.upload(perm.data(), perm.size(), s);
+    } else {
+        sperm.release();
+    }
+    k_csr_to_sell<S, T><<<ceil_div((long long)ns * 32, kThreads), kThreads, 0, s>>>(
+        dv, dc, dr, soff.p, perm.empty() ? nullptr : sperm.p, sval.p, scol.p, n);
     SENK_LAUNCH_CHECK();
+    if (!perm.empty()) SENK_CUDA(cudaStreamSynchronize(s));  // the host copy of perm may go away
 }
 
 template <typename T>
@@ -128,7 +158,8 @@ void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format
     // every FP64 instruction useful (GB300's FP64 pipe, not HBM, limits the
     // CSR-vector kernel). The CSR arrays go up as they are and the SELL copy is
     // built from them on the device.
-    use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_AUTO;
+    use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_SELL_SIGMA || format == SENK_SPMV_AUTO;
+    const int sigma = format == SENK_SPMV_SELL ? 0 : kSellSigma;
     val.alloc(std::max(nnz, 1));
     cind.alloc(std::max(nnz, 1));
     rptr.alloc(N + 1);
@@ -137,7 +168,11 @@ void SpmvOp<T>::upload(const T *v, const int *c, const int *r, int N, int format
     rptr.upload(r, N + 1, s);
     has_csr = true;
     h2d = (long long)(sizeof(T) + sizeof(int)) * nnz + sizeof(int) * (N + 1LL);
-    if (use_sell) sell_from_device<T>(val.p, cind.p, rptr.p, sell_offsets(r, N), s);
+    if (use_sell) {
+        std::vector<int> perm;
+        const std::vector<int> off = sell_offsets(r, N, sigma, &perm);
+        sell_from_device<T>(val.p, cind.p, rptr.p, off, perm, s);
+    }
     if (!keep_csr) drop_csr(s);
 }
 
@@ -151,17 +186,17 @@ void SpmvOp<T>::convert_from(const SpmvOp<S> &src, int format, cudaStream_t s, b
     n = src.n;
     nnz = src.nnz;
     lanes = src.lanes;
-    use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_AUTO;
+    use_sell = format == SENK_SPMV_SELL || format == SENK_SPMV_SELL_SIGMA || format == SENK_SPMV_AUTO;
     if (use_sell) {
         SENK_REQUIRE(!src.sell_off.empty() || !src.use_sell, "source SELL offsets missing");
-        std::vector<int> off = src.sell_off;
+        std::vector<int> off = src.sell_off, perm = src.sell_perm;
         if (off.empty()) {
             std::vector<int> hr(n + 1);
             SENK_CUDA(cudaMemcpyAsync(hr.data(), src.rptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
             SENK_CUDA(cudaStreamSynchronize(s));
-            off = sell_offsets(hr.data(), n);
+            off = sell_offsets(hr.data(), n, format == SENK_SPMV_SELL ? 0 : kSellSigma, &perm);
         }
-        sell_from_device<S>(src.val.p, src.cind.p, src.rptr.p, off, s);
+        sell_from_device<S>(src.val.p, src.cind.p, src.rptr.p, off, perm, s);
     }
     has_csr = keep_csr || !use_sell;
     if (has_csr) {
@@ -194,8 +229,8 @@ void SpmvOp<T>::apply(const T *x, T *y, cudaStream_t s, const int *gate) const
 {
     if (use_sell) {
         const long long nthreads = ((long long)n + 31) / 32 * 32;
-        k_spmv_sell32<T, T, 0><<<ceil_div(nthreads, kThreads), kThreads, 0, s>>>(sval.p, scol.p, soff.p, nullptr, x,
-                                                                               nullptr, y, n, gate);
+        k_spmv_sell32<T, T, 0><<<ceil_div(nthreads, kThreads), kThreads, 0, s>>>(
+            sval.p, scol.p, soff.p, sell_perm.empty() ? nullptr : sperm.p, x, nullptr, y, n, gate);
         SENK_LAUNCH_CHECK();
         return;
     }
@@ -210,7 +245,8 @@ void SpmvOp<T>::residual(const T *x, const T *b, T *y, ReduceScratch &red, doubl
     if (use_sell) {
         const int grid = ceil_div(n, kThreads);
         SENK_REQUIRE(grid <= red.ctas * ReduceScratch::kMaxCols, "N too large for the reduction scratch");
-        k_residual_sell32<T><<<grid, kThreads, 0, s>>>(sval.p, scol.p, soff.p, x, b, y, n, red.part.p, red.ticket.p,
+        k_residual_sell32<T><<<grid, kThreads, 0, s>>>(sval.p, scol.p, soff.p, sell_perm.empty() ? nullptr : sperm.p,
+                                                       x, b, y, n, red.part.p, red.ticket.p,
                                                        norm_out, inv_out);
         SENK_LAUNCH_CHECK();
         return;

@@ -17,7 +17,7 @@ LIB_PATH = _build.LIB
 
 OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_BREAKDOWN, ERR_ZERO_PIVOT = range(6)
 ORTH_CGS, ORTH_CGS2, ORTH_MGS = 0, 1, 2
-SPMV_AUTO, SPMV_CSR, SPMV_SELL = 0, 1, 2
+SPMV_AUTO, SPMV_CSR, SPMV_SELL, SPMV_SELL_SIGMA = 0, 1, 2, 3
 SWEEP_AUTO, SWEEP_COLOURS, SWEEP_DATAFLOW, SWEEP_COMPACT, SWEEP_PERSISTENT, SWEEP_WIDE = 0, 1, 2, 3, 4, 5
 SWEEP_ROWS, SWEEP_ROWS_WIDE = 6, 7
 PC_NONE, PC_ILU, PC_ILU_AMC, PC_ILU_ABMC, PC_ILUB, PC_ILUB_ABMC = 0, 1, 2, 3, 4, 5
@@ -108,6 +108,7 @@ def _declare(L):
     d("senk_system_gmres_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
     d("senk_system_gcr_ir", [_P, _D, _I, _I, _D, _D, _I, Rp])
     d("senk_system_apply_pc", [_P, _P, _P])
+    d("senk_system_apply_a", [_P, _P, _P])
     d("senk_dev_ilu0_d", [_P, _P, _P, _I, _P, _I, _I, _P])
     d("senk_dropin_cache", [_I])
     d("senk_dev_ilu0_s", [_P, _P, _P, _I, _P, _I, _I, _P])

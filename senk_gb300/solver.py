@@ -283,8 +283,7 @@ class System:
                                                                  inner_cycles, C.byref(r)))
         return r
 
-    def apply_precond(self, v):
-        """K v with the system's preconditioner, host vector in and out."""
+    def _apply(self, name, v):
         v = _arr(v, self.dtype)
         out = np.empty(self.n, self.dtype)
         nb = v.nbytes
@@ -294,13 +293,21 @@ class System:
             check("senk_mem_alloc", lib().senk_mem_alloc(C.byref(dy), nb))
             try:
                 check("senk_mem_h2d", lib().senk_mem_h2d(dx, ptr(v), nb))
-                check("senk_system_apply_pc", lib().senk_system_apply_pc(self._h, dx, dy))
+                check(name, getattr(lib(), name)(self._h, dx, dy))
                 check("senk_mem_d2h", lib().senk_mem_d2h(ptr(out), dy, nb))
             finally:
                 lib().senk_mem_free(dy)
         finally:
             lib().senk_mem_free(dx)
         return out
+
+    def apply_precond(self, v):
+        """K v with the system's preconditioner, host vector in and out."""
+        return self._apply("senk_system_apply_pc", v)
+
+    def apply_a(self, v):
+        """A v with the system's own SpMV format, host vector in and out."""
+        return self._apply("senk_system_apply_a", v)
 
     def gcr_ir(self, nrm_b, max_outer, m, epsilon, inner_tol=1e-4, inner_cycles=2) -> Result:
         """FP64-outer refinement around FP32 GCR(m) (systems created with mixed=1)."""
