@@ -172,7 +172,7 @@ def learned_leg(n=64, test_seeds=(900000, 900001, 900002)):
     same system; also the FP64 true residual after 3 restart cycles of each GCR
     and the bytes one application of the network moves against ILU(0)."""
     from senk_gb300 import learned as LN
-    params = np.load(os.path.join(ROOT, "senk_gb300", "weights", "mpnn_vardiff64_t1000.npy"))
+    params = np.load(os.path.join(ROOT, "senk_gb300", "weights", "mpnn_vardiff64_t2000.npy"))
     net = LN.Net(params)
     net.set_step(1)
     rows, mb = [], None
@@ -181,7 +181,7 @@ def learned_leg(n=64, test_seeds=(900000, 900001, 900002)):
         rows.append(LN.compare_gcr(net, mb, m=20, fixed_cycles=3, gmres_m=30))
     net.close()
     return {"family": f"vardiff3d {n}^3, sigma~U[0.5,2], corr~U[4,16], ABMC 16, ILU(0), GCR(20), 1e-8",
-            "trained_on": "1000 systems x 4 pairs, 1 epoch, on the GPU (senk_gb300/weights/README.md)",
+            "trained_on": "2000 systems x 4 pairs, 1 epoch, on the GPU (senk_gb300/weights/README.md)",
             "plain_iters": [r["plain"]["iters"] for r in rows], "learned_iters": [r["learned"]["iters"] for r in rows],
             "plain_ms": [round(r["plain"]["ms"], 2) for r in rows],
             "learned_ms": [round(r["learned"]["ms"], 2) for r in rows],
