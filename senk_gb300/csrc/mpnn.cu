@@ -30,7 +30,7 @@ namespace {
 // columns: 48 KB -> 4 CTAs x 64 columns; 66 KB -> 3 CTAs x 128 columns.
 constexpr int kSmemFwd = tc_gemm_smem(128, 64);  // 48 KB of operand tiles
 constexpr int kSmemDx = tc_gemm_smem(64, 128);   // 66 KB: the 128 x 132 FP32 result tile
-constexpr int kSmemTn = 8 * 1024;                       // + 24 KB static: 7 CTAs x 64 columns
+constexpr int kSmemTn = TnLayout<64>::kBytes;    // 100 KB of pipeline stages: 2 CTAs x 64 columns
 
 constexpr int kHid = 64;
 constexpr int kLayers = 4;
@@ -725,6 +725,7 @@ static void set_smem_limits()
     SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm<64, 128, kTcDx>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemDx));
     SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm<64, 128, kTcPlain>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    kSmemDx));
+    SENK_CUDA(cudaFuncSetAttribute(k_tc_gemm_tn<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTn));
     done = true;
 }
 
@@ -945,6 +946,8 @@ int senk_dev_gemm_tn_bf16(const void *X, const void *dZ, float *out, int n, void
 {
     return guarded("senk_dev_gemm_tn_bf16", [&] {
         SENK_REQUIRE(X && dZ && out && n > 0, "null argument");
+        SENK_REQUIRE(((uintptr_t)X & 15) == 0 && ((uintptr_t)dZ & 15) == 0, "operands must be 16-byte aligned");
+        set_smem_limits();
         static DevBuf<int> st;
         if (!st.p) {
             st.alloc(1);

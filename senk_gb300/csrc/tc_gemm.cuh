@@ -213,85 +213,171 @@ k_tc_gemm(const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__r
     }
 }
 
-// out[128][64] += X^T dZ over all n nodes: X is n x 128 (bf16, row stride xld),
-// dZ is n x 64 (bf16). Split over node chunks of KC: each CTA accumulates its
-// chunks in one TMEM accumulator (lanes = the 128 columns of X, columns = the
-// 64 of dZ), transposing both tiles into the K-major layout while staging them,
-// and adds its sum to `out` with FP32 atomics. (The launch may add dynamic
-// shared memory that the kernel does not touch, to cap resident CTAs.)
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Waits until at most `pending` of this thread's committed cp.async groups are in flight.
+template <int pending>
+__device__ __forceinline__ void cp_async_wait_pending()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(pending) : "memory");
+}
+
+// Four 8x8 matrices of 16-bit elements, transposed on the way into registers
+// (thread t: row t/4, columns 2(t%4), 2(t%4)+1 of each transposed matrix; the
+// row addresses come from threads 8j..8j+7 for matrix j).
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t addr, uint32_t (&r)[4])
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr)
+                 : "memory");
+}
+
+// Stores four 8x8 matrices from the same register layout, row r of matrix j
+// to the address of thread 8j + r.
+__device__ __forceinline__ void stsm_x4(uint32_t addr, const uint32_t (&r)[4])
+{
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(r[0]),
+                 "r"(r[1]), "r"(r[2]), "r"(r[3])
+                 : "memory");
+}
+
+// Shared-memory layout of k_tc_gemm_tn<KC>: two operand stages (A = X^T tile,
+// 128 x KC, then B = dZ^T tile, 64 x KC, K-major core matrices), then two raw
+// stages (the X rows, 128 features, and the dZ rows, 64, of KC nodes, each row
+// padded by 16 bytes so that the eight rows one ldmatrix reads fall in
+// different banks).
+template <int KC>
+struct TnLayout {
+    static constexpr int kXrs = 128 * 2 + 16, kZrs = 64 * 2 + 16;  // raw row strides (bytes)
+    static constexpr int kRaw = KC * (kXrs + kZrs);                 // one raw stage
+    static constexpr int kOpA = 128 * KC * 2, kOp = kOpA + 64 * KC * 2;  // one operand stage
+    static constexpr int kBytes = 2 * kOp + 2 * kRaw;
+};
+
+// Transposes a raw stage's tile of `F` features x KC nodes (rows = nodes,
+// stride RS bytes) into the K-major operand tile (rows = features, K = nodes):
+// each warp takes groups of four 8x8 blocks (one node block, four
+// consecutive feature blocks), reads them transposed with ldmatrix and writes
+// each transposed block's rows (eight nodes of one feature, 16 bytes) to its
+// core matrix with stmatrix.
+template <int KC, int F, int RS>
+__device__ __forceinline__ void tn_transpose(const unsigned char *raw, unsigned char *op, int warp, int lane)
+{
+    constexpr int FB = F / 8, GROUPS = (KC / 8) * FB / 4;
+    static_assert(FB % 4 == 0, "four feature blocks per group");
+    const int j = lane >> 3, r = lane & 7;
+    for (int g = warp; g < GROUPS; g += 4) {
+        const int b = 4 * g + j;  // this lane's block: node block kb, feature block fb
+        const int kb = b / FB, fb = b % FB;
+        uint32_t v[4];
+        ldsm_x4_trans(smem_addr(raw + (kb * 8 + r) * RS + fb * 16), v);
+        stsm_x4(smem_addr(op + tc::kmajor_offset(fb * 8 + r, kb * 8, KC)), v);
+    }
+}
+
+// out[128][64] += X^T dZ over all n nodes: X is n x 128 (bf16, row stride xld,
+// a multiple of 8, 16-byte aligned rows), dZ is n x 64 (bf16). Split over node
+// chunks of KC: CTA b takes chunks b, b + gridDim.x, ... in a two-stage
+// pipeline: the raw rows of chunk i+1 are copied (cp.async, rows past n
+// zero-filled) while chunk i is transposed into one of two operand stages and
+// the MMAs of chunk i-1 run on the other; thread 0 issues KC/16 MMAs per chunk
+// into one TMEM accumulator (lanes = the 128 columns of X, columns = the 64 of
+// dZ) and commits them to the stage's mbarrier, which the CTA waits for before
+// it overwrites that stage. The sum is added to `out` with FP32 atomics. A wait
+// that runs out sets *status; the CTA then waits once more (bounded) for the
+// last MMAs it issued, frees its TMEM and leaves.
 template <int KC>
 __global__ void __launch_bounds__(128)
 k_tc_gemm_tn(const __nv_bfloat16 *__restrict__ X, int xld, const __nv_bfloat16 *__restrict__ dZ, int n,
              float *__restrict__ out, int *status)
 {
     static_assert(KC % 16 == 0, "KC must be a multiple of 16");
-    __shared__ __align__(1024) unsigned char sa[128 * KC * 2];
-    __shared__ __align__(1024) unsigned char sb[64 * KC * 2];
-    __shared__ __align__(8) unsigned long long bar;
+    using Lt = TnLayout<KC>;
+    extern __shared__ __align__(1024) unsigned char tns[];
+    __shared__ __align__(8) unsigned long long bar[2];
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    auto op = [&](int b) { return tns + b * Lt::kOp; };
+    auto raw = [&](int b) { return tns + 2 * Lt::kOp + b * Lt::kRaw; };
     if (warp == 0) {
         tc::tmem_alloc(&tslot, 64);
         tc::tmem_relinquish();
     }
-    if (tid == 0) mbar_init(&bar, 1);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tslot;
     constexpr uint32_t idesc = tc::idesc_bf16_f32(128, 64);
     const int nchunks = (n + KC - 1) / KC;
-    unsigned phase = 0;
-    bool ok = true, any = false;
-    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    auto stage_raw = [&](int ch, unsigned char *rw) {
         const long long n0 = (long long)ch * KC;
-        // X^T tile: element (feature i, node k) <- X[n0 + k][i]
         for (int c = tid; c < KC * 16; c += 128) {
-            const int k = c / 16, i0 = (c % 16) * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (n0 + k < n) v = *reinterpret_cast<const uint4 *>(X + (n0 + k) * xld + i0);
-            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
-#pragma unroll
-            for (int q = 0; q < 8; q++)
-                *reinterpret_cast<__nv_bfloat16 *>(sa + tc::kmajor_offset(i0 + q, k, KC)) = e[q];
+            const int k = c >> 4, q = c & 15;
+            const bool in = n0 + k < n;
+            cp_async16(rw + k * Lt::kXrs + q * 16, in ? X + (n0 + k) * xld + q * 8 : X, in);
         }
-        // dZ^T tile: element (column j, node k) <- dZ[n0 + k][j]
         for (int c = tid; c < KC * 8; c += 128) {
-            const int k = c / 8, j0 = (c % 8) * 8;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (n0 + k < n) v = *reinterpret_cast<const uint4 *>(dZ + (n0 + k) * 64 + j0);
-            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
-#pragma unroll
-            for (int q = 0; q < 8; q++)
-                *reinterpret_cast<__nv_bfloat16 *>(sb + tc::kmajor_offset(j0 + q, k, KC)) = e[q];
+            const int k = c >> 3, q = c & 7;
+            const bool in = n0 + k < n;
+            cp_async16(rw + KC * Lt::kXrs + k * Lt::kZrs + q * 16, in ? dZ + (n0 + k) * 64 + q * 8 : dZ, in);
         }
+        cp_async_commit();
+    };
+    if ((int)blockIdx.x < nchunks) stage_raw(blockIdx.x, raw(0));
+    bool ok = true;
+    int last = -1;  // the last iteration whose MMAs were issued
+    for (int it = 0, ch = blockIdx.x; ch < nchunks; it++, ch += gridDim.x) {
+        const int b = it & 1;
+        if (ch + (int)gridDim.x < nchunks) {
+            stage_raw(ch + gridDim.x, raw(b ^ 1));  // read (transposed) in the previous iteration
+            cp_async_wait_pending<1>();
+        } else {
+            cp_async_wait_pending<0>();
+        }
+        __syncthreads();  // chunk ch's raw rows are in raw[b]
+        if (it >= 2) {    // the MMAs of iteration it-2 read op[b]
+            const bool done = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) - 1) & 1u, kTcWaitLimit);
+            if (__syncthreads_or(!done)) {
+                if (tid == 0) atomicExch(status, 1);
+                ok = false;
+                break;
+            }
+        }
+        tn_transpose<KC, 128, Lt::kXrs>(raw(b), op(b), warp, lane);
+        tn_transpose<KC, 64, Lt::kZrs>(raw(b) + KC * Lt::kXrs, op(b) + Lt::kOpA, warp, lane);
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
         if (tid == 0) {
-            const uint32_t a0 = smem_addr(sa), b0 = smem_addr(sb);
+            const uint32_t a0 = smem_addr(op(b)), b0 = smem_addr(op(b) + Lt::kOpA);
 #pragma unroll
             for (int s = 0; s < KC / 16; s++) {
                 const uint64_t ad = tc::smem_desc(a0 + 256u * s, tc::kLbo, KC * 16);
                 const uint64_t bd = tc::smem_desc(b0 + 256u * s, tc::kLbo, KC * 16);
-                tc::mma_bf16(tbase, ad, bd, idesc, (any || s > 0) ? 1u : 0u);
+                tc::mma_bf16(tbase, ad, bd, idesc, (it > 0 || s > 0) ? 1u : 0u);
             }
-            tc::mma_commit(&bar);
+            tc::mma_commit(&bar[b]);
         }
-        any = true;
-        // the tiles are overwritten next: wait for the MMAs that read them
-        bool done = mbar_wait_bounded(&bar, phase, kTcWaitLimit);
-        phase ^= 1u;
+        last = it;
+    }
+    cp_async_wait_pending<0>();  // copies still in flight (after an abort) land before the CTA leaves
+    if (last >= 0) {
+        // the last commit covers every MMA issued before it
+        const bool done = mbar_wait_bounded(&bar[last & 1], (unsigned)(last >> 1) & 1u, kTcWaitLimit);
         if (__syncthreads_or(!done)) {
             if (tid == 0) atomicExch(status, 1);
-            mbar_wait_bounded(&bar, phase ^ 1u, kTcWaitLimit);
+            mbar_wait_bounded(&bar[last & 1], (unsigned)(last >> 1) & 1u, kTcWaitLimit);
             ok = false;
-            break;
         }
-        tc::fence_after_sync();
     }
-    if (ok && any) {
+    tc::fence_after_sync();
+    if (ok && last >= 0) {
         const int i = warp * 32 + lane;
 #pragma unroll
         for (int c0 = 0; c0 < 64; c0 += 16) {
