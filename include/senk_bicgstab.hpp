@@ -50,11 +50,17 @@ template <typename T, int bnl, int bnw>
 void IlubBicgstab(T *val, int *cind, int *rptr, T *blval, int *blcind, int *blrptr, T *buval, int *bucind,
                   int *burptr, T *b, T *x, T nrm_b, int max_iter, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "IlubBicgstab: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_ilub_bicgstab_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b,
-                                       max_iter, N, epsilon, bnl, bnw, &o, nullptr),
-                  "senk_ilub_bicgstab_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_ilub_bicgstab_s(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x,
+                                           nrm_b, max_iter, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_ilub_bicgstab_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "IlubBicgstab: T must be double or float");
+        device::Check(senk_ilub_bicgstab_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x,
+                                           nrm_b, max_iter, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_ilub_bicgstab_d");
+    }
 }
 
 }  // namespace solver

@@ -48,11 +48,17 @@ template <typename T, int bnl, int bnw>
 void IlubGcrm(T *val, int *cind, int *rptr, T *blval, int *blcind, int *blrptr, T *buval, int *bucind, int *burptr,
               T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "IlubGcrm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_ilub_gcr_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, outer,
-                                  m, N, epsilon, bnl, bnw, &o, nullptr),
-                  "senk_ilub_gcr_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_ilub_gcr_s(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b,
+                                      outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_ilub_gcr_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "IlubGcrm: T must be double or float");
+        device::Check(senk_ilub_gcr_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b,
+                                      outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_ilub_gcr_d");
+    }
 }
 
 }  // namespace solver

@@ -34,11 +34,16 @@ void Gmresm(T *val, int *cind, int *rptr, T *b, T *x, T nrm_b, int outer, int m,
 template <typename T, int bnl, int bnw>
 void Gmresm(T *bval, int *bcind, int *brptr, T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "Gmresm<T,bnl,bnw>: the GPU library implements T = double");
     senk_options o = device::Printing();
     o.orth = SENK_ORTH_MGS;
-    device::Check(senk_bcsr_gmres_d(bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, &o, nullptr),
-                  "senk_bcsr_gmres_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_bcsr_gmres_s(bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_bcsr_gmres_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "Gmresm<T,bnl,bnw>: T must be double or float");
+        device::Check(senk_bcsr_gmres_d(bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_bcsr_gmres_d");
+    }
 }
 
 /** IluGmresm<T> (:197-270): right ILU-preconditioned GMRES(m). */
@@ -100,11 +105,17 @@ template <typename T>
 void BjIluGmresm(T *val, int *cind, int *rptr, T *lval, int *lcind, int *lrptr, T *uval, int *ucind, int *urptr,
                  int bnum, T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "BjIluGmresm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_bj_ilu_gmres_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, bnum, b, x, nrm_b,
-                                      outer, m, N, epsilon, &o, nullptr),
-                  "senk_bj_ilu_gmres_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_bj_ilu_gmres_s(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, bnum, b, x, nrm_b,
+                                          outer, m, N, epsilon, &o, nullptr),
+                      "senk_bj_ilu_gmres_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "BjIluGmresm: T must be double or float");
+        device::Check(senk_bj_ilu_gmres_d(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, bnum, b, x, nrm_b,
+                                          outer, m, N, epsilon, &o, nullptr),
+                      "senk_bj_ilu_gmres_d");
+    }
 }
 
 /** IlubGmresm<T,bnl,bnw> (:582-677): ILUB (BCSR factors). */
@@ -112,11 +123,17 @@ template <typename T, int bnl, int bnw>
 void IlubGmresm(T *val, int *cind, int *rptr, T *blval, int *blcind, int *blrptr, T *buval, int *bucind,
                 int *burptr, T *b, T *x, T nrm_b, int outer, int m, int N, T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "IlubGmresm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_ilub_gmres_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b,
-                                    outer, m, N, epsilon, bnl, bnw, &o, nullptr),
-                  "senk_ilub_gmres_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_ilub_gmres_s(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b,
+                                        outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_ilub_gmres_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "IlubGmresm: T must be double or float");
+        device::Check(senk_ilub_gmres_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b,
+                                        outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_ilub_gmres_d");
+    }
 }
 
 /** AbmcIlubGmresm<T,bnl,bnw> (:679-776): ILUB on an ABMC-ordered system. */
@@ -125,11 +142,17 @@ void AbmcIlubGmresm(T *val, int *cind, int *rptr, T *blval, int *blcind, int *bl
                     int *burptr, int *cptr, int cnum, int bsize, T *b, T *x, T nrm_b, int outer, int m, int N,
                     T epsilon)
 {
-    static_assert(device::IsDouble<T>::value, "AbmcIlubGmresm: the GPU library implements T = double");
     const senk_options o = device::Printing();
-    device::Check(senk_abmc_ilub_gmres_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, cptr, cnum,
-                                         bsize, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, &o, nullptr),
-                  "senk_abmc_ilub_gmres_d");
+    if constexpr (std::is_same<T, float>::value) {
+        device::Check(senk_abmc_ilub_gmres_s(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, cptr,
+                                             cnum, bsize, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_abmc_ilub_gmres_s");
+    } else {
+        static_assert(device::IsDouble<T>::value, "AbmcIlubGmresm: T must be double or float");
+        device::Check(senk_abmc_ilub_gmres_d(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, cptr,
+                                             cnum, bsize, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, &o, nullptr),
+                      "senk_abmc_ilub_gmres_d");
+    }
 }
 
 }  // namespace solver

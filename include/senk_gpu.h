@@ -316,6 +316,48 @@ int senk_ilub_bicgstab_d(const double *val, const int *cind, const int *rptr,
                          int max_iter, int N, double epsilon, int bnl, int bnw,
                          const senk_options *opt, senk_result *res);
 
+/* The FP32 forms (T = float) of the block, block-Jacobi and ILUB solvers:
+ * senk::solver::Gmresm<float,bnl,bnw> (include/senk_gmres.hpp:113-117),
+ * BjIluGmresm<float> (:487-494), IlubGmresm<float,bnl,bnw> (:582-588),
+ * AbmcIlubGmresm<float,bnl,bnw> (:679-686), IlubGcrm<float,bnl,bnw>
+ * (include/senk_gcr.hpp:163-169), IlubBicgstab<float,bnl,bnw>
+ * (include/senk_bicgstab.hpp:198-204); arguments as in the _d forms. */
+int senk_bcsr_gmres_s(const float *bval, const int *bcind, const int *brptr,
+                      const float *b, float *x, float nrm_b,
+                      int outer, int m, int N, float epsilon, int bnl, int bnw,
+                      const senk_options *opt, senk_result *res);
+int senk_bj_ilu_gmres_s(const float *val, const int *cind, const int *rptr,
+                        const float *lval, const int *lcind, const int *lrptr,
+                        const float *uval, const int *ucind, const int *urptr, int bnum,
+                        const float *b, float *x, float nrm_b,
+                        int outer, int m, int N, float epsilon,
+                        const senk_options *opt, senk_result *res);
+int senk_ilub_gmres_s(const float *val, const int *cind, const int *rptr,
+                      const float *blval, const int *blcind, const int *blrptr,
+                      const float *buval, const int *bucind, const int *burptr,
+                      const float *b, float *x, float nrm_b,
+                      int outer, int m, int N, float epsilon, int bnl, int bnw,
+                      const senk_options *opt, senk_result *res);
+int senk_abmc_ilub_gmres_s(const float *val, const int *cind, const int *rptr,
+                           const float *blval, const int *blcind, const int *blrptr,
+                           const float *buval, const int *bucind, const int *burptr,
+                           const int *cptr, int cnum, int bsize,
+                           const float *b, float *x, float nrm_b,
+                           int outer, int m, int N, float epsilon, int bnl, int bnw,
+                           const senk_options *opt, senk_result *res);
+int senk_ilub_gcr_s(const float *val, const int *cind, const int *rptr,
+                    const float *blval, const int *blcind, const int *blrptr,
+                    const float *buval, const int *bucind, const int *burptr,
+                    const float *b, float *x, float nrm_b,
+                    int outer, int m, int N, float epsilon, int bnl, int bnw,
+                    const senk_options *opt, senk_result *res);
+int senk_ilub_bicgstab_s(const float *val, const int *cind, const int *rptr,
+                         const float *blval, const int *blcind, const int *blrptr,
+                         const float *buval, const int *bucind, const int *burptr,
+                         const float *b, float *x, float nrm_b,
+                         int max_iter, int N, float epsilon, int bnl, int bnw,
+                         const senk_options *opt, senk_result *res);
+
 /* ================================================ device-resident systems ==
  * Upload once, solve many times (the timed path of the benchmark). */
 typedef struct senk_system senk_system;

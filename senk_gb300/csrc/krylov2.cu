@@ -478,6 +478,41 @@ int solve_ilub(const char *fn, Method method, const T *val, const int *cind, con
                            N, eps, opt, res, bnl, bnw);
 }
 
+// GMRES(m) on a BCSR matrix: SpmvBcsr (include/senk_sparse.hpp:70-91) sums
+// every block entry, zeros included, so the CSR form of all block entries
+// gives the same products.
+template <typename T>
+int bcsr_gmres(const char *fn, const T *bval, const int *bcind, const int *brptr, const T *b, T *x, double nrm_b,
+               int outer, int m, int N, double epsilon, int bnl, int bnw, const senk_options *opt, senk_result *res)
+{
+    std::vector<T> v;
+    std::vector<int> c, r;
+    bcsr_to_csr(bval, bcind, brptr, N, bnl, bnw, v, c, r);
+    return solve_dropin<T>(fn, kGmres, v.data(), c.data(), r.data(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                           nullptr, SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
+// Block-Jacobi ILU GMRES: the block-Jacobi factors (RemoveOffDiagonal pattern)
+// have no entries between blocks; their level sets solve every block's rows in
+// the sequential sweep's order, which is what the reference's per-block sweeps
+// compute.
+template <typename T>
+int bj_ilu_gmres(const char *fn, const T *val, const int *cind, const int *rptr, const T *lval, const int *lcind,
+                 const int *lrptr, const T *uval, const int *ucind, const int *urptr, int bnum, const T *b, T *x,
+                 double nrm_b, int outer, int m, int N, double epsilon, const senk_options *opt, senk_result *res)
+{
+    SENK_REQUIRE(bnum > 0 && N % bnum == 0, "N must be a multiple of bnum");
+    const int bs = N / bnum;
+    for (int i = 0; i < N; i++) {
+        for (int j = lrptr[i]; j < lrptr[i + 1]; j++)
+            SENK_REQUIRE(lcind[j] / bs == i / bs, "L factor couples two Jacobi blocks");
+        for (int j = urptr[i]; j < urptr[i + 1]; j++)
+            SENK_REQUIRE(ucind[j] / bs == i / bs, "U factor couples two Jacobi blocks");
+    }
+    return solve_dropin<T>(fn, kGmres, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, SENK_PC_ILU, nullptr,
+                           0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+}
+
 }  // namespace
 
 }  // namespace senkgpu
@@ -659,20 +694,8 @@ int senk_bj_ilu_gmres_d(const double *val, const int *cind, const int *rptr, con
                         const senk_options *opt, senk_result *res)
 {
     return guarded("senk_bj_ilu_gmres_d", [&] {
-        // The block-Jacobi factors (RemoveOffDiagonal pattern) have no entries
-        // between blocks; their level sets solve every block's rows in the
-        // sequential sweep's order, which is what the reference's per-block
-        // sweeps compute.
-        SENK_REQUIRE(bnum > 0 && N % bnum == 0, "N must be a multiple of bnum");
-        const int bs = N / bnum;
-        for (int i = 0; i < N; i++) {
-            for (int j = lrptr[i]; j < lrptr[i + 1]; j++)
-                SENK_REQUIRE(lcind[j] / bs == i / bs, "L factor couples two Jacobi blocks");
-            for (int j = urptr[i]; j < urptr[i + 1]; j++)
-                SENK_REQUIRE(ucind[j] / bs == i / bs, "U factor couples two Jacobi blocks");
-        }
-        return solve_dropin<double>("senk_bj_ilu_gmres_d", kGmres, val, cind, rptr, lval, lcind, lrptr, uval, ucind,
-                                    urptr, SENK_PC_ILU, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+        return bj_ilu_gmres<double>("senk_bj_ilu_gmres_d", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                                    bnum, b, x, nrm_b, outer, m, N, epsilon, opt, res);
     });
 }
 
@@ -681,14 +704,80 @@ int senk_bcsr_gmres_d(const double *bval, const int *bcind, const int *brptr, co
                       const senk_options *opt, senk_result *res)
 {
     return guarded("senk_bcsr_gmres_d", [&] {
-        // SpmvBcsr (include/senk_sparse.hpp:70-91) sums every block entry, zeros
-        // included: the CSR form of all block entries gives the same products.
-        std::vector<double> v;
-        std::vector<int> c, r;
-        bcsr_to_csr(bval, bcind, brptr, N, bnl, bnw, v, c, r);
-        return solve_dropin<double>("senk_bcsr_gmres_d", kGmres, v.data(), c.data(), r.data(), nullptr, nullptr,
-                                    nullptr, nullptr, nullptr, nullptr, SENK_PC_NONE, nullptr, 0, 0, b, x, nrm_b,
-                                    outer, m, N, epsilon, opt, res);
+        return bcsr_gmres<double>("senk_bcsr_gmres_d", bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl,
+                                  bnw, opt, res);
+    });
+}
+
+// FP32 forms of the block, block-Jacobi and ILUB drop-in solvers
+// (include/senk_gmres.hpp:113-117, 487-494, 582-588, 679-686;
+// include/senk_gcr.hpp:163-169; include/senk_bicgstab.hpp:198-204 at T = float).
+int senk_bcsr_gmres_s(const float *bval, const int *bcind, const int *brptr, const float *b, float *x, float nrm_b,
+                      int outer, int m, int N, float epsilon, int bnl, int bnw, const senk_options *opt,
+                      senk_result *res)
+{
+    return guarded("senk_bcsr_gmres_s", [&] {
+        return bcsr_gmres<float>("senk_bcsr_gmres_s", bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl,
+                                 bnw, opt, res);
+    });
+}
+
+int senk_bj_ilu_gmres_s(const float *val, const int *cind, const int *rptr, const float *lval, const int *lcind,
+                        const int *lrptr, const float *uval, const int *ucind, const int *urptr, int bnum,
+                        const float *b, float *x, float nrm_b, int outer, int m, int N, float epsilon,
+                        const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_bj_ilu_gmres_s", [&] {
+        return bj_ilu_gmres<float>("senk_bj_ilu_gmres_s", val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr,
+                                   bnum, b, x, nrm_b, outer, m, N, epsilon, opt, res);
+    });
+}
+
+int senk_ilub_gmres_s(const float *val, const int *cind, const int *rptr, const float *blval, const int *blcind,
+                      const int *blrptr, const float *buval, const int *bucind, const int *burptr, const float *b,
+                      float *x, float nrm_b, int outer, int m, int N, float epsilon, int bnl, int bnw,
+                      const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_ilub_gmres_s", [&] {
+        return solve_ilub<float>("senk_ilub_gmres_s", kGmres, val, cind, rptr, blval, blcind, blrptr, buval, bucind,
+                                 burptr, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, opt, res);
+    });
+}
+
+int senk_abmc_ilub_gmres_s(const float *val, const int *cind, const int *rptr, const float *blval,
+                           const int *blcind, const int *blrptr, const float *buval, const int *bucind,
+                           const int *burptr, const int *cptr, int cnum, int bsize, const float *b, float *x,
+                           float nrm_b, int outer, int m, int N, float epsilon, int bnl, int bnw,
+                           const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_abmc_ilub_gmres_s", [&] {
+        SENK_REQUIRE(cptr && cnum > 0, "colour pointer missing");
+        return solve_ilub<float>("senk_abmc_ilub_gmres_s", kGmres, val, cind, rptr, blval, blcind, blrptr, buval,
+                                 bucind, burptr, cptr, cnum, bsize, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, opt,
+                                 res);
+    });
+}
+
+int senk_ilub_gcr_s(const float *val, const int *cind, const int *rptr, const float *blval, const int *blcind,
+                    const int *blrptr, const float *buval, const int *bucind, const int *burptr, const float *b,
+                    float *x, float nrm_b, int outer, int m, int N, float epsilon, int bnl, int bnw,
+                    const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_ilub_gcr_s", [&] {
+        return solve_ilub<float>("senk_ilub_gcr_s", kGcr, val, cind, rptr, blval, blcind, blrptr, buval, bucind,
+                                 burptr, nullptr, 0, 0, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, opt, res);
+    });
+}
+
+int senk_ilub_bicgstab_s(const float *val, const int *cind, const int *rptr, const float *blval,
+                         const int *blcind, const int *blrptr, const float *buval, const int *bucind,
+                         const int *burptr, const float *b, float *x, float nrm_b, int max_iter, int N,
+                         float epsilon, int bnl, int bnw, const senk_options *opt, senk_result *res)
+{
+    return guarded("senk_ilub_bicgstab_s", [&] {
+        return solve_ilub<float>("senk_ilub_bicgstab_s", kBicgstab, val, cind, rptr, blval, blcind, blrptr, buval,
+                                 bucind, burptr, nullptr, 0, 0, b, x, nrm_b, max_iter, 0, N, epsilon, bnl, bnw, opt,
+                                 res);
     });
 }
 

@@ -126,6 +126,13 @@ def _declare(L):
     d("senk_ilu_bicgstab_d", [_P] * 11 + bd + [Op, Rp])
     d("senk_abmc_ilu_bicgstab_d", [_P] * 10 + [_I, _I, _P, _P] + bd + [Op, Rp])
     d("senk_ilub_bicgstab_d", [_P] * 11 + bd + [_I, _I, Op, Rp])
+    gs, bs = [_Fl, _I, _I, _I, _Fl], [_Fl, _I, _I, _Fl]
+    d("senk_bcsr_gmres_s", [_P] * 5 + gs + [_I, _I, Op, Rp])
+    d("senk_bj_ilu_gmres_s", [_P] * 9 + [_I, _P, _P] + gs + [Op, Rp])
+    d("senk_ilub_gmres_s", [_P] * 11 + gs + [_I, _I, Op, Rp])
+    d("senk_abmc_ilub_gmres_s", [_P] * 10 + [_I, _I, _P, _P] + gs + [_I, _I, Op, Rp])
+    d("senk_ilub_gcr_s", [_P] * 11 + gs + [_I, _I, Op, Rp])
+    d("senk_ilub_bicgstab_s", [_P] * 11 + bs + [_I, _I, Op, Rp])
     d("senk_system_gcr", [_P, _D, _I, _I, _D, Rp])
     d("senk_system_bicgstab", [_P, _D, _I, _D, Rp])
     d("senk_dev_spmv_csr_d", [_P, _P, _P, _P, _P, _I, _I, _P])

@@ -113,34 +113,38 @@ def _call(fn, *args):
 
 
 def BcsrGmresm(bval, bcind, brptr, b, x, nrm_b, outer, m, N, epsilon, bnl, bnw, **opt) -> Result:
-    """senk::solver::Gmresm<double,bnl,bnw> (include/senk_gmres.hpp:113-195)."""
-    k = _csr_args(np.float64, bval, bcind, brptr)
-    return _call("senk_bcsr_gmres_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+    """senk::solver::Gmresm<T,bnl,bnw> (include/senk_gmres.hpp:113-195); T from x."""
+    T = _T(x)
+    k = _csr_args(T, bval, bcind, brptr)
+    return _call("senk_bcsr_gmres" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N,
                  epsilon, bnl, bnw, C.byref(_opts(**opt)))
 
 
 def BjIluGmresm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, bnum, b, x, nrm_b, outer, m, N, epsilon,
                 **opt) -> Result:
-    """senk::solver::BjIluGmresm<double> (include/senk_gmres.hpp:487-580)."""
-    k = _csr_args(np.float64, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
-    return _call("senk_bj_ilu_gmres_d", *[ptr(a) for a in k], bnum, ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer,
+    """senk::solver::BjIluGmresm<T> (include/senk_gmres.hpp:487-580); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr)
+    return _call("senk_bj_ilu_gmres" + _sfx(T), *[ptr(a) for a in k], bnum, ptr(_arr(b, T)), ptr(x), nrm_b, outer,
                  m, N, epsilon, C.byref(_opts(**opt)))
 
 
 def IlubGmresm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, outer, m, N, epsilon,
                bnl, bnw, **opt) -> Result:
-    """senk::solver::IlubGmresm<double,bnl,bnw> (include/senk_gmres.hpp:582-677)."""
-    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
-    return _call("senk_ilub_gmres_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+    """senk::solver::IlubGmresm<T,bnl,bnw> (include/senk_gmres.hpp:582-677); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_ilub_gmres" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N,
                  epsilon, bnl, bnw, C.byref(_opts(**opt)))
 
 
 def AbmcIlubGmresm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, cptr, cnum, bsize, b, x, nrm_b,
                    outer, m, N, epsilon, bnl, bnw, **opt) -> Result:
-    """senk::solver::AbmcIlubGmresm<double,bnl,bnw> (include/senk_gmres.hpp:679-776)."""
-    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
-    return _call("senk_abmc_ilub_gmres_d", *[ptr(a) for a in k], ptr(_arr(cptr, np.int32)), cnum, bsize,
-                 ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N, epsilon, bnl, bnw, C.byref(_opts(**opt)))
+    """senk::solver::AbmcIlubGmresm<T,bnl,bnw> (include/senk_gmres.hpp:679-776); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_abmc_ilub_gmres" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(cptr, np.int32)), cnum, bsize,
+                 ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N, epsilon, bnl, bnw, C.byref(_opts(**opt)))
 
 
 def _sfx(T):
@@ -166,9 +170,10 @@ def IluGcrm(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, b, x, nrm_b
 
 def IlubGcrm(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, outer, m, N, epsilon,
              bnl, bnw, **opt) -> Result:
-    """senk::solver::IlubGcrm<double,bnl,bnw> (include/senk_gcr.hpp:163-231)."""
-    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
-    return _call("senk_ilub_gcr_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, outer, m, N,
+    """senk::solver::IlubGcrm<T,bnl,bnw> (include/senk_gcr.hpp:163-231); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_ilub_gcr" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, outer, m, N,
                  epsilon, bnl, bnw, C.byref(_opts(**opt)))
 
 
@@ -199,9 +204,10 @@ def AbmcIluBicgstab(val, cind, rptr, lval, lcind, lrptr, uval, ucind, urptr, cpt
 
 def IlubBicgstab(val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr, b, x, nrm_b, max_iter, N, epsilon,
                  bnl, bnw, **opt) -> Result:
-    """senk::solver::IlubBicgstab<double,bnl,bnw> (include/senk_bicgstab.hpp:198-267)."""
-    k = _csr_args(np.float64, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
-    return _call("senk_ilub_bicgstab_d", *[ptr(a) for a in k], ptr(_arr(b, np.float64)), ptr(x), nrm_b, max_iter,
+    """senk::solver::IlubBicgstab<T,bnl,bnw> (include/senk_bicgstab.hpp:198-267); T from x."""
+    T = _T(x)
+    k = _csr_args(T, val, cind, rptr, blval, blcind, blrptr, buval, bucind, burptr)
+    return _call("senk_ilub_bicgstab" + _sfx(T), *[ptr(a) for a in k], ptr(_arr(b, T)), ptr(x), nrm_b, max_iter,
                  N, epsilon, bnl, bnw, C.byref(_opts(**opt)))
 
 

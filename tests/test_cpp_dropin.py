@@ -30,11 +30,11 @@ def test_driver_compiles_against_the_dropin_headers(tmp_path):
 
 def test_unsupported_instantiation_fails_at_compile_time(tmp_path):
     src = tmp_path / "bad.cpp"
-    src.write_text('#include "senk.hpp"\nint main(){float*v=nullptr;int*c=nullptr;'
-                   'senk::solver::Gmresm<float,2,2>(v,c,c,v,v,1.f,1,1,4,1e-6f);}\n')
+    src.write_text('#include "senk.hpp"\nint main(){long double*v=nullptr;int*c=nullptr;'
+                   'senk::solver::Gmresm<long double,2,2>(v,c,c,v,v,1.0L,1,1,4,1e-6L);}\n')
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"), str(src)],
                        capture_output=True, text=True)
-    assert r.returncode != 0 and "the GPU library implements T = double" in r.stderr
+    assert r.returncode != 0 and "T must be double or float" in r.stderr
 
 
 @pytest.mark.gpu

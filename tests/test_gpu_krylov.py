@@ -283,3 +283,76 @@ def test_system_gcr_and_bicgstab_repeat(port, c1):
         assert its[0] == its[1] and its[2] == its[3]  # deterministic reductions
     finally:
         sy.close()
+
+
+# ------------------------------------------- FP32 block / block-Jacobi / ILUB
+
+def test_c1_float_block_solvers(port, c1):
+    """The T = float forms of Gmresm<T,2,2> (BCSR), BjIluGmresm, IlubGmresm,
+    AbmcIlubGmresm, IlubGcrm and IlubBicgstab on the 2D Poisson 128^2 system,
+    against the oracle's own FP32 solves of the same method: iteration counts
+    within 2 (GMRES), one restart (GCR, which tests at restarts) or 5
+    (BiCGStab, whose count moves with the association of its dot products),
+    and the true residual."""
+    import oracle as O
+    A, b, _ = c1
+    f32 = np.float32
+    bf = b.astype(f32)
+    nb = float(np.float32(np.sqrt(np.dot(b, b))))
+    eps = 1e-6
+
+    def fresh():
+        return np.zeros(A.n, f32)
+
+    def check_res(x, Am=A, bb=bf, bound=5e-6):
+        r = bb.astype(np.float64) - port.spmv_csr(Am, x.astype(np.float64))
+        assert np.linalg.norm(r) / np.linalg.norm(bb.astype(np.float64)) < bound
+
+    # GMRES(30) on the BCSR matrix (2x2 blocks, MGS as the reference's Gmresm)
+    bv, bc, brp = S.Csr2Bcsr(A, 2, 2)
+    x = fresh()
+    r = SV.BcsrGmresm(bv, bc, brp, bf, x, nb, 10000 // 30, 30, A.n, eps, 2, 2, orth=L.ORTH_MGS)
+    _, it, _, _ = port.solve("gmres", (bv, bc, brp), bf, op=O.OP_BCSR, bnl=2, bnw=2, outer=10000 // 30, m=30,
+                             eps=eps, nrm_b=nb, dtype=f32)
+    assert r.converged and near(r.iters, it), (r.iters, it)
+    check_res(x)
+    # block-Jacobi ILU(0), 16 blocks
+    Lj, Uj, _ = S.Split(S.Ilu0(S.RemoveOffDiagonal(A, 16)), "L-DU", True)
+    x = fresh()
+    r = SV.BjIluGmresm(A.val, A.cind, A.rptr, Lj.val, Lj.cind, Lj.rptr, Uj.val, Uj.cind, Uj.rptr, 16, bf, x, nb,
+                       10000 // 30, 30, A.n, eps)
+    _, it, _, _ = port.solve("gmres", A, bf, L=Lj, U=Uj, pc=O.PC_ILU_BJ, bnum=16, outer=10000 // 30, m=30, eps=eps,
+                             nrm_b=nb, dtype=f32)
+    assert r.converged and near(r.iters, it), (r.iters, it)
+    check_res(x)
+    # ILUB 8x1: GMRES(30), GCR(20) (FP32 GCR(20) levels off near 1.3e-6 here,
+    # in the oracle too, so it runs to 1e-5), BiCGStab
+    bl, bu, _, _ = _ilub_factors(A, 8, 1)
+    for method, e, call, tol in (
+            ("gmres", eps, lambda x, e: SV.IlubGmresm(A.val, A.cind, A.rptr, *bl, *bu, bf, x, nb, 10000 // 30, 30,
+                                                      A.n, e, 8, 1), 2),
+            ("gcr", 1e-5, lambda x, e: SV.IlubGcrm(A.val, A.cind, A.rptr, *bl, *bu, bf, x, nb, 10000 // M_GCR,
+                                                   M_GCR, A.n, e, 8, 1), 2 * M_GCR),
+            ("bicgstab", eps, lambda x, e: SV.IlubBicgstab(A.val, A.cind, A.rptr, *bl, *bu, bf, x, nb, 10000, A.n,
+                                                           e, 8, 1), 5)):
+        x = fresh()
+        r = call(x, e)
+        kw = dict(outer=10000 // 30, m=30) if method == "gmres" else (
+            dict(outer=10000 // M_GCR, m=M_GCR) if method == "gcr" else dict(max_iter=10000))
+        _, it, _, conv = port.solve(method, A, bf, L=bl, U=bu, pc=O.PC_ILUB, bnl=8, bnw=1, eps=e, nrm_b=nb,
+                                    dtype=f32, **kw)
+        assert conv and r.converged and abs(r.iters - it) <= tol, (method, r.iters, it)
+        check_res(x, bound=5 * e)
+    # ABMC-ordered ILUB 8x1 GMRES(30)
+    nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, 16, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    La, Ua, _ = S.Split(S.Ilu0(S.AllocBlockZero(Ar, 8, 1)), "L-DU", True)
+    bla, bua = S.Csr2Bcsr(La, 8, 1), S.Csr2Bcsr(Ua, 8, 1)
+    br = bf[LP]
+    x = fresh()
+    r = SV.AbmcIlubGmresm(Ar.val, Ar.cind, Ar.rptr, *bla, *bua, sc, nc, 16, br, x, nb, 10000 // 30, 30, A.n, eps, 8,
+                          1)
+    _, it, _, _ = port.solve("gmres", Ar, br, L=bla, U=bua, pc=O.PC_ILUB_ABMC, cptr=sc, cnum=nc, bsize=16, bnl=8,
+                             bnw=1, outer=10000 // 30, m=30, eps=eps, nrm_b=nb, dtype=f32)
+    assert r.converged and near(r.iters, it), (r.iters, it)
+    check_res(x, Ar, br)
