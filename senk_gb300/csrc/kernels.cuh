@@ -1263,10 +1263,19 @@ struct ChainRec {
     __device__ __forceinline__ void init_at(const int *iw, const VT *iv0, const unsigned char *cc, int row, XT t,
                                             XT d_inv)
     {
+        int at0, left;
+        cc_row_counts<BS, UPPER>(cc + BS, row, at0, left);
+        init_with(iw, iv0, at0, left, row, t, d_inv);
+    }
+
+    // as init_at, with the row's first in-chain entry (at0) and their number
+    // (left) already known
+    __device__ __forceinline__ void init_with(const int *iw, const VT *iv0, int at0, int left, int row, XT t,
+                                              XT d_inv)
+    {
         rr = row;
         iv = iv0;
-        int left;
-        cc_row_counts<BS, UPPER>(cc + BS, rr, at, left);
+        at = at0;
         mask = 0;
         for (int k = 0; k < left; k++) mask |= 1u << (iw[at + k] & 255);
         tt = t;
@@ -1685,23 +1694,44 @@ k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         for (int r = 0; r < R; r++)
             if (live[r]) t[r] = x[row[r]];
     }
+    // each warp leaves together (its lanes shuffle below), and no CTA barrier
+    // follows: a warp that saw the staging complete may use the block
     const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
-    if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicExch(status, 2);
-        if (!ok) mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (__any_sync(0xffffffffu, !ok)) {
+        if (!ok) {
+            atomicExch(status, 2);
+            mbar_wait_bounded(&bar, 0, kWaitLimit);
+        }
         return;
     }
     if (skip) return;
+    // the row's external entries (ne, from eo on in the chain's stream) and
+    // in-chain entries (left, from at on): the counts of the chain's rows
+    // before it (L) or after it (U), one scan of both counts over the chain's
+    // lanes (16 bits each)
+    int eo[R], ne[R], at[R], left[R], nmax = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const unsigned char *cq = cnt + qc[r] * 2 * BS;
+        ne[r] = cq[rr];
+        left[r] = cq[BS + rr];
+        const int own = ne[r] | (left[r] << 16);
+        int v = own;
+#pragma unroll
+        for (int o = 1; o < BS; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o, BS);
+            if (rr >= o) v += u;
+        }
+        if (UPPER) v = __shfl_sync(0xffffffffu, v, BS - 1, BS) - v;  // rows after this one
+        else v -= own;                                                 // rows before it
+        eo[r] = v & 0xffff;
+        at[r] = v >> 16;
+        nmax = max(nmax, ne[r]);
+    }
     // external entries, B at a time per chain with all gathers of a batch
     // issued before its first subtraction (R = 1: the second half of a batch
     // only where a lane of the warp needs it); each row's subtractions keep
     // its entries' order
-    int eo[R], ne[R], nmax = 0;
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-        cc_row_counts<BS, UPPER>(cnt + qc[r] * 2 * BS, rr, eo[r], ne[r]);
-        nmax = max(nmax, ne[r]);
-    }
     constexpr int B = R == 1 ? 6 : 3, H = R == 1 ? 3 : B;
     for (int k0 = 0; __any_sync(0xffffffffu, k0 < nmax); k0 += B) {  // warp-uniform
         VT vv[R][B];
@@ -1730,7 +1760,7 @@ k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
     ChainRec<VT, XT, BS, UPPER> a[R];
 #pragma unroll
     for (int r = 0; r < R; r++)
-        a[r].init_at(cw + d.emax * 32 + ib[r], vw + d.emax * 32 + ib[r], cnt + qc[r] * 2 * BS, rr, t[r], di[r]);
+        a[r].init_with(cw + d.emax * 32 + ib[r], vw + d.emax * 32 + ib[r], at[r], left[r], rr, t[r], di[r]);
 #pragma unroll
     for (int s = 0; s < BS; s++)
 #pragma unroll
