@@ -1655,25 +1655,18 @@ k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
         bulk_g2s(ccs + cbytes + vbytes, counts + (size_t)g * nbytes, nbytes, &bar);
     }
     __syncthreads();
-    // every warp reads the group's 32 chain descriptors (lane j: chain j) and
-    // the prefix of their in-chain counts (where each chain's in-chain entries
-    // start in the block)
-    const int2 cj = __ldg(chains + (size_t)g * 32 + lane);
-    const int nin = (int)((unsigned)cj.y >> 16);
-    int incl = nin;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += u;
-    }
+    // each lane reads its chains' descriptors: first row, and where the
+    // chain's in-chain entries start in the block (the chain-major layout
+    // keeps that offset in the descriptor)
     int qc[R], row[R], ib[R];
     bool live[R];
     XT t[R], di[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
         qc[r] = w * CPW + lane / BS + (32 / R) * r;
-        row[r] = __shfl_sync(0xffffffffu, cj.x, qc[r]) + rr;
-        ib[r] = __shfl_sync(0xffffffffu, incl - nin, qc[r]);
+        const int2 cd = __ldg(chains + (size_t)g * 32 + qc[r]);
+        row[r] = cd.x + rr;
+        ib[r] = (int)((unsigned)cd.y >> 16);
         live[r] = qc[r] < d.nchains;
         di[r] = UPPER && live[r] ? (XT)__ldg(dinv + row[r]) : XT(1);
         t[r] = XT(0);
@@ -1761,13 +1754,17 @@ k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 #pragma unroll
     for (int r = 0; r < R; r++)
         a[r].init_with(cw + d.emax * 32 + ib[r], vw + d.emax * 32 + ib[r], at[r], left[r], rr, t[r], di[r]);
+    // the last step's column (L: BS - 1, U: 0) is no row's in-chain entry;
+    // it leaves U's row 0 to be scaled by its inverted diagonal
 #pragma unroll
-    for (int s = 0; s < BS; s++)
+    for (int s = 0; s < BS - 1; s++)
 #pragma unroll
         for (int r = 0; r < R; r++) a[r].step(s);
 #pragma unroll
-    for (int r = 0; r < R; r++)
+    for (int r = 0; r < R; r++) {
+        if (UPPER && rr == 0) a[r].tt *= a[r].di;
         if (live[r]) y[row[r]] = a[r].tt;
+    }
 }
 
 // Colours [cbeg, cend) of one sweep in one cooperative launch, on the

@@ -23,7 +23,9 @@
 // chain_major: the external part instead chain after chain, entry k of lane q
 // at off + q*emax + k, with emax rounded up to an odd number (the chains'
 // streams then start in different shared-memory banks), for kernels whose
-// lanes are the rows of one chain (k_sweep_rl).
+// lanes are the rows of one chain (k_sweep_rl); the chain descriptors then
+// hold ibase_q in place of I ({first row, E | ibase_q << 16}), so that a lane
+// finds its chain's in-chain entries from its own descriptor.
 #pragma once
 
 #include <vector_functions.h>
@@ -262,6 +264,16 @@ bool make_wf_layout(WfLayout<VT> &out, bool upper, int N, const VT *val, const i
     for (size_t c = 0; c + 1 < cg.size(); c++)
         for (int g = cg[c]; g < cg[c + 1]; g++)
             out.colour_slots[c] = std::max(out.colour_slots[c], gd[g].emax + gd[g].imax);
+    if (chain_major)
+        for (int g = 0; g < ng; g++) {
+            unsigned ibase = 0;
+            for (int q = 0; q < 32; q++) {
+                int2 &c = chv[(size_t)g * 32 + q];
+                const unsigned I = (unsigned)c.y >> 16;
+                c.y = (int)(((unsigned)c.y & 0xffffu) | (ibase << 16));
+                ibase += I;
+            }
+        }
     out.colour_groups = std::move(cg);
     out.groups = std::move(gd);
     out.chains = std::move(chv);
