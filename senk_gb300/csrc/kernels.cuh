@@ -1250,12 +1250,16 @@ __device__ __forceinline__ void cc_row_counts(const unsigned char *cq, int l, in
 // steps (the reference's column order): `mask` holds their columns and `at`
 // the next one's place in the block. Every lane of the warp calls step(s) for
 // every s.
+//
+// U: `sc` keeps the row's value times its inverted diagonal, recomputed after
+// every step, so the lane of column c broadcasts sc (its final value once the
+// columns after c are done) and no step selects which lane scales.
 template <typename VT, typename XT, int BS, bool UPPER>
 struct ChainRec {
     const VT *iv;
     int at, rr;
     uint32_t mask;
-    XT tt, di;
+    XT tt, di, sc;
 
     // iw, iv0: the chain's in-chain entries in the block; cc: its 2*BS row
     // counts; t: the row's value after its external entries; d_inv: U's
@@ -1280,7 +1284,11 @@ struct ChainRec {
         for (int k = 0; k < left; k++) mask |= 1u << (iw[at + k] & 255);
         tt = t;
         di = d_inv;
+        if (UPPER) sc = tt * di;
     }
+
+    // the solved row: U's scaled by its inverted diagonal
+    __device__ __forceinline__ XT out() const { return UPPER ? sc : tt; }
 
     __device__ __forceinline__ void init(const WfGroup &d, const int *cw, const VT *vw, const unsigned char *cnt,
                                          const XT (*tsh)[BS + 1], const XT (*dsh)[BS + 1], const int *ibase, int qc,
@@ -1296,12 +1304,12 @@ struct ChainRec {
     __device__ __forceinline__ void step(int s)
     {
         const int c = UPPER ? BS - 1 - s : s;
-        if (UPPER) tt = rr == c ? tt * di : tt;
         const bool hit = (mask >> c) & 1u;
         const XT v = (XT)iv[at];
-        const XT yc = __shfl_sync(0xffffffffu, tt, c, BS);
+        const XT yc = __shfl_sync(0xffffffffu, UPPER ? sc : tt, c, BS);
         const XT nt = tt - v * yc;
         tt = hit ? nt : tt;
+        if (UPPER) sc = tt * di;
         at += hit ? 1 : 0;
     }
 };
@@ -1356,7 +1364,7 @@ __device__ __forceinline__ void cc_solve(const WfGroup &d, const int *cw, const 
         a.init(d, cw, vw, cnt, tsh, dsh, ibase, qc, lane % BS);
 #pragma unroll
         for (int s = 0; s < BS; s++) a.step(s);
-        tsh[qc][a.rr] = a.tt;
+        tsh[qc][a.rr] = a.out();
     }
     __syncthreads();
 }
@@ -1413,8 +1421,8 @@ __device__ __forceinline__ void cc_solve2(const WfGroup &d, const int *cw, const
             a.step(s);
             b.step(s);
         }
-        tsh[qa][a.rr] = a.tt;
-        tsh[qb][b.rr] = b.tt;
+        tsh[qa][a.rr] = a.out();
+        tsh[qb][b.rr] = b.out();
     }
     __syncthreads();
 }
@@ -1754,17 +1762,14 @@ k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 #pragma unroll
     for (int r = 0; r < R; r++)
         a[r].init_with(cw + d.emax * 32 + ib[r], vw + d.emax * 32 + ib[r], at[r], left[r], rr, t[r], di[r]);
-    // the last step's column (L: BS - 1, U: 0) is no row's in-chain entry;
-    // it leaves U's row 0 to be scaled by its inverted diagonal
+    // the last step's column (L: BS - 1, U: 0) is no row's in-chain entry
 #pragma unroll
     for (int s = 0; s < BS - 1; s++)
 #pragma unroll
         for (int r = 0; r < R; r++) a[r].step(s);
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        if (UPPER && rr == 0) a[r].tt *= a[r].di;
-        if (live[r]) y[row[r]] = a[r].tt;
-    }
+    for (int r = 0; r < R; r++)
+        if (live[r]) y[row[r]] = a[r].out();
 }
 
 // Colours [cbeg, cend) of one sweep in one cooperative launch, on the
