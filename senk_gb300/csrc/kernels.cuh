@@ -1617,8 +1617,14 @@ k_sweep_cc2(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__
 }
 
 // Resident CTAs per SM that k_sweep_rl is compiled for: one chain per lane as
-// k_sweep_cc (2,048 threads), two as k_sweep_cc2 (1,280 threads).
-constexpr int rl_min_blocks(int bs, int r) { return r == 1 ? cc_min_blocks(bs) : cc2_min_blocks(bs); }
+// k_sweep_cc (2,048 threads), two as k_sweep_cc2 (1,280 threads); with 8-byte
+// values a quarter (one chain) or one CTA (two chains) fewer, so that the
+// doubles fit the registers without spilling.
+constexpr int rl_min_blocks(int bs, int r, int vbytes)
+{
+    return r == 1 ? (vbytes == 8 && cc_min_blocks(bs) >= 2 ? cc_min_blocks(bs) * 3 / 4 : cc_min_blocks(bs))
+                  : (vbytes == 8 && cc2_min_blocks(bs) >= 2 ? cc2_min_blocks(bs) - 1 : cc2_min_blocks(bs));
+}
 
 // One colour per launch on the compact chain layout with the external part
 // chain-major (make_wf_layout with chain_major), one CTA per group of 32
@@ -1635,7 +1641,7 @@ constexpr int rl_min_blocks(int bs, int r) { return r == 1 ? cc_min_blocks(bs) :
 // holds. Prologue, programmatic launch, early_x, gate and error handling as in
 // k_sweep_cc.
 template <typename VT, typename XT, int BS, bool UPPER, int R>
-__global__ void __launch_bounds__(BS * 32 / R, rl_min_blocks(BS, R))
+__global__ void __launch_bounds__(BS * 32 / R, rl_min_blocks(BS, R, (int)(sizeof(VT) > sizeof(XT) ? sizeof(VT) : sizeof(XT))))
 k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
            const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
            const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x)
