@@ -1298,19 +1298,17 @@ struct ChainRec {
                 UPPER ? dsh[qc][row] : XT(1));
     }
 
-    // Branch-free: the next entry's value is loaded whether or not this step
-    // uses it (at most one past the chain's in-chain entries, which is still
-    // inside the CTA's staged buffers), and the step selects.
+    // Each step's subtraction, increment and rescale are predicated on the
+    // lane's bit for the step's column.
     __device__ __forceinline__ void step(int s)
     {
         const int c = UPPER ? BS - 1 - s : s;
-        const bool hit = (mask >> c) & 1u;
-        const XT v = (XT)iv[at];
         const XT yc = __shfl_sync(0xffffffffu, UPPER ? sc : tt, c, BS);
-        const XT nt = tt - v * yc;
-        tt = hit ? nt : tt;
-        if (UPPER) sc = tt * di;
-        at += hit ? 1 : 0;
+        if (mask & (1u << c)) {  // predicated, no branch
+            tt -= (XT)iv[at] * yc;
+            at++;
+            if (UPPER) sc = tt * di;
+        }
     }
 };
 
