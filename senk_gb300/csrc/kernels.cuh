@@ -1281,7 +1281,10 @@ struct ChainRec {
         iv = iv0;
         at = at0;
         mask = 0;
-        for (int k = 0; k < left; k++) mask |= 1u << (iw[at + k] & 255);
+#pragma unroll
+        for (int k = 0; k < 3; k++)  // a 7-point row's in-chain entries, predicated
+            if (k < left) mask |= 1u << (iw[at + k] & 255);
+        for (int k = 3; k < left; k++) mask |= 1u << (iw[at + k] & 255);
         tt = t;
         di = d_inv;
         if (UPPER) sc = tt * di;
@@ -1747,11 +1750,11 @@ k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ 
 #pragma unroll
             for (int u = 0; u < B; u++) {
                 if (u >= H && !more) break;
-                const bool in = k0 + u < ne[r];
-                const int at = qc[r] * d.emax + eo[r] + k0 + u;
-                const int c = in ? (cw[at] & kColMask) : 0;
-                vv[r][u] = in ? vw[at] : VT(0);
-                yy[r][u] = in ? __ldg(y + c) : XT(0);
+                if (k0 + u < ne[r]) {  // predicated loads, nothing selected
+                    const int at = qc[r] * d.emax + eo[r] + k0 + u;
+                    vv[r][u] = vw[at];
+                    yy[r][u] = __ldg(y + (cw[at] & kColMask));
+                }
             }
 #pragma unroll
         for (int r = 0; r < R; r++)
