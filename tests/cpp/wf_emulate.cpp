@@ -4,6 +4,7 @@
 // reads, groups run in processing order, and each gathered row is checked to be
 // finished and owned by a group on the reading group's dependency list. Test
 // code only: it runs no GPU code.
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <set>
@@ -288,6 +289,125 @@ int cp_schedule(int N, const VT *val, const int *cind, const int *rptr, int uppe
 
 }  // namespace
 
+// The row-per-lane sweep (k_sweep_rl) on the chain-major layout, repeated on
+// the CPU with every index checked: lane rr of chain q takes row rr; its
+// external entries are the chain's stream at q*emax from the prefix of the
+// external counts of the rows before it (L) or after it (U), its in-chain
+// entries start at the descriptor's offset (ibase, high half of .y) plus the
+// same prefix of the in-chain counts; the recurrence runs bs - 1 steps in
+// lockstep over the chain's lanes, a step's column broadcast from its lane
+// (U: the value times the inverted diagonal), each lane subtracting it when
+// the column's bit is in its mask.
+template <typename VT>
+int emulate_rl(int N, const VT *val, const int *cind, const int *rptr, int upper, const int *cptr, int cnum, int bs,
+               const VT *x, VT *y, char *err, int errlen)
+{
+    auto fail = [&](const std::string &m) {
+        std::snprintf(err, errlen, "%s", m.c_str());
+        return 1;
+    };
+    try {
+        std::vector<WfColour> colours;
+        std::vector<int> colour_of(N);
+        for (int k = 0; k < cnum; k++) {
+            const int c = upper ? cnum - 1 - k : k;
+            colours.push_back({cptr[c] * bs, cptr[c + 1] * bs});
+            for (int p = cptr[c] * bs; p < cptr[c + 1] * bs; p++) colour_of[p] = k;
+        }
+        WfLayout<VT> L;
+        if (!make_wf_layout(L, upper != 0, N, val, cind, rptr, colours, bs, colour_of.data(), (size_t)1 << 30,
+                            nullptr, true))
+            return fail("layout does not fit");
+        std::vector<int> done(N, 0);
+        std::vector<VT> yy(x, x + N);
+        std::vector<int> fin;  // rows the current colour finishes: readable once it ends
+        for (size_t col = 0; col + 1 < L.colour_groups.size(); col++) {
+            for (int g = L.colour_groups[col]; g < L.colour_groups[col + 1]; g++) {
+                const WfGroup d = L.groups[g];
+                if (d.emax > 0 && d.emax % 2 == 0) return fail("chain-major stride not odd");
+                const size_t slots = (size_t)d.emax + d.imax;
+                if ((size_t)d.off + slots * 32 > L.col.size()) return fail("block beyond the layout");
+                const int *cw = L.col.data() + d.off;
+                const VT *vw = L.val.data() + d.off;
+                for (int q = 0; q < d.nchains; q++) {
+                    const int2 cd = L.chains[(size_t)g * 32 + q];
+                    const int r0 = cd.x, ibase = (int)((unsigned)cd.y >> 16);
+                    const unsigned char *cq = L.counts.data() + ((size_t)g * 32 + q) * 2 * bs;
+                    std::vector<VT> tt(bs), sc(bs), di(bs);
+                    std::vector<int> at(bs), left(bs);
+                    std::vector<uint32_t> mask(bs, 0);
+                    for (int rr = 0; rr < bs; rr++) {
+                        int eo = 0, io = 0;
+                        for (int r = 0; r < bs; r++)
+                            if (upper ? r > rr : r < rr) {
+                                eo += cq[r];
+                                io += cq[bs + r];
+                            }
+                        const int ne = cq[rr];
+                        left[rr] = cq[bs + rr];
+                        VT t = yy[r0 + rr];
+                        for (int k = 0; k < ne; k++) {
+                            const int e = eo + k;
+                            if (e >= d.emax) return fail("external entry beyond the chain's stream");
+                            const size_t idx = (size_t)q * d.emax + e;
+                            const int w = cw[idx];
+                            const int c = w & kColMask, r = (int)((unsigned)w >> kColBits);
+                            if (r != rr) return fail("external entry of another row");
+                            if (c < 0 || c >= N) return fail("gather out of range");
+                            if (!done[c]) return fail("gather of an unfinished row");
+                            t -= vw[idx] * yy[c];
+                        }
+                        at[rr] = ibase + io;
+                        for (int k = 0; k < left[rr]; k++) {
+                            const size_t idx = (size_t)d.emax * 32 + at[rr] + k;
+                            if (idx >= slots * 32) return fail("in-chain entry beyond the block");
+                            const int w = cw[idx];
+                            if ((w >> 8) != rr) return fail("in-chain entry of another row");
+                            const int c = w & 255;
+                            if (c < 0 || c >= bs || (upper ? c <= rr : c >= rr)) return fail("in-chain column out of order");
+                            mask[rr] |= 1u << c;
+                        }
+                        tt[rr] = t;
+                        di[rr] = upper ? L.dinv[r0 + rr] : VT(1);
+                        sc[rr] = tt[rr] * di[rr];
+                    }
+                    const int end_ib = ibase + [&] {
+                        int s = 0;
+                        for (int r = 0; r < bs; r++) s += cq[bs + r];
+                        return s;
+                    }();
+                    for (int s = 0; s < bs - 1; s++) {
+                        const int c = upper ? bs - 1 - s : s;
+                        const VT yc = upper ? sc[c] : tt[c];
+                        for (int rr = 0; rr < bs; rr++) {
+                            if (!(mask[rr] & (1u << c))) continue;
+                            if (at[rr] >= end_ib) return fail("in-chain entries of the next chain");
+                            tt[rr] -= vw[(size_t)d.emax * 32 + at[rr]] * yc;
+                            at[rr]++;
+                            if (upper) sc[rr] = tt[rr] * di[rr];
+                        }
+                    }
+                    for (int rr = 0; rr < bs; rr++) {
+                        int io = 0;
+                        for (int r = 0; r < bs; r++)
+                            if (upper ? r > rr : r < rr) io += cq[bs + r];
+                        if (at[rr] != ibase + io + left[rr]) return fail("in-chain entries left unused");
+                        yy[r0 + rr] = upper ? sc[rr] : tt[rr];
+                        fin.push_back(r0 + rr);
+                    }
+                }
+            }
+            // the groups of a colour run at once: its rows are readable when it ends
+            for (int r : fin) done[r] = 1;
+            fin.clear();
+        }
+        std::memcpy(y, yy.data(), sizeof(VT) * N);
+        return 0;
+    } catch (const std::exception &ex) {
+        return fail(ex.what());
+    }
+}
+
 extern "C" int wf_emulate_d(int N, const double *val, const int *cind, const int *rptr, int upper, const int *cptr,
                             int cnum, int bs, const double *x, double *y, char *err, int errlen)
 {
@@ -317,4 +437,16 @@ extern "C" int wf_cp_schedule_d(int N, const double *val, const int *cind, const
                                 const int *cptr, int cnum, int bs, int grid, char *err, int errlen)
 {
     return cp_schedule<double>(N, val, cind, rptr, upper, cptr, cnum, bs, grid, err, errlen);
+}
+
+extern "C" int wf_emulate_rl_d(int N, const double *val, const int *cind, const int *rptr, int upper, const int *cptr,
+                               int cnum, int bs, const double *x, double *y, char *err, int errlen)
+{
+    return emulate_rl<double>(N, val, cind, rptr, upper, cptr, cnum, bs, x, y, err, errlen);
+}
+
+extern "C" int wf_emulate_rl_s(int N, const float *val, const int *cind, const int *rptr, int upper, const int *cptr,
+                               int cnum, int bs, const float *x, float *y, char *err, int errlen)
+{
+    return emulate_rl<float>(N, val, cind, rptr, upper, cptr, cnum, bs, x, y, err, errlen);
 }

@@ -35,7 +35,7 @@ def emu(tmp_path_factory):
         f.restype = C.c_int
         f.argtypes = [C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_char_p,
                                                       C.c_int]
-    for name in ("wf_emulate_d", "wf_emulate_s"):
+    for name in ("wf_emulate_d", "wf_emulate_s", "wf_emulate_rl_d", "wf_emulate_rl_s"):
         f = getattr(lib, name)
         f.restype = C.c_int
         f.argtypes = [C.c_int] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
@@ -47,11 +47,14 @@ def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def _run(emu, F, upper, sc, nc, bs, x):
+def _run(emu, F, upper, sc, nc, bs, x, rl=False):
     T = F.val.dtype
     y = np.zeros_like(x)
     err = C.create_string_buffer(256)
-    f = emu.wf_emulate_s if T == np.float32 else emu.wf_emulate_d
+    if rl:
+        f = emu.wf_emulate_rl_s if T == np.float32 else emu.wf_emulate_rl_d
+    else:
+        f = emu.wf_emulate_s if T == np.float32 else emu.wf_emulate_d
     keep = [np.ascontiguousarray(a) for a in (F.val, F.cind, F.rptr, np.asarray(sc, np.int32), x)]
     rc = f(F.n, _p(keep[0]), _p(keep[1]), _p(keep[2]), int(upper), _p(keep[3]), nc, bs, _p(keep[4]), _p(y), err, 256)
     assert rc == 0, err.value.decode()
@@ -85,6 +88,38 @@ def test_emulated_dataflow_sweep_matches_the_oracle(emu, port, kind, n, bs):
     t32 = _run(emu, U32, True, sc, nc, bs, _run(emu, L32, False, sc, nc, bs, v32))
     want32 = port.ilu_apply(L32, U32, v32, dtype=np.float32)
     assert np.max(np.abs(t32 - want32)) <= 1e-5 * np.max(np.abs(want32))
+
+
+@pytest.mark.parametrize("kind,n,bs", CASES)
+def test_emulated_row_per_lane_sweep_matches_the_oracle(emu, port, kind, n, bs):
+    """The chain-major layout and the row-per-lane kernel's accesses
+    (k_sweep_rl: chain streams at q*emax, in-chain offsets from the chain
+    descriptor, lane-scan offsets, bs - 1 lockstep recurrence steps with U's
+    scaled broadcast), repeated on the CPU with every index checked and rows of
+    a colour readable only after the colour; the result equals the oracle's
+    sequential sweep bit for bit, FP64 and FP32: each row subtracts the same
+    products in the same order (entries of earlier colours, then in-chain ones
+    in column order) and U scales by the same inverted diagonal."""
+    A = {"convdiff": lambda: P.convdiff3d(n, 0.5), "poisson": lambda: P.poisson2d(n),
+         "vardiff": lambda: P.vardiff3d(n, 1.5, 4.0, 3)}[kind]()
+    if bs == 1:
+        nc, sc, LP, RP = S.GetAMCPermutation(A.cind, A.rptr, A.n, False)
+    else:
+        nc, sc, LP, RP = S.GetABMCPermutation(A.cind, A.rptr, A.n, bs, False, "connect")
+    Ar = S.Reordering(A, LP, RP)
+    L_, U_, _ = S.Split(S.Ilu0(Ar), "L-DU", True)
+    v = np.random.default_rng(11).uniform(-1, 1, A.n)
+    tl = _run(emu, L_, False, sc, nc, bs, v, rl=True)
+    want_l = port.sptrsv(L_, v, False)
+    assert np.array_equal(tl, want_l)
+    t = _run(emu, U_, True, sc, nc, bs, want_l, rl=True)
+    want = port.sptrsv(U_, want_l, True)
+    assert np.array_equal(t, want)
+    L32, U32 = L_.astype(np.float32), U_.astype(np.float32)
+    v32 = v.astype(np.float32)
+    t32 = _run(emu, U32, True, sc, nc, bs, _run(emu, L32, False, sc, nc, bs, v32, rl=True), rl=True)
+    want32 = port.ilu_apply(L32, U32, v32, dtype=np.float32)
+    assert np.array_equal(t32, want32)
 
 
 def _levels(F, upper):
