@@ -784,8 +784,8 @@ void IluPlan<VT>::build(int N, const VT *lval, const int *lcind, const int *lrpt
     for (int k = cnum - 1; k >= 0; k--) bwd.push_back(fwd[k]);
     // AUTO, as measured on the 128^3 system: FP32 factors on compact chains
     // with the lanes of a chain holding its rows, one launch per colour
-    // (application 0.107 ms, against 0.139 ms with a lane per chain and 0.193
-    // ms on row slots), FP64 factors on row slots (0.301 ms against 0.354 ms
+    // (application 0.085 ms, against 0.139 ms with a lane per chain and 0.193
+    // ms on row slots), FP64 factors on row slots (0.303 ms against 0.318 ms
     // row-per-lane and 0.405 ms lane-per-chain). COLOURS: row slots; COMPACT:
     // compact chains per colour, a lane per chain; ROWS: a chain's rows in its
     // lanes; DATAFLOW: compact chains, one launch per sweep. A factor whose
