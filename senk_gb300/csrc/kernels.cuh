@@ -1639,10 +1639,14 @@ constexpr int rl_min_blocks(int bs, int r, int vbytes)
 // the row's value already in a register, and each lane stores its row; after
 // the staging wait no CTA barrier is needed. R = 2 (BS >= 2) halves the
 // threads of a group, for colours with more groups than one wave of R = 1
-// holds. Prologue, programmatic launch, early_x, gate and error handling as in
-// k_sweep_cc.
+// holds. Each lane reads its chains' descriptors itself (the chain-major
+// layout stores the chain's in-chain offset there) and finds its row's
+// offsets by one shuffle scan of the chain's counts. Prologue, programmatic
+// launch, early_x and gate as in k_sweep_cc; a staging wait that runs out sets
+// *status = 2 and its warp leaves (after a second bounded wait for the copy).
 template <typename VT, typename XT, int BS, bool UPPER, int R>
-__global__ void __launch_bounds__(BS * 32 / R, rl_min_blocks(BS, R, (int)(sizeof(VT) > sizeof(XT) ? sizeof(VT) : sizeof(XT))))
+__global__ void __launch_bounds__(BS * 32 / R,
+                                  rl_min_blocks(BS, R, (int)(sizeof(VT) > sizeof(XT) ? sizeof(VT) : sizeof(XT))))
 k_sweep_rl(const WfGroup *__restrict__ groups, int g0, const int2 *__restrict__ chains,
            const unsigned char *__restrict__ counts, const VT *__restrict__ val, const int *__restrict__ col,
            const VT *__restrict__ dinv, const XT *x, XT *y, const int *gate, int *status, int early_x)
